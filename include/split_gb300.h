@@ -1,0 +1,229 @@
+/*
+ * split_gb300.h - C ABI of the GB300-native segmentation hot path.
+ *
+ * Drop-in boundary for nitronoid/split's device entry points (k-means,
+ * connected components, label compression, small-segment merge, erosion,
+ * Sobel normals).  Every entry point:
+ *   - takes plain device pointers, sizes and a cudaStream_t (passed as void*);
+ *   - allocates nothing: all scratch comes from a caller-provided workspace
+ *     sized by the matching *_workspace_size query;
+ *   - is asynchronous on `stream` and never synchronises the host;
+ *   - returns a split_status for argument/launch errors.  Errors that only
+ *     the device can detect (a capacity overflow, an iteration cap) are
+ *     recorded in the workspace's status word and read back with
+ *     split_workspace_status();
+ *   - never throws, exits or spins without a bound.
+ *
+ * Layouts follow the reference (split/include/split/detail/internal.h:35-39,
+ * samples/src/main.cu:164-168): planar float features dim x n (row d holds
+ * dimension d of every pixel), row-major int32 label images, planar 3 x n
+ * float normals.  The packed layouts (RGB8 interleaved, float4 per pixel) are
+ * native extensions.
+ *
+ * A workspace must be zero-filled once before its first use (cudaMemset);
+ * every call leaves it ready for the next call.  Calls that share a
+ * workspace must be ordered on one stream.
+ */
+#ifndef SPLIT_GB300_H
+#define SPLIT_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+typedef enum split_status {
+  SPLIT_OK = 0,
+  SPLIT_ERR_INVALID = 1,       /* bad argument (null pointer, size, flag)   */
+  SPLIT_ERR_WORKSPACE = 2,     /* workspace too small or misaligned         */
+  SPLIT_ERR_NOT_CONVERGED = 3, /* a device loop reached its iteration cap   */
+  SPLIT_ERR_CUDA = 4,          /* a CUDA runtime call or launch failed      */
+  SPLIT_ERR_OVERFLOW = 5,      /* a device table ran out of capacity        */
+  SPLIT_ERR_TIMEOUT = 6,       /* a device-wide barrier wait hit its limit  */
+  SPLIT_ERR_UNSUPPORTED = 7    /* no GB300-class device / kernel image      */
+} split_status;
+
+/* ---- feature layouts --------------------------------------------------- */
+enum {
+  SPLIT_LAYOUT_PLANAR = 0, /* float, dim x n, row d = dimension d            */
+  SPLIT_LAYOUT_FLOAT4 = 1, /* float4 per pixel (r, g, b, unused)             */
+  SPLIT_LAYOUT_RGB8 = 2    /* uint8 r, g, b interleaved; value = byte / 255  */
+};
+/* For FLOAT4 and RGB8 layouts, dim is 3 (colour) or 5 (colour plus
+ * xy_scale * column and xy_scale * row, synthesised from the pixel index). */
+
+/* ---- label conventions / policies -------------------------------------- */
+enum {
+  SPLIT_LABEL_MIN_INDEX = 0, /* component label = its minimum linear index  */
+  SPLIT_LABEL_MAX_INDEX = 1  /* component label = its maximum linear index,
+                                the reference's fixed point                  */
+};
+enum {
+  SPLIT_MERGE_MOST_BOUNDARY = 0, /* join the neighbour sharing most edges   */
+  SPLIT_MERGE_REF_CHROMA = 1     /* the reference's nearest-chroma rule      */
+};
+
+const char* split_version(void);
+const char* split_status_string(int status);
+
+/* Reads (and clears) the device-side status word of a workspace after the
+ * work queued on `stream` completes.  Synchronises `stream`. */
+int split_workspace_status(void* workspace, void* stream, int* out_status);
+
+/* ======================================================================== */
+/* k-means                                                                  */
+/* ======================================================================== */
+
+/* Replaces split::device::kmeans::cluster_workspace
+ * (split/include/split/device/kmeans/cluster.cuh:46-47). */
+size_t split_kmeans_cluster_workspace_size(int64_t npoints, int nclusters,
+                                           int dim);
+
+/* Replaces split::device::kmeans::cluster (cluster.cuh:31-37,
+ * split/src/split/device/kmeans/cluster.cu:27-93).
+ * points: layout-dependent, see above; width: image width (pixels per row,
+ * used for the synthesised xy features; any value >= 1 otherwise).
+ * centroids: dim x nclusters planar, in/out.  labels: int32[npoints] out.
+ * Runs until max_iter iterations, or until |delta - old_delta| <= threshold
+ * where delta is the L2 shift of the centroid matrix (threshold < 0: exactly
+ * max_iter iterations).  The convergence test runs on the device; the number
+ * of iterations performed is written to *d_iterations (device int) if not
+ * null.  The returned labels are the assignment computed from the centroids
+ * of the final iteration's input, the returned centroids the update computed
+ * from those labels, as in the reference. */
+int split_kmeans_cluster(const void* points, int layout, int dim,
+                         int64_t npoints, int width, float xy_scale,
+                         float* centroids, int nclusters, int32_t* labels,
+                         void* workspace, size_t workspace_bytes, int max_iter,
+                         float threshold, int32_t* d_iterations, void* stream);
+
+/* Replaces split::device::kmeans::label_points_workspace (label.cuh:39-40). */
+size_t split_kmeans_assign_workspace_size(int64_t npoints, int nclusters);
+
+/* Replaces split::device::kmeans::label_points (label.cuh:27-31,
+ * label.cu:74-106): nearest centroid, squared distance accumulated in
+ * dimension order, ties to the lowest cluster index. */
+int split_kmeans_assign(const void* points, int layout, int dim,
+                        int64_t npoints, int width, float xy_scale,
+                        const float* centroids, int nclusters, int32_t* labels,
+                        void* workspace, size_t workspace_bytes, void* stream);
+
+/* Replaces split::device::kmeans::calculate_centroids_workspace
+ * (centroids.cuh:39-40). */
+size_t split_kmeans_update_workspace_size(int64_t npoints, int nclusters,
+                                          int dim);
+
+/* Replaces split::device::kmeans::calculate_centroids (centroids.cuh:26-30,
+ * centroids.cu:22-101): per-cluster mean of the member points, accumulated
+ * in FP32 in a fixed order (bit-reproducible).  A cluster with no members
+ * keeps its previous centroid (the reference shifts later slots instead).
+ * labels outside [0, nclusters) are ignored. */
+int split_kmeans_update(const int32_t* labels, const void* points, int layout,
+                        int dim, int64_t npoints, int width, float xy_scale,
+                        float* centroids, int nclusters, void* workspace,
+                        size_t workspace_bytes, void* stream);
+
+/* Replaces split::device::kmeans::propagate_centroids (propagation.cuh:23-26,
+ * propagation.cu:9-24): out[d * npoints + i] = centroids[d * nclusters +
+ * labels[i]] for d < dim (planar output). */
+int split_kmeans_propagate(const int32_t* labels, int64_t npoints,
+                           const float* centroids, int nclusters, int dim,
+                           float* out, void* stream);
+
+/* ======================================================================== */
+/* connected components / label compression                                 */
+/* ======================================================================== */
+
+/* Replaces the temp-size contract of split::device::ccl::connected_components
+ * (connected_components.cuh:25-29), which allocates internally
+ * (connected_components.cu:93-94, 140-142). */
+size_t split_ccl_workspace_size(int width, int height);
+
+/* Replaces split::device::ccl::connected_components (connected_components.cuh:
+ * 25-29, connected_components.cu:80-181).  labels_in: row-major int32 image
+ * (any values; equality defines the regions); labels_out: int32[w*h].
+ * connectivity: 4 (reference) or 8.  convention: SPLIT_LABEL_MIN_INDEX or
+ * SPLIT_LABEL_MAX_INDEX (the reference's converged labels).
+ * d_sizes: optional int32[w*h]; if not null, d_sizes[root] receives the pixel
+ * count of the component labelled `root` (entries at non-label indices are
+ * left unspecified).  Always converges (union-find); the reference's
+ * i_max_iterations cap has no counterpart. */
+int split_ccl(const int32_t* labels_in, int width, int height,
+              int connectivity, int convention, int32_t* labels_out,
+              int32_t* d_sizes, void* workspace, size_t workspace_bytes,
+              void* stream);
+
+/* Replaces split::device::ccl::compress_labels (compress_labels.cuh:21-23,
+ * compress_labels.cu:10-35): labels (in place) become their rank among the
+ * distinct values.  Values must lie in [-1, n).  The number of distinct
+ * labels is written to *d_count (device int). */
+size_t split_compress_labels_workspace_size(int64_t n);
+int split_compress_labels(int32_t* labels, int64_t n, int32_t* d_count,
+                          void* workspace, size_t workspace_bytes,
+                          void* stream);
+
+/* ======================================================================== */
+/* small-segment merge                                                      */
+/* ======================================================================== */
+
+/* Replaces split::device::ccl::merge_small_segments_workspace
+ * (merge_small_segments.cuh:21-22). */
+size_t split_merge_small_workspace_size(int width, int height);
+
+/* Replaces split::device::ccl::merge_small_segments (merge_small_segments.cuh:
+ * 15-19, merge_small_segments.cu:92-196).  labels (in/out): segment ids in
+ * [0, w*h).  Segments smaller than P join one 8-adjacent neighbour chosen by
+ * `policy` (SPLIT_MERGE_MOST_BOUNDARY: most shared 8-neighbour edges, ties to
+ * the lowest id; SPLIT_MERGE_REF_CHROMA: the reference's nearest mean-chroma
+ * rule, chroma = planar 2 x n float, only row 0 read as in the reference).
+ * Mutual pairs keep the larger id; chains resolve to their end.  Output ids
+ * are input ids (not compressed).  d_sizes: optional per-segment pixel counts
+ * indexed by segment id (as produced by split_ccl); null = computed here. */
+int split_merge_small(int32_t* labels, int width, int height, int P,
+                      int policy, const float* chroma, const int32_t* d_sizes,
+                      void* workspace, size_t workspace_bytes, void* stream);
+
+/* ======================================================================== */
+/* erosion / normals / feature preparation                                  */
+/* ======================================================================== */
+
+/* Replaces split::device::morph::erode (erode.cuh:16-18, erode.cu:139-159):
+ * square (2r+1)^2 erosion of every label's mask, image border = background,
+ * eroded pixels = -1.  in and out must not overlap; r in [1, 16]. */
+int split_erode(const int32_t* labels_in, int32_t* labels_out, int width,
+                int height, int radius, void* stream);
+
+/* Erosion of merged labels: out = erode(map[labels_in]) where map is the
+ * segment map left in `merge_workspace` by the last split_merge_small call on
+ * the same labels (fused relabel + erosion; labels_in is then the pre-merge
+ * image). */
+int split_erode_mapped(const int32_t* labels_in, int32_t* labels_out,
+                       int width, int height, int radius,
+                       const void* merge_workspace, void* stream);
+
+/* Replaces split::device::sfs::sobel_normals (sobel_normals.cuh:17-20,
+ * sobel_normals.cu:86-119): heights row-major float[h*w] -> planar 3 x n
+ * float normals, n = normalize(Gx, Gy, 1 / max(0.001, depth)), z >= 0. */
+int split_sobel_normals(const float* heights, int width, int height,
+                        float depth, float* normals, void* stream);
+
+/* Normals from an RGB8 image: heights = luminance L* / 100 (fused, the
+ * luminance plane is never written). */
+int split_sobel_normals_rgb8(const uint8_t* rgb, int width, int height,
+                             float depth, float* normals, void* stream);
+
+/* Feature preparation (samples/src/main.cu:164-223): RGB8 interleaved ->
+ * float4 (r, g, b, 0) / 255 (optional) and luminance L* / 100 of the
+ * channels clamped to >= 1/255 (optional, split/include/split/device/color/
+ * detail/conversion.inl:8-64). */
+int split_pack_rgb8(const uint8_t* rgb, int64_t npixels, float* features4,
+                    float* luminance, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SPLIT_GB300_H */

@@ -1,0 +1,149 @@
+"""ORACLE - test infrastructure only.
+
+numpy wrappers over oracle/oracle.c, the CPU restatement of the reference's
+segmentation hot path (see that file for the per-function reference
+citations).  Imported by tests/, by __graft_entry__.smoke() and by bench.py's
+cpu_baseline leg as the checker; the product library never uses it.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_lib = None
+
+
+def _load():
+    global _lib
+    if _lib is None:
+        import sys
+        sys.path.insert(0, os.path.dirname(_HERE))
+        from split_gb300 import build as b
+        path = b.build_oracle()
+        lib = C.CDLL(path)
+        vp, i32, i64, f32 = C.c_void_p, C.c_int, C.c_int64, C.c_float
+        sigs = {
+            "orc_kmeans_assign_f32": (None, [vp, i32, i64, vp, i32, vp]),
+            "orc_kmeans_assign_f64": (None, [vp, i32, i64, vp, i32, vp, vp, vp]),
+            "orc_kmeans_update_f64": (None, [vp, vp, i32, i64, vp, i32, vp, vp]),
+            "orc_ccl": (i32, [vp, i32, i32, i32, i32, vp]),
+            "orc_compress_labels": (i64, [vp, i64]),
+            "orc_merge_small": (i32, [vp, i32, i32, i32, i32, vp, vp]),
+            "orc_erode": (i32, [vp, i32, i32, i32, vp]),
+            "orc_sobel_normals_f64": (i32, [vp, i32, i32, f32, vp]),
+            "orc_luminance_f64": (None, [vp, i64, vp]),
+        }
+        for name, (res, args) in sigs.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = lib
+    return _lib
+
+
+def _p(a):
+    return None if a is None else C.c_void_p(a.ctypes.data)
+
+
+def _c(a, dtype):
+    return np.ascontiguousarray(a, dtype=dtype)
+
+
+def kmeans_assign_f32(points: np.ndarray, centroids: np.ndarray) -> np.ndarray:
+    """points (D, N), centroids (D, K) float32 -> labels (N,) int32."""
+    p, c = _c(points, np.float32), _c(centroids, np.float32)
+    out = np.empty(p.shape[1], dtype=np.int32)
+    _load().orc_kmeans_assign_f32(_p(p), p.shape[0], p.shape[1], _p(c), c.shape[1], _p(out))
+    return out
+
+
+def kmeans_assign_f64(points: np.ndarray, centroids: np.ndarray):
+    """-> (labels, best distance, second-best distance) in FP64."""
+    p, c = _c(points, np.float32), _c(centroids, np.float32)
+    n = p.shape[1]
+    lab = np.empty(n, dtype=np.int32)
+    d1 = np.empty(n, dtype=np.float64)
+    d2 = np.empty(n, dtype=np.float64)
+    _load().orc_kmeans_assign_f64(_p(p), p.shape[0], n, _p(c), c.shape[1], _p(lab), _p(d1),
+                                  _p(d2))
+    return lab, d1, d2
+
+
+def kmeans_update_f64(labels: np.ndarray, points: np.ndarray, centroids_in: np.ndarray):
+    """-> (centroids (D, K) float64, counts (K,) int64); empty clusters keep
+    their input centroid."""
+    lab, p, c = _c(labels, np.int32), _c(points, np.float32), _c(centroids_in, np.float32)
+    d, k = c.shape
+    out = np.empty((d, k), dtype=np.float64)
+    cnt = np.empty(k, dtype=np.int64)
+    _load().orc_kmeans_update_f64(_p(lab), _p(p), d, p.shape[1], _p(c), k, _p(out), _p(cnt))
+    return out, cnt
+
+
+def ccl(labels: np.ndarray, connectivity: int = 4, convention: int = 0) -> np.ndarray:
+    """(H, W) int32 -> (H, W) int32 component labels (0: min index, 1: max)."""
+    a = _c(labels, np.int32)
+    h, w = a.shape
+    out = np.empty_like(a)
+    rc = _load().orc_ccl(_p(a), w, h, connectivity, convention, _p(out))
+    if rc:
+        raise RuntimeError(f"orc_ccl failed ({rc})")
+    return out
+
+
+def compress_labels(labels: np.ndarray):
+    a = _c(labels, np.int32).copy()
+    n = _load().orc_compress_labels(_p(a), a.size)
+    return a, int(n)
+
+
+def merge_small(labels: np.ndarray, P: int, policy: int = 0,
+                chroma: np.ndarray | None = None) -> np.ndarray:
+    """(H, W) segment ids in [0, H*W) -> merged ids (policy 0 most boundary,
+    1 reference chroma on chroma row 0)."""
+    a = _c(labels, np.int32)
+    h, w = a.shape
+    ch = None if chroma is None else _c(chroma, np.float32).reshape(-1)
+    out = np.empty_like(a)
+    rc = _load().orc_merge_small(_p(a), w, h, P, policy, _p(ch), _p(out))
+    if rc:
+        raise RuntimeError(f"orc_merge_small failed ({rc})")
+    return out
+
+
+def erode(labels: np.ndarray, radius: int = 1) -> np.ndarray:
+    a = _c(labels, np.int32)
+    h, w = a.shape
+    out = np.empty_like(a)
+    rc = _load().orc_erode(_p(a), w, h, radius, _p(out))
+    if rc:
+        raise RuntimeError(f"orc_erode failed ({rc})")
+    return out
+
+
+def sobel_normals_f64(heights: np.ndarray, depth: float = 1.0) -> np.ndarray:
+    """(H, W) float32 -> (3, H*W) float64 normals."""
+    a = _c(heights, np.float32)
+    h, w = a.shape
+    out = np.empty((3, h * w), dtype=np.float64)
+    _load().orc_sobel_normals_f64(_p(a), w, h, depth, _p(out))
+    return out
+
+
+def luminance_f64(rgb: np.ndarray) -> np.ndarray:
+    """RGB8 (..., 3) -> L*/100 (N,) float64."""
+    a = _c(rgb, np.uint8)
+    n = a.size // 3
+    out = np.empty(n, dtype=np.float64)
+    _load().orc_luminance_f64(_p(a), n, _p(out))
+    return out
+
+
+def canonical(labels: np.ndarray) -> np.ndarray:
+    """Relabel a partition by the minimum linear index of each label class."""
+    flat = np.asarray(labels).reshape(-1)
+    _, first, inv = np.unique(flat, return_index=True, return_inverse=True)
+    return first[inv].reshape(np.asarray(labels).shape).astype(np.int64)

@@ -1,0 +1,99 @@
+"""ctypes bindings of libsplit_gb300.so (the C ABI declared in include/split_gb300.h
+and include/split_synth.h).
+
+The library is built in-tree by ``split_gb300.build``.  Loading fails loudly when
+it is missing: there is no fallback implementation of any entry point.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+from . import build as _build
+
+_lib = None
+
+# status codes (split_status in include/split_gb300.h)
+OK, ERR_INVALID, ERR_WORKSPACE, ERR_NOT_CONVERGED, ERR_CUDA, ERR_OVERFLOW, ERR_TIMEOUT, \
+    ERR_UNSUPPORTED = range(8)
+LAYOUT_PLANAR, LAYOUT_FLOAT4, LAYOUT_RGB8 = 0, 1, 2
+LABEL_MIN_INDEX, LABEL_MAX_INDEX = 0, 1
+MERGE_MOST_BOUNDARY, MERGE_REF_CHROMA = 0, 1
+
+_vp, _sz, _i32, _i64, _f32, _u64 = C.c_void_p, C.c_size_t, C.c_int, C.c_int64, C.c_float, \
+    C.c_uint64
+
+_SIGS = {
+    "split_version": (C.c_char_p, []),
+    "split_status_string": (C.c_char_p, [_i32]),
+    "split_workspace_status": (_i32, [_vp, _vp, C.POINTER(C.c_int)]),
+    "split_kmeans_cluster_workspace_size": (_sz, [_i64, _i32, _i32]),
+    "split_kmeans_cluster": (_i32, [_vp, _i32, _i32, _i64, _i32, _f32, _vp, _i32, _vp, _vp, _sz,
+                                    _i32, _f32, _vp, _vp]),
+    "split_kmeans_assign_workspace_size": (_sz, [_i64, _i32]),
+    "split_kmeans_assign": (_i32, [_vp, _i32, _i32, _i64, _i32, _f32, _vp, _i32, _vp, _vp, _sz,
+                                   _vp]),
+    "split_kmeans_update_workspace_size": (_sz, [_i64, _i32, _i32]),
+    "split_kmeans_update": (_i32, [_vp, _vp, _i32, _i32, _i64, _i32, _f32, _vp, _i32, _vp, _sz,
+                                   _vp]),
+    "split_kmeans_propagate": (_i32, [_vp, _i64, _vp, _i32, _i32, _vp, _vp]),
+    "split_ccl_workspace_size": (_sz, [_i32, _i32]),
+    "split_ccl": (_i32, [_vp, _i32, _i32, _i32, _i32, _vp, _vp, _vp, _sz, _vp]),
+    "split_compress_labels_workspace_size": (_sz, [_i64]),
+    "split_compress_labels": (_i32, [_vp, _i64, _vp, _vp, _sz, _vp]),
+    "split_merge_small_workspace_size": (_sz, [_i32, _i32]),
+    "split_merge_small": (_i32, [_vp, _i32, _i32, _i32, _i32, _vp, _vp, _vp, _sz, _vp]),
+    "split_erode": (_i32, [_vp, _vp, _i32, _i32, _i32, _vp]),
+    "split_erode_mapped": (_i32, [_vp, _vp, _i32, _i32, _i32, _vp, _vp]),
+    "split_sobel_normals": (_i32, [_vp, _i32, _i32, _f32, _vp, _vp]),
+    "split_sobel_normals_rgb8": (_i32, [_vp, _i32, _i32, _f32, _vp, _vp]),
+    "split_pack_rgb8": (_i32, [_vp, _i64, _vp, _vp, _vp]),
+    "split_synth_voronoi_rgb8": (_i32, [_u64, _i32, _i32, _i32, _i32, _i32, C.c_double, _vp]),
+    "split_synth_pick_centroids": (_i32, [_u64, _vp, _i32, _i32, _i32, _i32, _f32, _vp]),
+    "split_synth_feature_u8": (_f32, [C.c_uint8]),
+    "split_synth_maze_labels": (_i32, [_u64, _i32, _i32, _vp]),
+}
+
+
+class SplitError(RuntimeError):
+    def __init__(self, status: int, where: str):
+        self.status = status
+        super().__init__(f"{where}: {status_string(status)} (status {status})")
+
+
+def lib_path() -> str:
+    return _build.LIB
+
+
+def load(build_if_missing: bool = False):
+    """Load the native library (optionally building it first)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = lib_path()
+    if not os.path.exists(path):
+        if not build_if_missing:
+            raise ImportError(
+                f"{path} is missing: build it with `python -c 'import __graft_entry__ as g; "
+                "g.build()'` (or python split_gb300/build.py)")
+        _build.build_library()
+    lib = C.CDLL(path)
+    for name, (res, args) in _SIGS.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def exported_symbols() -> list[str]:
+    return list(_SIGS)
+
+
+def status_string(status: int) -> str:
+    return load().split_status_string(status).decode()
+
+
+def check(status: int, where: str) -> None:
+    if status != OK:
+        raise SplitError(status, where)

@@ -1,0 +1,62 @@
+// Library-level entry points: version, status strings, device queries and the
+// workspace status word.
+#include <mutex>
+
+#include "common.cuh"
+
+namespace sg {
+
+int device_info(DeviceInfo* out) {
+  static std::mutex mu;
+  static DeviceInfo cache[64];
+  static bool valid[64] = {false};
+  int dev = 0;
+  SG_CUDA_TRY(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) return SPLIT_ERR_CUDA;
+  std::lock_guard<std::mutex> lock(mu);
+  if (!valid[dev]) {
+    DeviceInfo d;
+    d.device = dev;
+    SG_CUDA_TRY(cudaDeviceGetAttribute(&d.sm_count, cudaDevAttrMultiProcessorCount, dev));
+    SG_CUDA_TRY(cudaDeviceGetAttribute(&d.max_smem_optin,
+                                       cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    int major = 0;
+    SG_CUDA_TRY(cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev));
+    if (major < 10) return SPLIT_ERR_UNSUPPORTED;
+    cache[dev] = d;
+    valid[dev] = true;
+  }
+  *out = cache[dev];
+  return SPLIT_OK;
+}
+
+}  // namespace sg
+
+using namespace sg;
+
+extern "C" const char* split_version(void) { return "split_gb300 0.1.0 (sm_103a)"; }
+
+extern "C" const char* split_status_string(int status) {
+  switch (status) {
+    case SPLIT_OK: return "ok";
+    case SPLIT_ERR_INVALID: return "invalid argument";
+    case SPLIT_ERR_WORKSPACE: return "workspace too small or misaligned";
+    case SPLIT_ERR_NOT_CONVERGED: return "device loop reached its iteration cap";
+    case SPLIT_ERR_CUDA: return "CUDA runtime error";
+    case SPLIT_ERR_OVERFLOW: return "device table capacity exceeded";
+    case SPLIT_ERR_TIMEOUT: return "device-wide barrier wait timed out";
+    case SPLIT_ERR_UNSUPPORTED: return "unsupported device";
+    default: return "unknown status";
+  }
+}
+
+extern "C" int split_workspace_status(void* workspace, void* stream, int* out_status) {
+  if (!workspace || !out_status) return SPLIT_ERR_INVALID;
+  cudaStream_t st = as_stream(stream);
+  int h = 0;
+  SG_CUDA_TRY(cudaMemcpyAsync(&h, workspace, sizeof(int), cudaMemcpyDeviceToHost, st));
+  SG_CUDA_TRY(cudaStreamSynchronize(st));
+  SG_CUDA_TRY(cudaMemsetAsync(workspace, 0, sizeof(int), st));
+  *out_status = h;
+  return SPLIT_OK;
+}

@@ -1,0 +1,126 @@
+// Shared helpers of the sm_103a kernels: status handling, workspace carving,
+// the bounded device-wide barrier and small device utilities.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stddef.h>
+
+#include <cuda/atomic>
+
+#include "../../include/split_gb300.h"
+
+namespace sg {
+
+// ---------------------------------------------------------------------------
+// host-side status helpers
+// ---------------------------------------------------------------------------
+#define SG_CUDA_TRY(expr)                          \
+  do {                                             \
+    cudaError_t e_ = (expr);                       \
+    if (e_ != cudaSuccess) return SPLIT_ERR_CUDA;  \
+  } while (0)
+
+#define SG_TRY(expr)              \
+  do {                            \
+    int s_ = (expr);              \
+    if (s_ != SPLIT_OK) return s_; \
+  } while (0)
+
+inline int launch_status() {
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaErrorNoKernelImageForDevice || e == cudaErrorInvalidDeviceFunction)
+    return SPLIT_ERR_UNSUPPORTED;
+  return e == cudaSuccess ? SPLIT_OK : SPLIT_ERR_CUDA;
+}
+
+inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
+
+// Per-device properties cached after the first query.
+struct DeviceInfo {
+  int device;
+  int sm_count;
+  int max_smem_optin;
+};
+int device_info(DeviceInfo* out);
+
+// ---------------------------------------------------------------------------
+// workspace layout
+// ---------------------------------------------------------------------------
+// Every workspace starts with this header.  `status` holds the first error a
+// device detected (0 = none).  The barrier words back the device-wide barrier
+// of persistent kernels; `count` returns to zero after every barrier.
+struct WsHeader {
+  int status;
+  unsigned barrier_count;
+  unsigned barrier_gen;
+  unsigned work_counter[2];
+  int pad[59];
+};
+static_assert(sizeof(WsHeader) == 256, "header is one 256-byte line");
+
+// Bump allocator over a caller workspace; with base == nullptr it only
+// measures, so size queries and carving share one code path.
+struct Carver {
+  char* base;
+  size_t off;
+  explicit Carver(void* b) : base(static_cast<char*>(b)), off(0) {}
+  template <class T>
+  T* take(size_t count) {
+    off = (off + 255) & ~size_t(255);
+    T* p = base ? reinterpret_cast<T*>(base + off) : nullptr;
+    off += count * sizeof(T);
+    return p;
+  }
+  size_t size() const { return (off + 255) & ~size_t(255); }
+};
+
+// ---------------------------------------------------------------------------
+// device helpers
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void set_status(int* st, int code) {
+  atomicCAS(st, 0, code);
+}
+
+// Iteration limit of every spin wait (about a second with the back-off below).
+constexpr unsigned kSpinLimit = 1u << 24;
+
+// Device-wide barrier for a cooperative (co-resident) grid.  Sense is carried
+// by a generation counter.  A wait that exceeds kSpinLimit records
+// SPLIT_ERR_TIMEOUT and returns false; callers then leave the kernel.
+__device__ __forceinline__ bool grid_barrier(WsHeader* h) {
+  __syncthreads();
+  __shared__ int ok;
+  if (threadIdx.x == 0) {
+    cuda::atomic_ref<unsigned, cuda::thread_scope_device> gen(h->barrier_gen);
+    cuda::atomic_ref<unsigned, cuda::thread_scope_device> cnt(h->barrier_count);
+    const unsigned nblocks = gridDim.x * gridDim.y * gridDim.z;
+    const unsigned g = gen.load(cuda::memory_order_relaxed);
+    ok = 1;
+    // acq_rel: publish this block's writes, observe the others' on release
+    const unsigned arrived = cnt.fetch_add(1, cuda::memory_order_acq_rel);
+    if (arrived == nblocks - 1) {
+      cnt.store(0, cuda::memory_order_relaxed);
+      gen.fetch_add(1, cuda::memory_order_release);
+    } else {
+      unsigned spins = 0;
+      while (gen.load(cuda::memory_order_acquire) == g) {
+        if (++spins > kSpinLimit) {
+          set_status(&h->status, SPLIT_ERR_TIMEOUT);
+          ok = 0;
+          break;
+        }
+        __nanosleep(64);
+      }
+    }
+    if (cuda::atomic_ref<int, cuda::thread_scope_device>(h->status).load(
+            cuda::memory_order_relaxed) == SPLIT_ERR_TIMEOUT)
+      ok = 0;
+  }
+  __syncthreads();
+  return ok != 0;
+}
+
+__device__ __forceinline__ int warp_lane() { return threadIdx.x & 31; }
+
+}  // namespace sg

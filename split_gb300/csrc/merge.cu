@@ -1,0 +1,351 @@
+// Small-segment merge: a boundary-histogram pass plus a relabel.
+//
+// Restates split/src/split/device/ccl/merge_small_segments.cu:92-196 with its
+// helpers segment_adjacency.cu:112-142 (8-neighbour edge set),
+// detail/fix_map_cycles.cuh:14-44 (mutual pairs keep the larger id) and
+// detail/map_until_converged.cuh:14-31 (every label follows its map chain to
+// the end).  Instead of materialising 16 ints per pixel of edges and radix
+// sorting them, pixels of small segments insert their (segment, neighbour
+// segment) pairs into a hash table with multiplicities; each pair then bids
+// for its segment with one 64-bit atomicMax:
+//   MOST_BOUNDARY: (edge count << 32) | ~neighbour      (most edges, lowest id)
+//   REF_CHROMA   : ~((bits(d2) << 32) | neighbour)       (least d2, lowest id)
+// and the winning pair writes the segment's map entry.
+//
+// Workspace state (kept clean between calls):
+//   table keys / counts / slot list   zero outside a call
+//   best[n]                            zero outside a call
+// Per-call arrays: size[n] (unless the caller passes component sizes),
+// map[n], fin[n] (final target of every small segment), sum[n] (chroma).
+#include "merge_state.cuh"
+
+namespace sg {
+namespace mrg {
+
+constexpr int kThreads = 256;
+constexpr int kProbeCap = 1 << 16;
+constexpr unsigned kChainCap = 1u << 24;
+
+struct Layout {
+  WsHeader* hdr;
+  State* state;
+  int32_t* size;
+  int32_t* map;
+  int32_t* fin;
+  unsigned long long* best;
+  double* sum;
+  unsigned long long* keys;
+  unsigned* counts;
+  int32_t* list;
+  int cap_log2;
+  size_t bytes;
+};
+
+inline int cap_log2_for(int64_t n) {
+  int l = 12;
+  while ((1ll << l) < n && l < 31) ++l;
+  return l;
+}
+
+inline Layout carve(void* ws, int64_t n) {
+  Carver c(ws);
+  Layout l;
+  l.hdr = c.take<WsHeader>(1);
+  l.state = c.take<State>(1);
+  l.size = c.take<int32_t>((size_t)n);
+  l.map = c.take<int32_t>((size_t)n);
+  l.fin = c.take<int32_t>((size_t)n);
+  l.best = c.take<unsigned long long>((size_t)n);
+  l.sum = c.take<double>((size_t)n);
+  l.cap_log2 = cap_log2_for(n);
+  const size_t cap = (size_t)1 << l.cap_log2;
+  l.keys = c.take<unsigned long long>(cap);
+  l.counts = c.take<unsigned>(cap);
+  l.list = c.take<int32_t>(cap);
+  l.bytes = c.size();
+  return l;
+}
+
+__device__ __forceinline__ unsigned long long pair_key(int s, int t) {
+  return (((unsigned long long)(unsigned)s << 32) | (unsigned)t) + 1ull;
+}
+__device__ __forceinline__ int key_s(unsigned long long k) { return (int)((k - 1ull) >> 32); }
+__device__ __forceinline__ int key_t(unsigned long long k) { return (int)(unsigned)((k - 1ull) & 0xffffffffull); }
+
+__device__ void insert(const Layout& L, int s, int t, unsigned m, int* status) {
+  const unsigned long long key = pair_key(s, t);
+  const unsigned mask = (1u << L.cap_log2) - 1u;
+  unsigned h = (unsigned)((key * 0x9E3779B97F4A7C15ull) >> (64 - L.cap_log2));
+  for (int probe = 0; probe < kProbeCap; ++probe, h = (h + 1) & mask) {
+    unsigned long long k = *(volatile unsigned long long*)(L.keys + h);
+    if (k == 0ull) {
+      k = atomicCAS(L.keys + h, 0ull, key);
+      if (k == 0ull) {
+        atomicAdd(L.counts + h, m);
+        const unsigned idx = atomicAdd(&L.state->list_count, 1u);
+        L.list[idx] = (int)h;
+        return;
+      }
+    }
+    if (k == key) {
+      atomicAdd(L.counts + h, m);
+      return;
+    }
+  }
+  set_status(status, SPLIT_ERR_OVERFLOW);
+}
+
+// sizes (generic path) and chroma sums; REF_CHROMA also notes whether the
+// labels were already sorted (merge_small_segments.cu:124-126, :192-195)
+__global__ void __launch_bounds__(kThreads)
+size_kernel(const int32_t* __restrict__ lab, int64_t n, Layout L, bool count_sizes,
+            const float* __restrict__ chroma, int* status) {
+  const unsigned full = 0xffffffffu;
+  for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < n;
+       base += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = base + threadIdx.x;
+    int s = -1;
+    if (i < n) {
+      s = __ldg(lab + i);
+      if (s < 0 || s >= n) {
+        set_status(status, SPLIT_ERR_INVALID);
+        s = -1;
+      } else if (chroma && i + 1 < n && __ldg(lab + i + 1) < s) {
+        L.state->unsorted = 1;
+      }
+    }
+    const unsigned peers = __match_any_sync(full, s);
+    const int leader = __ffs(peers) - 1;
+    if (count_sizes && s >= 0 && (threadIdx.x & 31) == leader) atomicAdd(L.size + s, __popc(peers));
+    if (chroma && s >= 0) atomicAdd(L.sum + s, (double)__ldg(chroma + i));
+  }
+}
+
+// boundary histogram of small segments
+__global__ void __launch_bounds__(kThreads)
+pair_kernel(const int32_t* __restrict__ lab, int W, int H, Layout L, const int32_t* sizes,
+            int P, int* status) {
+  const int64_t n = (int64_t)W * H;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int s = __ldg(lab + i);
+    if (s < 0 || s >= n) continue;
+    if (__ldg(sizes + s) >= P) continue;
+    L.fin[s] = s;
+    const int y = (int)(i / W), x = (int)(i - (int64_t)y * W);
+    int t[8];
+    int nt = 0;
+#pragma unroll
+    for (int d = 0; d < 8; ++d) {
+      const int dx = (d == 0 || d == 3 || d == 5) ? -1 : (d == 2 || d == 4 || d == 7) ? 1 : 0;
+      const int dy = d < 3 ? -1 : d > 4 ? 1 : 0;
+      const int nx = x + dx, ny = y + dy;
+      int v = -1;
+      if (nx >= 0 && ny >= 0 && nx < W && ny < H) v = __ldg(lab + (int64_t)ny * W + nx);
+      if (v >= n) {
+        set_status(status, SPLIT_ERR_INVALID);
+        v = -1;
+      }
+      if (v != s && v >= 0) t[nt++] = v;
+    }
+    for (int a = 0; a < nt; ++a) {
+      bool first = true;
+      unsigned m = 1;
+      for (int b = 0; b < a; ++b) first &= (t[b] != t[a]);
+      if (!first) continue;
+      for (int b = a + 1; b < nt; ++b) m += (t[b] == t[a]);
+      insert(L, s, t[a], m, status);
+    }
+  }
+}
+
+__device__ __forceinline__ float seg_mean(const Layout& L, const int32_t* sizes, int s) {
+  return (float)L.sum[s] / (float)__ldg(sizes + s);
+}
+
+__global__ void bid_kernel(Layout L, const int32_t* sizes, int policy) {
+  const unsigned cnt = *(volatile unsigned*)&L.state->list_count;
+  for (unsigned j = blockIdx.x * blockDim.x + threadIdx.x; j < cnt; j += gridDim.x * blockDim.x) {
+    const int h = L.list[j];
+    const unsigned long long k = L.keys[h];
+    const int s = key_s(k), t = key_t(k);
+    unsigned long long bid;
+    if (policy == SPLIT_MERGE_MOST_BOUNDARY) {
+      bid = ((unsigned long long)L.counts[h] << 32) | (unsigned)(0xffffffffu - (unsigned)t);
+    } else {
+      const float x = seg_mean(L, sizes, s) - seg_mean(L, sizes, t);
+      const float d2 = __fadd_rn(__fmul_rn(x, x), __fmul_rn(x, x));
+      bid = ~(((unsigned long long)__float_as_uint(d2) << 32) | (unsigned)t);
+    }
+    atomicMax(L.best + s, bid);
+  }
+}
+
+__device__ __forceinline__ int bid_target(unsigned long long b, int policy) {
+  if (policy == SPLIT_MERGE_MOST_BOUNDARY) return (int)(0xffffffffu - (unsigned)(b & 0xffffffffull));
+  return (int)(unsigned)((~b) & 0xffffffffull);
+}
+
+__global__ void decide_kernel(Layout L, int policy) {
+  const unsigned cnt = *(volatile unsigned*)&L.state->list_count;
+  for (unsigned j = blockIdx.x * blockDim.x + threadIdx.x; j < cnt; j += gridDim.x * blockDim.x) {
+    const unsigned long long k = L.keys[L.list[j]];
+    const int s = key_s(k), t = key_t(k);
+    if (bid_target(L.best[s], policy) == t) L.map[s] = t;
+  }
+}
+
+// next segment along the map: small segments with a winning neighbour move
+__device__ __forceinline__ int next_of(const Layout& L, const int32_t* sizes, int P, int r) {
+  if (__ldg(sizes + r) >= P) return r;
+  if (*(volatile unsigned long long*)(L.best + r) == 0ull) return r;
+  return *(volatile int*)(L.map + r);
+}
+
+// mutual pairs: the larger id keeps itself (fix_map_cycles.cuh:28-43)
+__global__ void cycle_kernel(Layout L, const int32_t* sizes, int P, int policy) {
+  const unsigned cnt = *(volatile unsigned*)&L.state->list_count;
+  for (unsigned j = blockIdx.x * blockDim.x + threadIdx.x; j < cnt; j += gridDim.x * blockDim.x) {
+    const unsigned long long k = L.keys[L.list[j]];
+    const int s = key_s(k), t = key_t(k);
+    if (bid_target(L.best[s], policy) != t) continue;
+    if (next_of(L, sizes, P, t) == s && s > t) *(volatile int*)(L.map + s) = s;
+  }
+}
+
+__global__ void resolve_kernel(Layout L, const int32_t* sizes, int P, int policy, int* status) {
+  const unsigned cnt = *(volatile unsigned*)&L.state->list_count;
+  for (unsigned j = blockIdx.x * blockDim.x + threadIdx.x; j < cnt; j += gridDim.x * blockDim.x) {
+    const unsigned long long k = L.keys[L.list[j]];
+    const int s = key_s(k), t = key_t(k);
+    if (bid_target(L.best[s], policy) != t) continue;
+    int r = s;
+    unsigned steps = 0;
+    for (;;) {
+      const int nx = next_of(L, sizes, P, r);
+      if (nx == r) break;
+      r = nx;
+      if (++steps > kChainCap) {
+        set_status(status, SPLIT_ERR_NOT_CONVERGED);
+        break;
+      }
+    }
+    L.fin[s] = r;
+  }
+}
+
+// return the table and the bids to zero
+__global__ void cleanup_kernel(Layout L) {
+  const unsigned cnt = *(volatile unsigned*)&L.state->list_count;
+  for (unsigned j = blockIdx.x * blockDim.x + threadIdx.x; j < cnt; j += gridDim.x * blockDim.x) {
+    const int h = L.list[j];
+    const unsigned long long k = L.keys[h];
+    L.best[key_s(k)] = 0ull;
+    L.keys[h] = 0ull;
+    L.counts[h] = 0u;
+  }
+}
+
+__global__ void relabel_kernel(int32_t* lab, int64_t n, const State* stp, const int32_t* fin) {
+  const State st = *stp;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    lab[i] = relabel(st, fin, lab[i]);
+}
+
+__global__ void set_state_kernel(State* st, const int32_t* sizes, int P, int policy, int cap_log2,
+                                 int n) {
+  st->n = n;
+  st->sizes = sizes;
+  st->P = P;
+  st->policy = policy;
+  st->unsorted = 0;
+  st->list_count = 0;
+  st->cap_log2 = cap_log2;
+}
+
+}  // namespace mrg
+
+int merge_view(const void* ws, int width, int height, MergeView* out) {
+  if (!ws || width < 1 || height < 1) return SPLIT_ERR_INVALID;
+  mrg::Layout l = mrg::carve(const_cast<void*>(ws), (int64_t)width * height);
+  out->state = l.state;
+  out->fin = l.fin;
+  return SPLIT_OK;
+}
+
+}  // namespace sg
+
+using namespace sg;
+
+extern "C" size_t split_merge_small_workspace_size(int width, int height) {
+  if (width < 1 || height < 1) return 0;
+  return mrg::carve(nullptr, (int64_t)width * height).bytes;
+}
+
+// Runs the decision passes; the caller's labels are relabelled unless
+// `relabel_labels` is false (the fused erosion relabels instead).
+static int merge_decide(int32_t* labels, int width, int height, int P, int policy,
+                        const float* chroma, const int32_t* d_sizes, void* workspace,
+                        size_t workspace_bytes, cudaStream_t st, bool relabel_labels) {
+  if (!labels || width < 1 || height < 1) return SPLIT_ERR_INVALID;
+  const int64_t n = (int64_t)width * height;
+  if (n > 0x7fffffffLL) return SPLIT_ERR_INVALID;
+  if (policy != SPLIT_MERGE_MOST_BOUNDARY && policy != SPLIT_MERGE_REF_CHROMA)
+    return SPLIT_ERR_INVALID;
+  if (policy == SPLIT_MERGE_REF_CHROMA && !chroma) return SPLIT_ERR_INVALID;
+  mrg::Layout l = mrg::carve(nullptr, n);
+  if (!workspace || workspace_bytes < l.bytes || (reinterpret_cast<uintptr_t>(workspace) & 255))
+    return SPLIT_ERR_WORKSPACE;
+  l = mrg::carve(workspace, n);
+  DeviceInfo di;
+  SG_TRY(device_info(&di));
+  int64_t blocks = (n + mrg::kThreads - 1) / mrg::kThreads;
+  if (blocks > (int64_t)di.sm_count * 8) blocks = (int64_t)di.sm_count * 8;
+  const int grid = (int)blocks;
+  const int32_t* sizes = d_sizes ? d_sizes : l.size;
+  const bool ref = policy == SPLIT_MERGE_REF_CHROMA;
+  mrg::set_state_kernel<<<1, 1, 0, st>>>(l.state, sizes, P, policy, l.cap_log2, (int)n);
+  SG_TRY(launch_status());
+  if (!d_sizes) SG_CUDA_TRY(cudaMemsetAsync(l.size, 0, sizeof(int32_t) * (size_t)n, st));
+  if (ref) SG_CUDA_TRY(cudaMemsetAsync(l.sum, 0, sizeof(double) * (size_t)n, st));
+  if (!d_sizes || ref) {
+    mrg::size_kernel<<<grid, mrg::kThreads, 0, st>>>(labels, n, l, !d_sizes,
+                                                      ref ? chroma : nullptr, &l.hdr->status);
+    SG_TRY(launch_status());
+  }
+  mrg::pair_kernel<<<grid, mrg::kThreads, 0, st>>>(labels, width, height, l, sizes, P,
+                                                    &l.hdr->status);
+  SG_TRY(launch_status());
+  mrg::bid_kernel<<<grid, mrg::kThreads, 0, st>>>(l, sizes, policy);
+  SG_TRY(launch_status());
+  mrg::decide_kernel<<<grid, mrg::kThreads, 0, st>>>(l, policy);
+  SG_TRY(launch_status());
+  mrg::cycle_kernel<<<grid, mrg::kThreads, 0, st>>>(l, sizes, P, policy);
+  SG_TRY(launch_status());
+  mrg::resolve_kernel<<<grid, mrg::kThreads, 0, st>>>(l, sizes, P, policy, &l.hdr->status);
+  SG_TRY(launch_status());
+  mrg::cleanup_kernel<<<grid, mrg::kThreads, 0, st>>>(l);
+  SG_TRY(launch_status());
+  if (relabel_labels) {
+    mrg::relabel_kernel<<<grid, mrg::kThreads, 0, st>>>(labels, n, l.state, l.fin);
+    SG_TRY(launch_status());
+  }
+  return SPLIT_OK;
+}
+
+extern "C" int split_merge_small(int32_t* labels, int width, int height, int P, int policy,
+                                 const float* chroma, const int32_t* d_sizes, void* workspace,
+                                 size_t workspace_bytes, void* stream) {
+  return merge_decide(labels, width, height, P, policy, chroma, d_sizes, workspace,
+                      workspace_bytes, as_stream(stream), true);
+}
+
+namespace sg {
+int merge_decide_only(const int32_t* labels, int width, int height, int P, int policy,
+                      const float* chroma, const int32_t* d_sizes, void* workspace,
+                      size_t workspace_bytes, cudaStream_t st) {
+  return merge_decide(const_cast<int32_t*>(labels), width, height, P, policy, chroma, d_sizes,
+                      workspace, workspace_bytes, st, false);
+}
+}  // namespace sg

@@ -1,0 +1,364 @@
+// 2-D stencils of the segmentation path, staged through shared memory by the
+// tensor memory accelerator (one cp.async.bulk.tensor tile + halo per block,
+// completion on an mbarrier), with a plain-load variant for buffers TMA cannot
+// address (row pitch not a multiple of 16 bytes, unaligned base):
+//   - square (2r+1)^2 label erosion, optionally fused with the merge relabel;
+//   - Sobel normals from a height map or straight from RGB8 (luminance L*/100
+//     computed in shared memory, never written);
+//   - RGB8 feature packing (float4 features, luminance).
+#include <math.h>
+
+#include "merge_state.cuh"
+#include "tma.cuh"
+
+namespace sg {
+
+static PFN_cuTensorMapEncodeTiled_v12000 tmap_encoder() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static bool tried = false;
+  if (!tried) {
+    tried = true;
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                         &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  }
+  return fn;
+}
+
+int make_tmap_2d(CUtensorMap* map, CUtensorMapDataType dtype, int elem_bytes, const void* base,
+                 uint64_t width, uint64_t height, uint64_t row_bytes, uint32_t box_w,
+                 uint32_t box_h) {
+  if ((reinterpret_cast<uintptr_t>(base) & 15) || (row_bytes & 15)) return SPLIT_ERR_INVALID;
+  if (box_w > 256 || box_h > 256 || (box_w * elem_bytes) % 16) return SPLIT_ERR_INVALID;
+  auto enc = tmap_encoder();
+  if (!enc) return SPLIT_ERR_UNSUPPORTED;
+  cuuint64_t dims[2] = {width, height};
+  cuuint64_t strides[1] = {row_bytes};
+  cuuint32_t box[2] = {box_w, box_h};
+  cuuint32_t estr[2] = {1, 1};
+  CUresult r = enc(map, dtype, 2, const_cast<void*>(base), dims, strides, box, estr,
+                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                   CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS ? SPLIT_OK : SPLIT_ERR_INVALID;
+}
+
+namespace stn {
+
+constexpr int TH = 32, TW = 64, kThreads = 256;
+constexpr unsigned kWaitLimit = 1u << 24;
+
+// Stage a box of `sw` x `sh` elements starting at (x0, y0) into `dst`: TMA
+// when a tensor map is given, plain coalesced loads (zero outside) otherwise.
+template <typename T>
+__device__ __forceinline__ bool stage(T* dst, const CUtensorMap* map, const T* src, int W, int H,
+                                      int x0, int y0, int sw, int sh, uint64_t* bar, int* status) {
+  if (map) {
+    if (threadIdx.x == 0) {
+      mbar_init(bar, 1);
+      mbar_arrive_expect_tx(bar, (unsigned)(sw * sh * sizeof(T)));
+      tma_load_2d(dst, map, x0, y0, bar);
+    }
+    __syncthreads();
+    if (!mbar_wait(bar, 0, kWaitLimit)) {
+      set_status(status, SPLIT_ERR_TIMEOUT);
+      mbar_wait(bar, 0, kWaitLimit);  // let the copy land before leaving
+      return false;
+    }
+    return true;
+  }
+  for (int i = threadIdx.x; i < sw * sh; i += blockDim.x) {
+    const int r = i / sw, c = i % sw;
+    const int gx = x0 + c, gy = y0 + r;
+    dst[i] = (gx >= 0 && gy >= 0 && gx < W && gy < H) ? src[(size_t)gy * W + gx] : T(0);
+  }
+  __syncthreads();
+  return true;
+}
+
+// ---- erosion ---------------------------------------------------------------
+struct ErodeArgs {
+  const int32_t* in;
+  int32_t* out;
+  int W, H, R, XP;
+  const mrg::State* mstate;  // fused relabel when not null
+  const int32_t* mfin;
+  int* status;
+};
+
+template <bool R1>
+__global__ void __launch_bounds__(kThreads)
+erode_kernel(const __grid_constant__ CUtensorMap tmap, bool use_tma, ErodeArgs a) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  __shared__ __align__(8) uint64_t bar;
+  const int R = R1 ? 1 : a.R, XP = R1 ? 4 : a.XP;
+  const int SW = TW + 2 * XP, SH = TH + 2 * R;
+  int32_t* lab = reinterpret_cast<int32_t*>(smem);
+  const int tx0 = blockIdx.x * TW, ty0 = blockIdx.y * TH;
+  if (!stage<int32_t>(lab, use_tma ? &tmap : nullptr, a.in, a.W, a.H, tx0 - XP, ty0 - R, SW, SH,
+                      &bar, a.status))
+    return;
+  if (a.mstate) {
+    const mrg::State ms = *a.mstate;
+    for (int i = threadIdx.x; i < SW * SH; i += blockDim.x) lab[i] = mrg::relabel(ms, a.mfin, lab[i]);
+    __syncthreads();
+  }
+  if (R1) {
+    for (int i = threadIdx.x; i < TH * TW; i += blockDim.x) {
+      const int r = i / TW, c = i % TW;
+      const int x = tx0 + c, y = ty0 + r;
+      if (x >= a.W || y >= a.H) continue;
+      const int* p = lab + (r + 1) * SW + (c + XP);
+      const int v = p[0];
+      bool keep = x >= 1 && y >= 1 && x + 1 < a.W && y + 1 < a.H;
+      keep = keep && p[-SW - 1] == v && p[-SW] == v && p[-SW + 1] == v && p[-1] == v &&
+             p[1] == v && p[SW - 1] == v && p[SW] == v && p[SW + 1] == v;
+      a.out[(size_t)y * a.W + x] = keep ? v : -1;
+    }
+    return;
+  }
+  // separable square window: vertical run test per staged column, then the
+  // horizontal test over the vertical flags
+  unsigned char* vert = smem + (size_t)SW * SH * sizeof(int32_t);
+  for (int i = threadIdx.x; i < TH * SW; i += blockDim.x) {
+    const int r = i / SW, c = i % SW;
+    const int* p = lab + (r + R) * SW + c;
+    const int v = p[0];
+    bool ok = true;
+    for (int dy = -R; dy <= R && ok; ++dy) ok = p[dy * SW] == v;
+    vert[i] = ok;
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < TH * TW; i += blockDim.x) {
+    const int r = i / TW, c = i % TW;
+    const int x = tx0 + c, y = ty0 + r;
+    if (x >= a.W || y >= a.H) continue;
+    const int* p = lab + (r + R) * SW + (c + XP);
+    const unsigned char* f = vert + r * SW + (c + XP);
+    const int v = p[0];
+    bool keep = x >= R && y >= R && x + R < a.W && y + R < a.H;
+    for (int dx = -R; dx <= R && keep; ++dx) keep = p[dx] == v && f[dx];
+    a.out[(size_t)y * a.W + x] = keep ? v : -1;
+  }
+}
+
+static int erode_launch(const int32_t* in, int32_t* out, int W, int H, int R,
+                        const mrg::State* ms, const int32_t* mfin, int* status, cudaStream_t st) {
+  const int XP = (R + 3) / 4 * 4;
+  const int SW = TW + 2 * XP, SH = TH + 2 * R;
+  CUtensorMap map;
+  memset(&map, 0, sizeof(map));
+  const bool use_tma = make_tmap_2d(&map, CU_TENSOR_MAP_DATA_TYPE_INT32, 4, in, (uint64_t)W,
+                                    (uint64_t)H, (uint64_t)W * 4, (uint32_t)SW,
+                                    (uint32_t)SH) == SPLIT_OK;
+  ErodeArgs a{in, out, W, H, R, XP, ms, mfin, status};
+  dim3 grid((W + TW - 1) / TW, (H + TH - 1) / TH);
+  size_t smem = (size_t)SW * SH * sizeof(int32_t);
+  if (R == 1) {
+    erode_kernel<true><<<grid, kThreads, smem, st>>>(map, use_tma, a);
+  } else {
+    smem += (size_t)TH * SW;
+    if (smem > 48 * 1024)
+      SG_CUDA_TRY(cudaFuncSetAttribute(erode_kernel<false>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    erode_kernel<false><<<grid, kThreads, smem, st>>>(map, use_tma, a);
+  }
+  return launch_status();
+}
+
+// ---- luminance ----------------------------------------------------------------
+// sRGB byte -> linear * 100 after the sample's clamp to >= 1/255
+// (samples/src/main.cu:170-173, conversion.inl:15-20).
+__device__ __forceinline__ float lin100(int byte) {
+  float v = (float)byte / 255.0f;
+  v = fmaxf(v, 1.0f / 255.0f);
+  const float r1 = 1.0f / 1.055f, r2 = 1.0f / 12.92f;
+  const float l = v > 0.04045f ? powf(__fmul_rn(__fadd_rn(v, 0.055f), r1), 2.4f) : __fmul_rn(v, r2);
+  return __fmul_rn(l, 100.0f);
+}
+
+// L* / 100 from linear channels (conversion.inl:22-24 Y row, :46-64 L*).
+__device__ __forceinline__ float lum_from_lin(float r, float g, float b) {
+  const float Y = __fadd_rn(__fadd_rn(__fmul_rn(r, 0.2126729f), __fmul_rn(g, 0.7151522f)),
+                            __fmul_rn(b, 0.0721750f));
+  const float y = __fmul_rn(Y, 0.01f);
+  const float fy = y > 0.008856f ? cbrtf(y) : __fadd_rn(__fmul_rn(7.787f, y), 16.0f / 116.0f);
+  return __fmul_rn(__fsub_rn(__fmul_rn(116.0f, fy), 16.0f), 0.01f);
+}
+
+// ---- Sobel normals --------------------------------------------------------------
+// h is a (TH + 2) x (TW + 2) tile of heights with a one-pixel halo; outside
+// the image the accessor returns 0 (row/column ends are zero-extended) and
+// the differencing rows/columns are clamped (sobel_normals.cu:49-83).
+__device__ __forceinline__ void sobel_tile(const float* h, int hp, int tx0, int ty0, int W, int H,
+                                           float zinv, float* out) {
+  const size_t n = (size_t)W * H;
+  for (int i = threadIdx.x; i < TH * TW; i += blockDim.x) {
+    const int r = i / TW, c = i % TW;
+    const int x = tx0 + c, y = ty0 + r;
+    if (x >= W || y >= H) continue;
+    auto hz = [&](int xx, int yy) -> float {
+      if (xx < 0 || xx >= W || yy < 0 || yy >= H) return 0.0f;
+      return h[(yy - ty0 + 1) * hp + (xx - tx0 + 1)];
+    };
+    const int yb = min(y + 1, H - 1), yt = max(y - 1, 0);
+    const int xr = min(x + 1, W - 1), xl = max(x - 1, 0);
+    const float sb = __fadd_rn(__fadd_rn(hz(x - 1, yb), __fmul_rn(2.0f, hz(x, yb))), hz(x + 1, yb));
+    const float st = __fadd_rn(__fadd_rn(hz(x - 1, yt), __fmul_rn(2.0f, hz(x, yt))), hz(x + 1, yt));
+    const float tr = __fadd_rn(__fadd_rn(hz(xr, y - 1), __fmul_rn(2.0f, hz(xr, y))), hz(xr, y + 1));
+    const float tl = __fadd_rn(__fadd_rn(hz(xl, y - 1), __fmul_rn(2.0f, hz(xl, y))), hz(xl, y + 1));
+    const float gy = __fsub_rn(sb, st);
+    const float gx = __fsub_rn(tr, tl);
+    const float m2 = __fmaf_rn(gx, gx, __fmaf_rn(gy, gy, __fmul_rn(zinv, zinv)));
+    const float rm = 1.0f / sqrtf(m2);
+    const size_t g = (size_t)y * W + x;
+    out[g] = __fmul_rn(gx, rm);
+    out[n + g] = __fmul_rn(gy, rm);
+    out[2 * n + g] = __fmul_rn(fabsf(zinv), rm);
+  }
+}
+
+struct NormArgs {
+  const float* heights;
+  const uint8_t* rgb;
+  float* out;
+  int W, H;
+  float zinv;
+  int* status;
+};
+
+// heights (float) -> normals; staged box (TW + 8) x (TH + 2) from (tx0-4, ty0-1)
+__global__ void __launch_bounds__(kThreads)
+normals_kernel(const __grid_constant__ CUtensorMap tmap, bool use_tma, NormArgs a) {
+  __shared__ __align__(128) float tile[(TH + 2) * (TW + 8)];
+  __shared__ __align__(8) uint64_t bar;
+  const int tx0 = blockIdx.x * TW, ty0 = blockIdx.y * TH;
+  constexpr int SW = TW + 8, SH = TH + 2;
+  if (!stage<float>(tile, use_tma ? &tmap : nullptr, a.heights, a.W, a.H, tx0 - 4, ty0 - 1, SW,
+                    SH, &bar, a.status))
+    return;
+  // shift the view so that column index 0 is x = tx0 - 1
+  sobel_tile(tile + 3, SW, tx0, ty0, a.W, a.H, a.zinv, a.out);
+}
+
+// RGB8 -> luminance tile -> normals; staged bytes (3 TW + 32) x (TH + 2)
+// from byte column 3 tx0 - 16.
+__global__ void __launch_bounds__(kThreads)
+normals_rgb8_kernel(const __grid_constant__ CUtensorMap tmap, bool use_tma, NormArgs a) {
+  constexpr int SWB = 3 * TW + 32, SH = TH + 2, HP = TW + 2;
+  __shared__ __align__(128) unsigned char bytes[SWB * SH];
+  __shared__ float lum[SH * HP];
+  __shared__ float lin[256];
+  __shared__ __align__(8) uint64_t bar;
+  const int tx0 = blockIdx.x * TW, ty0 = blockIdx.y * TH;
+  for (int i = threadIdx.x; i < 256; i += blockDim.x) lin[i] = lin100(i);
+  if (!stage<unsigned char>(bytes, use_tma ? &tmap : nullptr, a.rgb, 3 * a.W, a.H, 3 * tx0 - 16,
+                            ty0 - 1, SWB, SH, &bar, a.status))
+    return;
+  for (int i = threadIdx.x; i < SH * HP; i += blockDim.x) {
+    const int r = i / HP, c = i % HP;  // pixel x = tx0 - 1 + c
+    const unsigned char* p = bytes + r * SWB + 3 * c + 13;
+    lum[i] = lum_from_lin(lin[p[0]], lin[p[1]], lin[p[2]]);
+  }
+  __syncthreads();
+  sobel_tile(lum, HP, tx0, ty0, a.W, a.H, a.zinv, a.out);
+}
+
+// ---- feature packing ------------------------------------------------------------
+__global__ void pack_kernel(const uint8_t* __restrict__ rgb, int64_t n, float4* __restrict__ f4,
+                            float* __restrict__ lumo) {
+  __shared__ float u8[256];
+  __shared__ float lin[256];
+  for (int i = threadIdx.x; i < 256; i += blockDim.x) {
+    u8[i] = (float)i / 255.0f;
+    lin[i] = lin100(i);
+  }
+  __syncthreads();
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int r = rgb[3 * i], g = rgb[3 * i + 1], b = rgb[3 * i + 2];
+    if (f4) f4[i] = make_float4(u8[r], u8[g], u8[b], 0.0f);
+    if (lumo) lumo[i] = lum_from_lin(lin[r], lin[g], lin[b]);
+  }
+}
+
+}  // namespace stn
+}  // namespace sg
+
+using namespace sg;
+
+extern "C" int split_erode(const int32_t* labels_in, int32_t* labels_out, int width, int height,
+                           int radius, void* stream) {
+  if (!labels_in || !labels_out || width < 1 || height < 1 || radius < 1 || radius > 16)
+    return SPLIT_ERR_INVALID;
+  if ((int64_t)width * height > 0x7fffffffLL) return SPLIT_ERR_INVALID;
+  const size_t n = (size_t)width * height;
+  const char* a = reinterpret_cast<const char*>(labels_in);
+  const char* b = reinterpret_cast<const char*>(labels_out);
+  if (a < b + n * 4 && b < a + n * 4) return SPLIT_ERR_INVALID;
+  return stn::erode_launch(labels_in, labels_out, width, height, radius, nullptr, nullptr,
+                           nullptr, as_stream(stream));
+}
+
+extern "C" int split_erode_mapped(const int32_t* labels_in, int32_t* labels_out, int width,
+                                  int height, int radius, const void* merge_workspace,
+                                  void* stream) {
+  if (!labels_in || !labels_out || !merge_workspace || width < 1 || height < 1 || radius < 1 ||
+      radius > 16)
+    return SPLIT_ERR_INVALID;
+  if ((int64_t)width * height > 0x7fffffffLL) return SPLIT_ERR_INVALID;
+  const size_t n = (size_t)width * height;
+  const char* a = reinterpret_cast<const char*>(labels_in);
+  const char* b = reinterpret_cast<const char*>(labels_out);
+  if (a < b + n * 4 && b < a + n * 4) return SPLIT_ERR_INVALID;
+  MergeView mv;
+  SG_TRY(merge_view(merge_workspace, width, height, &mv));
+  return stn::erode_launch(labels_in, labels_out, width, height, radius, mv.state, mv.fin,
+                           nullptr, as_stream(stream));
+}
+
+extern "C" int split_sobel_normals(const float* heights, int width, int height, float depth,
+                                   float* normals, void* stream) {
+  if (!heights || !normals || width < 1 || height < 1) return SPLIT_ERR_INVALID;
+  if ((int64_t)width * height > 0x7fffffffLL) return SPLIT_ERR_INVALID;
+  CUtensorMap map;
+  memset(&map, 0, sizeof(map));
+  const bool use_tma =
+      make_tmap_2d(&map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, heights, (uint64_t)width,
+                   (uint64_t)height, (uint64_t)width * 4, stn::TW + 8, stn::TH + 2) == SPLIT_OK;
+  stn::NormArgs a{heights, nullptr, normals, width, height, 1.0f / fmaxf(0.001f, depth), nullptr};
+  dim3 grid((width + stn::TW - 1) / stn::TW, (height + stn::TH - 1) / stn::TH);
+  stn::normals_kernel<<<grid, stn::kThreads, 0, as_stream(stream)>>>(map, use_tma, a);
+  return launch_status();
+}
+
+extern "C" int split_sobel_normals_rgb8(const uint8_t* rgb, int width, int height, float depth,
+                                        float* normals, void* stream) {
+  if (!rgb || !normals || width < 1 || height < 1) return SPLIT_ERR_INVALID;
+  if ((int64_t)width * height * 3 > 0x7fffffffLL) return SPLIT_ERR_INVALID;
+  CUtensorMap map;
+  memset(&map, 0, sizeof(map));
+  const bool use_tma =
+      make_tmap_2d(&map, CU_TENSOR_MAP_DATA_TYPE_UINT8, 1, rgb, (uint64_t)width * 3,
+                   (uint64_t)height, (uint64_t)width * 3, 3 * stn::TW + 32,
+                   stn::TH + 2) == SPLIT_OK;
+  stn::NormArgs a{nullptr, rgb, normals, width, height, 1.0f / fmaxf(0.001f, depth), nullptr};
+  dim3 grid((width + stn::TW - 1) / stn::TW, (height + stn::TH - 1) / stn::TH);
+  stn::normals_rgb8_kernel<<<grid, stn::kThreads, 0, as_stream(stream)>>>(map, use_tma, a);
+  return launch_status();
+}
+
+extern "C" int split_pack_rgb8(const uint8_t* rgb, int64_t npixels, float* features4,
+                               float* luminance, void* stream) {
+  if (!rgb || npixels <= 0 || (!features4 && !luminance)) return SPLIT_ERR_INVALID;
+  if (features4 && (reinterpret_cast<uintptr_t>(features4) & 15)) return SPLIT_ERR_INVALID;
+  DeviceInfo di;
+  SG_TRY(device_info(&di));
+  int64_t blocks = (npixels + 255) / 256;
+  if (blocks > (int64_t)di.sm_count * 8) blocks = (int64_t)di.sm_count * 8;
+  stn::pack_kernel<<<(int)blocks, 256, 0, as_stream(stream)>>>(
+      rgb, npixels, reinterpret_cast<float4*>(features4), luminance);
+  return launch_status();
+}

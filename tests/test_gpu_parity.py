@@ -1,0 +1,155 @@
+"""GPU parity tests: the CUDA path through the C ABI against the oracle."""
+import numpy as np
+import pytest
+
+import oracle
+from split_gb300 import synth
+
+pytestmark = pytest.mark.gpu
+
+
+def _t(a, dev):
+    import torch
+    return torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+
+
+# ---------------------------------------------------------------- k-means
+@pytest.mark.parametrize("dim,layout", [(3, 0), (3, 1), (3, 2), (5, 0), (5, 1), (5, 2)])
+def test_kmeans_lockstep(cuda, dim, layout):
+    import torch
+    from split_gb300 import kmeans
+    w, h, k = 200, 150, 8
+    rgb = synth.voronoi_rgb8(7, w, h, 32, sigma=4.0)
+    feats = synth.features(rgb, dim)
+    c0 = synth.pick_centroids(7, rgb, k, dim)
+    if layout == 0:
+        pts = _t(feats, cuda)
+    elif layout == 1:
+        f4 = np.zeros((w * h, 4), np.float32)
+        f4[:, :3] = feats[:3].T
+        pts = _t(f4, cuda)
+    else:
+        pts = _t(rgb.reshape(-1, 3), cuda)
+    cent = _t(c0, cuda)
+    labels = torch.empty(w * h, dtype=torch.int32, device=cuda)
+    ws = None
+    c = c0.copy()
+    for it in range(6):
+        ws = kmeans.cluster(pts, cent, labels, ws, max_iter=1, threshold=-1.0, layout=layout,
+                            dim=dim, width=w)
+        gl = labels.cpu().numpy()
+        gc = cent.cpu().numpy()
+        exact = oracle.kmeans_assign_f32(feats, c)
+        assert np.array_equal(gl, exact), f"iteration {it}: labels differ from the f32 oracle"
+        ref, cnt = oracle.kmeans_update_f64(gl, feats, c)
+        assert (cnt > 0).all()
+        rel = np.abs(gc - ref) / np.maximum(np.abs(ref), 1e-30)
+        assert rel.max() <= 1e-5, f"iteration {it}: centroid rel err {rel.max():.3g}"
+        c = gc
+    ws.check("kmeans")
+
+
+def test_kmeans_full_run_equals_steps(cuda):
+    import torch
+    from split_gb300 import kmeans
+    w, h, k = 160, 120, 8
+    rgb = synth.voronoi_rgb8(3, w, h, 32, sigma=4.0)
+    pts = _t(rgb.reshape(-1, 3), cuda)
+    c0 = synth.pick_centroids(3, rgb, k, 5)
+    a = _t(c0, cuda)
+    la = torch.empty(w * h, dtype=torch.int32, device=cuda)
+    kmeans.cluster(pts, a, la, None, max_iter=10, threshold=-1.0, layout=2, dim=5, width=w)
+    b = _t(c0, cuda)
+    lb = torch.empty_like(la)
+    for _ in range(10):
+        kmeans.cluster(pts, b, lb, None, max_iter=1, threshold=-1.0, layout=2, dim=5, width=w)
+    assert torch.equal(a, b) and torch.equal(la, lb)
+
+
+# ---------------------------------------------------------------- CCL
+@pytest.mark.parametrize("shape", [(1, 1), (1, 37), (41, 1), (97, 131), (256, 256), (67, 300)])
+@pytest.mark.parametrize("conn", [4, 8])
+@pytest.mark.parametrize("conv", [0, 1])
+def test_ccl_random(cuda, shape, conn, conv):
+    import torch
+    from split_gb300 import ccl
+    rng = np.random.default_rng(shape[0] * 1000 + shape[1])
+    lab = rng.integers(0, 3, size=shape).astype(np.int32)
+    out = torch.empty(shape, dtype=torch.int32, device=cuda)
+    ccl.connected_components(_t(lab, cuda), None, out, connectivity=conn, convention=conv)
+    assert np.array_equal(out.cpu().numpy(), oracle.ccl(lab, conn, conv))
+
+
+def test_ccl_maze(cuda):
+    import torch
+    from split_gb300 import ccl
+    lab = synth.maze_labels(11, 512, 384)
+    for conn in (4, 8):
+        out = torch.empty(lab.shape, dtype=torch.int32, device=cuda)
+        sizes = torch.zeros(lab.size, dtype=torch.int32, device=cuda)
+        ccl.connected_components(_t(lab, cuda), None, out, connectivity=conn, convention=0,
+                                 sizes=sizes)
+        ref = oracle.ccl(lab, conn, 0)
+        got = out.cpu().numpy()
+        assert np.array_equal(got, ref)
+        roots, counts = np.unique(ref, return_counts=True)
+        assert np.array_equal(sizes.cpu().numpy()[roots], counts)
+
+
+# ---------------------------------------------------------------- merge
+@pytest.mark.parametrize("policy", [0, 1])
+def test_merge_small(cuda, policy):
+    import torch
+    from split_gb300 import ccl
+    w, h = 240, 180
+    rng = np.random.default_rng(5)
+    lab = rng.integers(0, 4, size=(h // 4, w // 4)).repeat(4, 0).repeat(4, 1)
+    lab[rng.random((h, w)) < 0.05] = 7
+    seg = oracle.ccl(lab.astype(np.int32), 8, 0)
+    chroma = (rng.integers(0, 256, size=(2, h * w)) / 256.0).astype(np.float32)
+    ref = oracle.merge_small(seg, 24, policy, chroma)
+    g = _t(seg, cuda)
+    ccl.merge_small_segments(_t(chroma, cuda), g, None, 24, policy=policy)
+    assert np.array_equal(g.cpu().numpy(), ref)
+
+
+# ---------------------------------------------------------------- erosion / normals
+@pytest.mark.parametrize("shape", [(64, 64), (67, 129), (3, 5), (200, 320)])
+@pytest.mark.parametrize("radius", [1, 2, 3])
+def test_erode(cuda, shape, radius):
+    import torch
+    from split_gb300 import morph
+    rng = np.random.default_rng(shape[0] + radius)
+    lab = rng.integers(0, 3, size=(shape[0] // 3 + 1, shape[1] // 3 + 1)).repeat(3, 0).repeat(3, 1)
+    lab = np.ascontiguousarray(lab[: shape[0], : shape[1]]).astype(np.int32)
+    out = morph.erode(_t(lab, cuda), radius, out=torch.empty(shape, dtype=torch.int32,
+                                                            device=cuda))
+    assert np.array_equal(out.cpu().numpy(), oracle.erode(lab, radius))
+
+
+@pytest.mark.parametrize("shape", [(64, 64), (67, 129), (1, 1), (2, 3), (130, 256)])
+def test_sobel_normals(cuda, shape):
+    import torch
+    from split_gb300 import sfs
+    rng = np.random.default_rng(shape[0])
+    hgt = rng.random(shape, dtype=np.float32)
+    out = torch.empty((3, hgt.size), dtype=torch.float32, device=cuda)
+    sfs.sobel_normals(_t(hgt, cuda), out, 1.0)
+    ref = oracle.sobel_normals_f64(hgt, 1.0)
+    got = out.cpu().numpy().astype(np.float64)
+    cosang = np.clip((got * ref).sum(0) / np.linalg.norm(got, axis=0), -1, 1)
+    assert np.arccos(cosang).max() <= 1e-4
+
+
+def test_sobel_normals_rgb8(cuda):
+    import torch
+    from split_gb300 import sfs
+    rgb = synth.voronoi_rgb8(9, 256, 96, 16, sigma=3.0)
+    out = torch.empty((3, 256 * 96), dtype=torch.float32, device=cuda)
+    sfs.sobel_normals_rgb8(_t(rgb, cuda), out, 1.0)
+    lum = oracle.luminance_f64(rgb).reshape(96, 256)
+    # FP64 normals of the FP64 luminance; the device computes L* in FP32
+    ref = oracle.sobel_normals_f64(lum.astype(np.float32), 1.0)
+    got = out.cpu().numpy().astype(np.float64)
+    cosang = np.clip((got * ref).sum(0) / np.linalg.norm(got, axis=0), -1, 1)
+    assert np.arccos(cosang).max() <= 1e-4
