@@ -141,10 +141,10 @@ __device__ __forceinline__ int nearest(const float (&f)[DIM],
     t = __fsub_rn(f[2], c0.z);
     d = __fmaf_rn(t, t, d);
     if (DIM == 5) {
-      const float2 c1 = *reinterpret_cast<const float2*>(cs + k * CS + 4);
-      t = __fsub_rn(f[3], c1.x);
+      // dims 0..3 sit in c0 (x = column feature in c0.w), dim 4 right after
+      t = __fsub_rn(f[3], c0.w);
       d = __fmaf_rn(t, t, d);
-      t = __fsub_rn(f[4], c1.y);
+      t = __fsub_rn(f[4], cs[k * CS + 4]);
       d = __fmaf_rn(t, t, d);
     }
     if (d < best) {
