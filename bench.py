@@ -1,0 +1,336 @@
+"""Benchmark of the segmentation path on the 4K configuration.
+
+Workload (one step): a 3840x2160 RGB8 image (256 seeded Voronoi cells coloured
+from a 16-entry palette, illumination gradient x0.6..x1.0, Gaussian noise
+sigma 3) -> float32 5-D features (RGB / 255, 0.1 * column, 0.1 * row) ->
+k-means K=16, 20 iterations -> 8-connected labelling -> merge of segments
+< 256 px into the neighbour sharing most boundary -> 3x3 erosion -> Sobel
+normals of the luminance plane.  Synthetic data stands in for user images
+(the reference ships none).
+
+value : Mpix/s with the image resident in HBM, device-timed with CUDA events
+        (L2 flushed by a 256 MiB write before every step, outside the events).
+e2e   : Mpix/s through the public pipeline call with host buffers: pinned
+        RGB8 in, labels + normals + centroids out, copies inside the timing.
+
+Runs N independent replicas under torchrun (one image per GPU per step; the
+path has no cross-image exchange), reports the whole-job rate.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+W4K, H4K = 3840, 2160
+SEED = 0x5EED0001
+PROFILE_TRAFFIC = os.path.join(ROOT, "profiles", "kmeans_cluster_4k.txt")
+
+
+def make_image(width, height, seed=SEED):
+    from split_gb300 import synth
+    rgb = synth.voronoi_rgb8(seed, width, height, 256, npalette=16, illum_gradient=True,
+                             sigma=3.0)
+    c0 = synth.pick_centroids(seed, rgb, 16, 5, 0.1)
+    return rgb, c0
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def profiled_traffic():
+    """DRAM bytes per k-means launch from the committed ncu summary, if any."""
+    try:
+        with open(PROFILE_TRAFFIC) as f:
+            for line in f:
+                if line.startswith("traffic_bytes_per_launch:"):
+                    return float(line.split(":", 1)[1])
+    except OSError:
+        pass
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        rows = []
+        try:
+            with open(self.path) as f:
+                for line in f:
+                    parts = [p.strip() for p in line.split(",")]
+                    if len(parts) >= 9:
+                        rows.append(parts)
+            os.unlink(self.path)
+        except OSError:
+            pass
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i] == "Active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(rows)}
+
+
+# ------------------------------------------------------------------------ CPU
+def cpu_pipeline_oracle(rgb, c0, iters):
+    """The path on the host with the oracle restatement (single thread)."""
+    import numpy as np
+    import oracle
+    from split_gb300 import synth
+    h, w = rgb.shape[:2]
+    feats = synth.features(rgb, 5)
+    c = c0.copy()
+    lab = None
+    for _ in range(iters):
+        lab = oracle.kmeans_assign_f32(feats, c)
+        c64, _ = oracle.kmeans_update_f64(lab, feats, c)
+        c = c64.astype(np.float32)
+    seg = oracle.ccl(lab.reshape(h, w), 8, 0)
+    seg = oracle.merge_small(seg, 256, 0)
+    oracle.erode(seg, 1)
+    lum = oracle.luminance_f64(rgb).reshape(h, w).astype(np.float32)
+    oracle.sobel_normals_f64(lum, 1.0)
+
+
+def cpu_baseline_sample(side=1024, iters=20):
+    rgb, c0 = make_image(side, side, SEED + 1)
+    t0 = time.perf_counter()
+    cpu_pipeline_oracle(rgb, c0, iters)
+    dt = time.perf_counter() - t0
+    return {"value": round(side * side / dt / 1e6, 4), "unit": "Mpix/s", "cores": 1,
+            "kind": "port",
+            "sample": f"one {side}x{side} image of the 4K recipe through the oracle "
+                      f"restatement (k-means K=16 5-D x{iters}, 8-CCL, merge<256, erosion, "
+                      f"normals), {dt:.1f} s"}
+
+
+def run_reference(args, rank):
+    if rank != 0:
+        return
+    w = args.warmup
+    vals = []
+    for i in range(w + args.steps):
+        t0 = time.perf_counter()
+        rgb, c0 = make_image(args.ref_side, args.ref_side, SEED + 7 + i)
+        t1 = time.perf_counter()
+        cpu_pipeline_oracle(rgb, c0, 20)
+        dt = time.perf_counter() - t1
+        del t0
+        if i >= w:
+            vals.append(args.ref_side * args.ref_side / dt / 1e6)
+    v = statistics.median(vals)
+    line = {
+        "impl": "reference", "metric": "Mpix/s segment pipeline (4K)", "value": round(v, 4),
+        "unit": "Mpix/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(args.ref_side ** 2 / v / 1e3, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "4K recipe (K=16, 5-D, 20 iterations, 8-CCL, merge<256, "
+                               "erosion r=1, normals) on a bounded CPU sample",
+                   "sample": f"{args.ref_side}x{args.ref_side} image per step"},
+        "cpu_baseline": {"value": round(v, 4), "unit": "Mpix/s", "cores": 1, "kind": "port",
+                         "sample": f"{args.ref_side}x{args.ref_side} image per step"},
+        "e2e": {"value": round(v, 4), "unit": "Mpix/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------------------------ GPU
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="native", choices=["native", "reference"])
+    ap.add_argument("--width", type=int, default=W4K)
+    ap.add_argument("--height", type=int, default=H4K)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--ref-side", type=int, default=512)
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+
+    if args.impl == "reference":
+        run_reference(args, rank)
+        return
+
+    import numpy as np
+    import torch
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=dev)
+
+    from split_gb300 import _native, pipeline
+    _native.load()
+    W, H = args.width, args.height
+    npx = W * H
+    rgb_np, c0_np = make_image(W, H, SEED + rank)
+    rgb = torch.from_numpy(rgb_np).to(dev)
+    c0 = torch.from_numpy(c0_np).to(dev)
+    params = pipeline.Params()
+    pipe = pipeline.Pipeline(W, H, params, dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    nst = len(_native.PIPELINE_STAGES)
+
+    def barrier():
+        torch.cuda.synchronize()
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    for _ in range(args.warmup):
+        pipe.run(rgb, c0)
+    barrier()
+
+    # ---- device-resident timed region
+    ev = [[torch.cuda.Event(enable_timing=True) for _ in range(2 * nst)] for _ in range(args.steps)]
+    l0 = pipeline.launch_count()
+    with ClockSampler(local) as clk:
+        barrier()
+        t_wall = time.perf_counter()
+        for s in range(args.steps):
+            flush.zero_()
+            pipe.run(rgb, c0, stage_events=ev[s])
+        barrier()
+        t_wall = time.perf_counter() - t_wall
+    launches = pipeline.launch_count() - l0
+    clocks = clk.summary()
+    stage_ms = {name: 0.0 for name in _native.PIPELINE_STAGES}
+    total_ms = 0.0
+    for s in range(args.steps):
+        for i, name in enumerate(_native.PIPELINE_STAGES):
+            stage_ms[name] += ev[s][2 * i].elapsed_time(ev[s][2 * i + 1]) / args.steps
+        total_ms += ev[s][0].elapsed_time(ev[s][-1]) / args.steps
+    step_ms = total_ms
+    if dist is not None:
+        t = torch.tensor([step_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        step_ms = float(t.item())
+    value = world * npx / (step_ms * 1e-3) / 1e6
+
+    # ---- end-to-end through the public call with host buffers
+    h_rgb = torch.from_numpy(rgb_np).pin_memory()
+    h_c0 = torch.from_numpy(c0_np).pin_memory()
+    h_lab = torch.empty((H, W), dtype=torch.int32).pin_memory()
+    h_nrm = torch.empty((3, npx), dtype=torch.float32).pin_memory()
+    h_cen = torch.empty((5, 16), dtype=torch.float32).pin_memory()
+    d_rgb = torch.empty_like(rgb)
+    e2e_steps = max(10, args.steps // 4)
+    barrier()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for s in range(e2e_steps):
+        d_rgb.copy_(h_rgb, non_blocking=True)
+        pipe.centroids.copy_(h_c0, non_blocking=True)
+        pipe.run(d_rgb)
+        h_lab.copy_(pipe.segment_labels, non_blocking=True)
+        h_nrm.copy_(pipe.normals, non_blocking=True)
+        h_cen.copy_(pipe.centroids, non_blocking=True)
+    e1.record()
+    barrier()
+    e2e_ms = e0.elapsed_time(e1) / e2e_steps
+    if dist is not None:
+        t = torch.tensor([e2e_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+    e2e_value = world * npx / (e2e_ms * 1e-3) / 1e6
+
+    # ---- roofline of the dominant kernel (k-means, one cooperative launch)
+    iters = params.kmeans_iters
+    km_bytes = npx * (16 * iters + 4)  # float4 features per iteration + final labels
+    km_ms = stage_ms["kmeans"]
+    peak, peak_kind = peaks()
+    achieved = km_bytes / (km_ms * 1e-3) / 1e9
+    roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 4), "traffic": profiled_traffic(),
+                "kernel": "kmeans_kernel (cooperative, 20 iterations)",
+                "algorithmic_bytes_per_launch": km_bytes, "peak_source": peak_kind}
+
+    if rank == 0:
+        cpu = None
+        if not args.no_cpu_baseline:
+            cpu = cpu_baseline_sample()
+        line = {
+            "metric": "Mpix/s segment pipeline (4K)", "value": round(value, 2),
+            "unit": "Mpix/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(step_ms, 4), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": f"{W}x{H} single image per GPU per step: K=16 5-D float32 "
+                                   "features, 20 k-means iterations, 8-CCL, merge <256 px "
+                                   "(most boundary), 3x3 erosion, luminance normals",
+                       "mode": "plain launch sequence", "l2": "flushed (256 MiB write) "
+                       "before every step, outside the events",
+                       "parallelism": f"replicas x{world}"},
+            "e2e": {"value": round(e2e_value, 2), "unit": "Mpix/s",
+                    "h2d_bytes_per_step": rgb_np.nbytes + c0_np.nbytes,
+                    "d2h_bytes_per_step": npx * 4 + npx * 12 + 5 * 16 * 4},
+            "gpu_launches": int(launches),
+            "roofline": roofline,
+            "cpu_baseline": cpu,
+            "clocks": clocks,
+            "stages_ms": {k: round(v, 4) for k, v in stage_ms.items()},
+            "wall_s_timed_region": round(t_wall, 3),
+        }
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

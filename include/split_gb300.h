@@ -222,6 +222,50 @@ int split_sobel_normals_rgb8(const uint8_t* rgb, int width, int height,
 int split_pack_rgb8(const uint8_t* rgb, int64_t npixels, float* features4,
                     float* luminance, void* stream);
 
+/* ======================================================================== */
+/* pipeline                                                                  */
+/* ======================================================================== */
+
+/* The sample's segmentation path as one call (samples/src/main.cu:154-314:
+ * features -> kmeans::cluster -> ccl::connected_components -> small-segment
+ * merge -> morph::erode) plus Sobel normals of the luminance plane. */
+typedef struct split_pipeline_params {
+  int nclusters;          /* K <= 64                                         */
+  int dim;                /* 3 (RGB) or 5 (RGB + xy_scale * (column, row))   */
+  float xy_scale;
+  int kmeans_iters;
+  float kmeans_threshold; /* < 0: exactly kmeans_iters iterations            */
+  int features;           /* SPLIT_LAYOUT_FLOAT4: pack float4 features first;
+                             SPLIT_LAYOUT_RGB8: read the bytes directly      */
+  int connectivity;       /* 4 or 8                                          */
+  int convention;         /* SPLIT_LABEL_MIN_INDEX / SPLIT_LABEL_MAX_INDEX   */
+  int merge_P;            /* merge segments smaller than P; 0 = no merge     */
+  int merge_policy;       /* SPLIT_MERGE_MOST_BOUNDARY                       */
+  int erode_radius;       /* 0 = no erosion                                  */
+  int compute_normals;    /* nonzero: normals of L* / 100                    */
+  float depth;
+} split_pipeline_params;
+
+enum { SPLIT_PIPELINE_STAGES = 6 }; /* pack, kmeans, ccl, merge, erode, normals */
+
+size_t split_pipeline_workspace_size(int width, int height,
+                                     const split_pipeline_params* params);
+
+/* rgb: device RGB8 interleaved image.  centroids: dim x K planar, in/out
+ * (initial centroids in).  cluster_labels, segment_labels: int32[w*h] out
+ * (segment_labels = merged, eroded labels; -1 = eroded).  normals: planar
+ * 3 x w*h float out (may be null when compute_normals == 0).
+ * stage_events: null, or 2 * SPLIT_PIPELINE_STAGES cudaEvent_t recorded
+ * before/after each stage (a skipped stage records both back to back). */
+int split_pipeline_run(const uint8_t* rgb, int width, int height,
+                       const split_pipeline_params* params, float* centroids,
+                       int32_t* cluster_labels, int32_t* segment_labels,
+                       float* normals, void* workspace, size_t workspace_bytes,
+                       void* const* stage_events, void* stream);
+
+/* Kernels launched by this library since it was loaded (all entry points). */
+unsigned long long split_launch_count(void);
+
 #ifdef __cplusplus
 }
 #endif

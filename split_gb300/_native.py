@@ -48,11 +48,26 @@ _SIGS = {
     "split_sobel_normals": (_i32, [_vp, _i32, _i32, _f32, _vp, _vp]),
     "split_sobel_normals_rgb8": (_i32, [_vp, _i32, _i32, _f32, _vp, _vp]),
     "split_pack_rgb8": (_i32, [_vp, _i64, _vp, _vp, _vp]),
+    "split_pipeline_workspace_size": (_sz, [_i32, _i32, _vp]),
+    "split_pipeline_run": (_i32, [_vp, _i32, _i32, _vp, _vp, _vp, _vp, _vp, _vp, _sz, _vp, _vp]),
+    "split_launch_count": (C.c_ulonglong, []),
     "split_synth_voronoi_rgb8": (_i32, [_u64, _i32, _i32, _i32, _i32, _i32, C.c_double, _vp]),
     "split_synth_pick_centroids": (_i32, [_u64, _vp, _i32, _i32, _i32, _i32, _f32, _vp]),
     "split_synth_feature_u8": (_f32, [C.c_uint8]),
     "split_synth_maze_labels": (_i32, [_u64, _i32, _i32, _vp]),
 }
+
+
+class PipelineParams(C.Structure):
+    """split_pipeline_params (include/split_gb300.h)."""
+    _fields_ = [("nclusters", C.c_int), ("dim", C.c_int), ("xy_scale", C.c_float),
+                ("kmeans_iters", C.c_int), ("kmeans_threshold", C.c_float),
+                ("features", C.c_int), ("connectivity", C.c_int), ("convention", C.c_int),
+                ("merge_P", C.c_int), ("merge_policy", C.c_int), ("erode_radius", C.c_int),
+                ("compute_normals", C.c_int), ("depth", C.c_float)]
+
+
+PIPELINE_STAGES = ("pack", "kmeans", "ccl", "merge", "erode", "normals")
 
 
 class SplitError(RuntimeError):

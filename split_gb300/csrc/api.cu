@@ -1,10 +1,14 @@
 // Library-level entry points: version, status strings, device queries and the
 // workspace status word.
+#include <atomic>
 #include <mutex>
 
 #include "common.cuh"
 
 namespace sg {
+
+static std::atomic<unsigned long long> g_launches{0};
+void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 
 int device_info(DeviceInfo* out) {
   static std::mutex mu;
@@ -33,6 +37,10 @@ int device_info(DeviceInfo* out) {
 }  // namespace sg
 
 using namespace sg;
+
+extern "C" unsigned long long split_launch_count(void) {
+  return g_launches.load(std::memory_order_relaxed);
+}
 
 extern "C" const char* split_version(void) { return "split_gb300 0.1.0 (sm_103a)"; }
 

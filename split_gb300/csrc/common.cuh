@@ -27,7 +27,12 @@ namespace sg {
     if (s_ != SPLIT_OK) return s_; \
   } while (0)
 
+// Kernels launched by the library since load (every launch site reports
+// through launch_status()).
+void count_launch();
+
 inline int launch_status() {
+  count_launch();
   cudaError_t e = cudaGetLastError();
   if (e == cudaErrorNoKernelImageForDevice || e == cudaErrorInvalidDeviceFunction)
     return SPLIT_ERR_UNSUPPORTED;

@@ -1,0 +1,130 @@
+// The segmentation path as one plain launch sequence for one image: feature
+// packing, k-means, connected components, small-segment merge decision,
+// fused relabel + erosion, and Sobel normals of the luminance plane.
+// Mirrors the stage order of samples/src/main.cu:154-314.
+#include "merge_state.cuh"
+
+namespace sg {
+namespace pipe {
+
+struct Layout {
+  WsHeader* hdr;
+  float* features4;
+  int32_t* seg;
+  int32_t* sizes;
+  void* km_ws;
+  size_t km_bytes;
+  void* ccl_ws;
+  size_t ccl_bytes;
+  void* mrg_ws;
+  size_t mrg_bytes;
+  size_t bytes;
+};
+
+static Layout carve(void* ws, int W, int H, const split_pipeline_params& p) {
+  const int64_t n = (int64_t)W * H;
+  Carver c(ws);
+  Layout l;
+  l.hdr = c.take<WsHeader>(1);
+  l.features4 = p.features == SPLIT_LAYOUT_FLOAT4 ? c.take<float>((size_t)n * 4) : nullptr;
+  l.seg = c.take<int32_t>((size_t)n);
+  l.sizes = c.take<int32_t>((size_t)n);
+  l.km_bytes = split_kmeans_cluster_workspace_size(n, p.nclusters, p.dim);
+  l.km_ws = c.take<char>(l.km_bytes);
+  l.ccl_bytes = split_ccl_workspace_size(W, H);
+  l.ccl_ws = c.take<char>(l.ccl_bytes);
+  l.mrg_bytes = p.merge_P > 0 ? split_merge_small_workspace_size(W, H) : 0;
+  l.mrg_ws = p.merge_P > 0 ? c.take<char>(l.mrg_bytes) : nullptr;
+  l.bytes = c.size();
+  return l;
+}
+
+static bool valid(const split_pipeline_params* p) {
+  return p && p->nclusters >= 1 && p->nclusters <= 64 && (p->dim == 3 || p->dim == 5) &&
+         p->kmeans_iters >= 0 &&
+         (p->features == SPLIT_LAYOUT_FLOAT4 || p->features == SPLIT_LAYOUT_RGB8) &&
+         (p->connectivity == 4 || p->connectivity == 8) &&
+         (p->convention == SPLIT_LABEL_MIN_INDEX || p->convention == SPLIT_LABEL_MAX_INDEX) &&
+         p->merge_P >= 0 && p->merge_policy == SPLIT_MERGE_MOST_BOUNDARY && p->erode_radius >= 0 &&
+         p->erode_radius <= 16;
+}
+
+}  // namespace pipe
+}  // namespace sg
+
+using namespace sg;
+
+extern "C" size_t split_pipeline_workspace_size(int width, int height,
+                                                const split_pipeline_params* params) {
+  if (width < 1 || height < 1 || !pipe::valid(params)) return 0;
+  return pipe::carve(nullptr, width, height, *params).bytes;
+}
+
+extern "C" int split_pipeline_run(const uint8_t* rgb, int width, int height,
+                                  const split_pipeline_params* params, float* centroids,
+                                  int32_t* cluster_labels, int32_t* segment_labels,
+                                  float* normals, void* workspace, size_t workspace_bytes,
+                                  void* const* stage_events, void* stream) {
+  if (!rgb || !centroids || !cluster_labels || !segment_labels || width < 1 || height < 1 ||
+      !pipe::valid(params))
+    return SPLIT_ERR_INVALID;
+  if ((int64_t)width * height * 3 > 0x7fffffffLL) return SPLIT_ERR_INVALID;
+  const split_pipeline_params& p = *params;
+  if (p.compute_normals && !normals) return SPLIT_ERR_INVALID;
+  pipe::Layout l = pipe::carve(nullptr, width, height, p);
+  if (!workspace || workspace_bytes < l.bytes || (reinterpret_cast<uintptr_t>(workspace) & 255))
+    return SPLIT_ERR_WORKSPACE;
+  l = pipe::carve(workspace, width, height, p);
+  cudaStream_t st = as_stream(stream);
+  const int64_t n = (int64_t)width * height;
+  auto mark = [&](int i) -> int {
+    if (stage_events)
+      SG_CUDA_TRY(cudaEventRecord(reinterpret_cast<cudaEvent_t>(stage_events[i]), st));
+    return SPLIT_OK;
+  };
+  // 0: features
+  SG_TRY(mark(0));
+  if (p.features == SPLIT_LAYOUT_FLOAT4)
+    SG_TRY(split_pack_rgb8(rgb, n, l.features4, nullptr, stream));
+  SG_TRY(mark(1));
+  // 1: k-means
+  SG_TRY(mark(2));
+  const void* pts = p.features == SPLIT_LAYOUT_FLOAT4 ? static_cast<const void*>(l.features4)
+                                                       : static_cast<const void*>(rgb);
+  SG_TRY(split_kmeans_cluster(pts, p.features, p.dim, n, width, p.xy_scale, centroids,
+                              p.nclusters, cluster_labels, l.km_ws, l.km_bytes, p.kmeans_iters,
+                              p.kmeans_threshold, nullptr, stream));
+  SG_TRY(mark(3));
+  // 2: connected components (+ component sizes for the merge)
+  SG_TRY(mark(4));
+  SG_TRY(split_ccl(cluster_labels, width, height, p.connectivity, p.convention, l.seg,
+                   p.merge_P > 0 ? l.sizes : nullptr, l.ccl_ws, l.ccl_bytes, stream));
+  SG_TRY(mark(5));
+  // 3: merge decision (the relabel is fused into the erosion below)
+  SG_TRY(mark(6));
+  if (p.merge_P > 0)
+    SG_TRY(merge_decide_only(l.seg, width, height, p.merge_P, p.merge_policy, nullptr, l.sizes,
+                             l.mrg_ws, l.mrg_bytes, st));
+  SG_TRY(mark(7));
+  // 4: relabel + erosion
+  SG_TRY(mark(8));
+  if (p.erode_radius > 0) {
+    if (p.merge_P > 0)
+      SG_TRY(split_erode_mapped(l.seg, segment_labels, width, height, p.erode_radius, l.mrg_ws,
+                                stream));
+    else
+      SG_TRY(split_erode(l.seg, segment_labels, width, height, p.erode_radius, stream));
+  } else {
+    SG_CUDA_TRY(cudaMemcpyAsync(segment_labels, l.seg, sizeof(int32_t) * (size_t)n,
+                                cudaMemcpyDeviceToDevice, st));
+    if (p.merge_P > 0)
+      SG_TRY(split_merge_small(segment_labels, width, height, p.merge_P, p.merge_policy, nullptr,
+                               l.sizes, l.mrg_ws, l.mrg_bytes, stream));
+  }
+  SG_TRY(mark(9));
+  // 5: normals of the luminance plane, straight from the bytes
+  SG_TRY(mark(10));
+  if (p.compute_normals) SG_TRY(split_sobel_normals_rgb8(rgb, width, height, p.depth, normals, stream));
+  SG_TRY(mark(11));
+  return SPLIT_OK;
+}
