@@ -239,6 +239,10 @@ def main():
 
     # ---- device-resident timed region
     ev = [[torch.cuda.Event(enable_timing=True) for _ in range(2 * nst)] for _ in range(args.steps)]
+    for row in ev:  # torch creates the CUDA event on first record
+        for e in row:
+            e.record()
+    torch.cuda.synchronize()
     l0 = pipeline.launch_count()
     with ClockSampler(local) as clk:
         barrier()

@@ -62,6 +62,9 @@ class Pipeline:
             self.centroids.copy_(init_centroids, non_blocking=True)
         ev = None
         if stage_events is not None:
+            if any(e.cuda_event == 0 for e in stage_events):
+                raise ValueError("stage events must have been recorded once (torch creates "
+                                 "CUDA events lazily)")
             ev = (C.c_void_p * len(stage_events))(*[e.cuda_event for e in stage_events])
         st = N.load().split_pipeline_run(
             ptr(rgb), self.width, self.height, C.byref(self._cp), ptr(self.centroids),
