@@ -36,9 +36,14 @@ __device__ __forceinline__ bool better(int a, int b) {
 }
 
 // ---- shared-memory union-find --------------------------------------------
+// Find with path halving.  Safe next to concurrent hooking: a halving store
+// only ever points a node at one of its ancestors, and a hook that loses such
+// a race is retried by sunite with the node's new parent.
 __device__ __forceinline__ int sfind(volatile int* par, int x) {
   int p = par[x];
   while (p != x) {
+    const int gp = par[p];
+    if (gp != p) par[x] = gp;
     x = p;
     p = par[x];
   }
@@ -91,10 +96,19 @@ __device__ void gunite(int* P, int a, int b, int* status) {
   set_status(status, SPLIT_ERR_NOT_CONVERGED);
 }
 
+// Tile pass.  Thread t owns 8 consecutive pixels of row t / 8; runs of equal
+// label inside those 8 pixels are linked without atomics, and a union is only
+// issued where run adjacency does not already imply it:
+//   W  : only at the first pixel of a thread's 8 (other W links are runs);
+//   N  : unless W and NW both carry the label (the NW/N run already joins);
+//   NW : only if neither W nor N carries the label;
+//   NE : only if N does not carry the label and E (in the tile) does not
+//        either (E's own N link covers NE).
 template <bool MAXC, int CONN>
 __global__ void __launch_bounds__(kThreads)
 tile_kernel(const int32_t* __restrict__ in, int W, int H, int* __restrict__ P,
             int32_t* __restrict__ sizes, int* status) {
+  static_assert(TW == 64 && TH * TW == kThreads * 8, "8 pixels per thread");
   __shared__ int lab[TH * TW];
   __shared__ int par[TH * TW];
   const int tx0 = blockIdx.x * TW, ty0 = blockIdx.y * TH;
@@ -102,31 +116,69 @@ tile_kernel(const int32_t* __restrict__ in, int W, int H, int* __restrict__ P,
   for (int i = threadIdx.x; i < TH * TW; i += kThreads) {
     const int r = i / TW, c = i % TW;
     lab[i] = (r < th && c < tw) ? __ldg(in + (size_t)(ty0 + r) * W + tx0 + c) : 0;
-    par[i] = i;
   }
   __syncthreads();
-  for (int i = threadIdx.x; i < TH * TW; i += kThreads) {
-    const int r = i / TW, c = i % TW;
-    if (r >= th || c >= tw) continue;
-    const int v = lab[i];
-    if (c > 0 && lab[i - 1] == v) sunite<MAXC>(par, i, i - 1, status);
-    if (r > 0) {
-      if (lab[i - TW] == v) sunite<MAXC>(par, i, i - TW, status);
-      if (CONN == 8) {
-        if (c > 0 && lab[i - TW - 1] == v) sunite<MAXC>(par, i, i - TW - 1, status);
-        if (c + 1 < tw && lab[i - TW + 1] == v) sunite<MAXC>(par, i, i - TW + 1, status);
+  const int r = threadIdx.x >> 3, c0 = (threadIdx.x & 7) * 8;
+  const int base = r * TW + c0;
+  {
+    // runs point at their best pixel: the first (minimum index convention)
+    // or the last (maximum index convention)
+    const bool ok_row = r < th;
+    if (!MAXC) {
+      int run = base;
+      par[base] = base;
+#pragma unroll
+      for (int j = 1; j < 8; ++j) {
+        const int i = base + j;
+        if (!(ok_row && c0 + j < tw) || lab[i] != lab[i - 1]) run = i;
+        par[i] = run;
+      }
+    } else {
+      int run = base + 7;
+      par[base + 7] = base + 7;
+#pragma unroll
+      for (int j = 6; j >= 0; --j) {
+        const int i = base + j;
+        if (!(ok_row && c0 + j + 1 < tw) || lab[i] != lab[i + 1]) run = i;
+        par[i] = run;
       }
     }
   }
   __syncthreads();
-  for (int i = threadIdx.x; i < TH * TW; i += kThreads) {
-    const int r = i / TW, c = i % TW;
-    if (r >= th || c >= tw) continue;
-    const int root = sfind(par, i);
-    const int rr = root / TW, rc = root % TW;
-    const int g = (ty0 + r) * W + tx0 + c;
-    P[g] = (ty0 + rr) * W + tx0 + rc;
-    if (sizes && root == i) sizes[g] = 0;
+  if (r < th) {
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const int c = c0 + j;
+      if (c >= tw) break;
+      const int i = base + j;
+      const int v = lab[i];
+      const bool hasW = c > 0 && lab[i - 1] == v;
+      if (j == 0 && hasW) sunite<MAXC>(par, i, i - 1, status);
+      if (r > 0) {
+        const bool n = lab[i - TW] == v;
+        const bool nw = c > 0 && lab[i - TW - 1] == v;
+        if (n && !(hasW && nw)) sunite<MAXC>(par, i, i - TW, status);
+        if (CONN == 8) {
+          if (nw && !hasW && !n) sunite<MAXC>(par, i, i - TW - 1, status);
+          const bool ne = c + 1 < tw && lab[i - TW + 1] == v;
+          const bool e = c + 1 < tw && lab[i + 1] == v;
+          if (ne && !n && !e) sunite<MAXC>(par, i, i - TW + 1, status);
+        }
+      }
+    }
+  }
+  __syncthreads();
+  if (r < th) {
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const int c = c0 + j;
+      if (c >= tw) break;
+      const int i = base + j;
+      const int root = sfind(par, i);
+      const int g = (ty0 + r) * W + tx0 + c;
+      P[g] = (ty0 + root / TW) * W + tx0 + root % TW;
+      if (sizes && root == i) sizes[g] = 0;
+    }
   }
 }
 
@@ -168,9 +220,11 @@ flatten_kernel(int* P, int64_t n, int32_t* __restrict__ sizes, int* status) {
     int root = -1;
     if (g < n) {
       unsigned budget = kUnionCap;
-      root = gfind(P, __ldcg(P + g), budget);
+      const int lr = __ldcg(P + g);
+      root = gfind(P, lr, budget);
       if (!budget) set_status(status, SPLIT_ERR_NOT_CONVERGED);
       P[g] = root;
+      if (lr != root) P[lr] = root;  // later pixels of this local tree: one hop
     }
     if (sizes) {
       const unsigned peers = __match_any_sync(full, root);

@@ -123,16 +123,68 @@ struct Loader {
   }
 };
 
-// Nearest centroid: d = fma chain of (x - c)^2 in dimension order, strict <
-// in ascending k, so ties go to the lowest k (label.cu:23-32, :98-105).
+// Order-preserving float -> int key (for warp min/max reductions).
+__device__ __forceinline__ int fkey(float x) {
+  const int i = __float_as_int(x);
+  return i ^ ((i >> 31) & 0x7fffffff);
+}
+__device__ __forceinline__ float fkey_inv(int k) {
+  return __int_as_float(k ^ ((k >> 31) & 0x7fffffff));
+}
+
+// Candidate clusters of a 32-pixel batch whose features lie in the box
+// [lo, hi]: lane l bounds clusters l and l + 32.  For every cluster,
+// LB = squared distance from the centroid to the box (a lower bound of each
+// pixel's distance) and UB = squared distance to the farthest box corner (an
+// upper bound).  A cluster whose LB exceeds the smallest UB by more than the
+// 1e-4 relative margin is strictly farther than the winner from every pixel
+// of the batch even after FP32 rounding (a few ulp), so skipping it leaves
+// every argmin - ties included - unchanged.
 template <int DIM>
-__device__ __forceinline__ int nearest(const float (&f)[DIM],
-                                       const float* __restrict__ cs, int K) {
+__device__ __forceinline__ unsigned long long candidates(const float (&lo)[DIM],
+                                                         const float (&hi)[DIM],
+                                                         const float* __restrict__ cs, int K) {
+  constexpr int CS = cstride(DIM);
+  const int lane = threadIdx.x & 31;
+  float lb[2], ubm = INFINITY;
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    const int k = lane + 32 * h;
+    lb[h] = INFINITY;
+    if (k < K) {
+      float l = 0.0f, u = 0.0f;
+#pragma unroll
+      for (int d = 0; d < DIM; ++d) {
+        const float c = cs[k * CS + d];
+        const float g = fmaxf(fmaxf(lo[d] - c, c - hi[d]), 0.0f);
+        const float e = fmaxf(c - lo[d], hi[d] - c);
+        l = __fmaf_rn(g, g, l);
+        u = __fmaf_rn(e, e, u);
+      }
+      lb[h] = l;
+      ubm = fminf(ubm, u);
+    }
+  }
+  // UB >= 0: its bit pattern orders like the value
+  const float ub = __int_as_float(__reduce_min_sync(0xffffffffu, __float_as_int(ubm)));
+  const float thr = ub * 1.0001f;
+  const unsigned m0 = __ballot_sync(0xffffffffu, lb[0] <= thr);
+  const unsigned m1 = __ballot_sync(0xffffffffu, lb[1] <= thr);
+  return ((unsigned long long)m1 << 32) | m0;
+}
+
+// Nearest centroid among `mask`: d = fma chain of (x - c)^2 in dimension
+// order, strict < in ascending k, so ties go to the lowest k (label.cu:23-32,
+// :98-105).
+template <int DIM>
+__device__ __forceinline__ int nearest(const float (&f)[DIM], const float* __restrict__ cs,
+                                       unsigned long long mask) {
   constexpr int CS = cstride(DIM);
   float best = INFINITY;
   int bk = 0;
-#pragma unroll 4
-  for (int k = 0; k < K; ++k) {
+  while (mask) {
+    const int k = __ffsll((long long)mask) - 1;
+    mask &= mask - 1;
     const float4 c0 = *reinterpret_cast<const float4*>(cs + k * CS);
     float t = __fsub_rn(f[0], c0.x);
     float d = __fmul_rn(t, t);
@@ -205,13 +257,29 @@ __device__ void process_unit(const Image& im, int unit, Smem& sm,
     const bool valid = px < im.npoints;
     float f[DIM];
     int lab = -1;
-    if (valid) {
-      ld.load(px, row, col, f);
-      if (MODE == kUpdateOnly) {
+    if (valid) ld.load(px, row, col, f);
+    if (MODE == kUpdateOnly) {
+      if (valid) {
         lab = __ldg(im.labels_in + px);
         if (lab < 0 || lab >= im.K) lab = -1;
-      } else {
-        lab = nearest<DIM>(f, sm.cent, im.K);
+      }
+    } else {
+      // bounding box of the batch, then the candidate clusters
+      float lo[DIM], hi[DIM];
+      bool nan = false;
+#pragma unroll
+      for (int d = 0; d < DIM; ++d) {
+        nan |= valid && (f[d] != f[d]);
+        lo[d] = fkey_inv(__reduce_min_sync(0xffffffffu, fkey(valid ? f[d] : INFINITY)));
+        hi[d] = fkey_inv(__reduce_max_sync(0xffffffffu, fkey(valid ? f[d] : -INFINITY)));
+      }
+      unsigned long long mask;
+      if (__any_sync(0xffffffffu, nan))
+        mask = im.K >= 64 ? ~0ull : ((1ull << im.K) - 1ull);
+      else
+        mask = candidates<DIM>(lo, hi, sm.cent, im.K);
+      if (valid) {
+        lab = nearest<DIM>(f, sm.cent, mask);
         if (write_labels) im.labels[px] = lab;
       }
     }
@@ -396,9 +464,12 @@ __global__ void __launch_bounds__(kThreads) kmeans_kernel(Params p) {
     for (;;) {
       if (threadIdx.x == 0) sm.unit = (int)atomicAdd(&p.hdr->work_counter[it & 1], 1u);
       __syncthreads();
-      const int u = sm.unit;
+      const int raw = sm.unit;
       __syncthreads();
-      if (u >= p.total_units) break;
+      if (raw >= p.total_units) break;
+      // odd iterations walk the units backwards: they start on the units the
+      // previous iteration touched last, which are still resident in L2
+      const int u = (it & 1) ? p.total_units - 1 - raw : raw;
       const int img = find_image(p, u);
       const Image& im = image_of(p, img);
       if (MODE != kAssignOnly && *(volatile int*)&p.state[img].done) continue;

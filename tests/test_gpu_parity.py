@@ -153,3 +153,23 @@ def test_sobel_normals_rgb8(cuda):
     got = out.cpu().numpy().astype(np.float64)
     cosang = np.clip((got * ref).sum(0) / np.linalg.norm(got, axis=0), -1, 1)
     assert np.arccos(cosang).max() <= 1e-4
+
+
+@pytest.mark.parametrize("k", [1, 5, 16, 33, 64])
+def test_kmeans_assign_pruning_exact(cuda, k):
+    """Candidate pruning must not change any argmin: arbitrary planar 5-D
+    features (negative values, duplicates, NaN rows) against the exact
+    FP32 oracle."""
+    import torch
+    from split_gb300 import kmeans
+    rng = np.random.default_rng(k)
+    n = 70001
+    pts = rng.normal(0, 3, size=(5, n)).astype(np.float32)
+    pts[:, 100:200] = pts[:, 100:101]          # duplicates
+    pts[2, 5000:5100] = np.nan                 # NaN features
+    cent = rng.normal(0, 3, size=(5, k)).astype(np.float32)
+    if k > 1:
+        cent[:, 1] = cent[:, 0]                # duplicate centroid: ties
+    lab = torch.empty(n, dtype=torch.int32, device=cuda)
+    kmeans.label_points(_t(cent, cuda), _t(pts, cuda), lab, None, dim=5)
+    assert np.array_equal(lab.cpu().numpy(), oracle.kmeans_assign_f32(pts, cent))
