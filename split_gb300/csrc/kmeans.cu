@@ -16,6 +16,7 @@
 // unit order; the last block to finish a group of an image sums the group
 // partials in group order and forms c_new = c + S / n.  All sums therefore
 // have one fixed shape: the update is bit-reproducible.
+#include <limits.h>
 #include <math.h>
 
 #include "common.cuh"
@@ -237,74 +238,274 @@ __device__ __forceinline__ void advance(int& row, int& col, int s, int w) {
   }
 }
 
-// Process one unit: assign (unless update-only) and accumulate per-warp sums.
-template <int LAYOUT, int DIM, int MODE>
-__device__ void process_unit(const Image& im, int unit, Smem& sm,
-                             bool write_labels) {
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int64_t span = (int64_t)unit * kUnit + (int64_t)warp * kWarpSpan;
-  Loader<LAYOUT, DIM> ld{im.points, im.npoints, im.xy_scale, sm.lut};
-  int row = 0, col = 0;
-  const int64_t first = span + lane;
-  if (DIM == 5) {
-    row = (int)(first / im.width);
-    col = (int)(first - (int64_t)row * im.width);
+// ---- packed FP32x2 helpers (per-lane IEEE round-to-nearest, so results are
+// bit-identical to the scalar __fsub_rn / __fmul_rn / __fmaf_rn forms)
+__device__ __forceinline__ float2 fsub2(float2 a, float2 b) {
+  float2 r;
+  asm("{.reg .b64 a_, b_, r_;\n\t"
+      "mov.b64 a_, {%2, %3};\n\tmov.b64 b_, {%4, %5};\n\t"
+      "sub.rn.f32x2 r_, a_, b_;\n\tmov.b64 {%0, %1}, r_;}"
+      : "=f"(r.x), "=f"(r.y)
+      : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+  return r;
+}
+__device__ __forceinline__ float2 fmul2(float2 a, float2 b) {
+  float2 r;
+  asm("{.reg .b64 a_, b_, r_;\n\t"
+      "mov.b64 a_, {%2, %3};\n\tmov.b64 b_, {%4, %5};\n\t"
+      "mul.rn.f32x2 r_, a_, b_;\n\tmov.b64 {%0, %1}, r_;}"
+      : "=f"(r.x), "=f"(r.y)
+      : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+  return r;
+}
+__device__ __forceinline__ float2 ffma2(float2 a, float2 b, float2 c) {
+  float2 r;
+  asm("{.reg .b64 a_, b_, c_, r_;\n\t"
+      "mov.b64 a_, {%2, %3};\n\tmov.b64 b_, {%4, %5};\n\tmov.b64 c_, {%6, %7};\n\t"
+      "fma.rn.f32x2 r_, a_, b_, c_;\n\tmov.b64 {%0, %1}, r_;}"
+      : "=f"(r.x), "=f"(r.y)
+      : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y), "f"(c.x), "f"(c.y));
+  return r;
+}
+
+constexpr int kPx = 4;                 // consecutive pixels per lane
+constexpr int kBatch = 32 * kPx;       // pixels per warp batch
+static_assert(kWarpSpan % kBatch == 0, "whole batches per warp span");
+
+// The lane's kPx consecutive pixels starting at px0 (row, col of px0).
+template <int LAYOUT, int DIM>
+__device__ __forceinline__ void load_px(const Image& im, const float* lut, int64_t px0, int row,
+                                        int col, float (&f)[kPx][DIM], bool (&ok)[kPx]) {
+  const int64_t n = im.npoints;
+#pragma unroll
+  for (int j = 0; j < kPx; ++j) ok[j] = px0 + j < n;
+  if (LAYOUT == SPLIT_LAYOUT_FLOAT4) {
+    const float4* p = static_cast<const float4*>(im.points) + px0;
+#pragma unroll
+    for (int j = 0; j < kPx; ++j) {
+      const float4 v = ok[j] ? __ldg(p + j) : make_float4(0.f, 0.f, 0.f, 0.f);
+      f[j][0] = v.x;
+      f[j][1] = v.y;
+      f[j][2] = v.z;
+    }
+  } else if (LAYOUT == SPLIT_LAYOUT_RGB8) {
+    const uint8_t* p = static_cast<const uint8_t*>(im.points) + 3 * px0;
+#pragma unroll
+    for (int j = 0; j < kPx; ++j)
+#pragma unroll
+      for (int c = 0; c < 3; ++c) f[j][c] = ok[j] ? lut[__ldg(p + 3 * j + c)] : 0.0f;
+  } else {
+    const float* p = static_cast<const float*>(im.points);
+#pragma unroll
+    for (int d = 0; d < DIM; ++d)
+#pragma unroll
+      for (int j = 0; j < kPx; ++j) f[j][d] = ok[j] ? __ldg(p + (int64_t)d * n + px0 + j) : 0.0f;
   }
-  constexpr int CS = cstride(DIM);
-  for (int b = 0; b < kWarpSpan / 32; ++b) {
-    const int64_t px = first + (int64_t)b * 32;
-    if (b > 0 && DIM == 5) advance(row, col, 32, im.width);
-    const bool valid = px < im.npoints;
-    float f[DIM];
-    int lab = -1;
-    if (valid) ld.load(px, row, col, f);
-    if (MODE == kUpdateOnly) {
-      if (valid) {
-        lab = __ldg(im.labels_in + px);
-        if (lab < 0 || lab >= im.K) lab = -1;
+  if (DIM == 5 && LAYOUT != SPLIT_LAYOUT_PLANAR) {
+    int r = row, c = col;
+#pragma unroll
+    for (int j = 0; j < kPx; ++j) {
+      f[j][3] = __fmul_rn(im.xy_scale, (float)c);
+      f[j][4] = __fmul_rn(im.xy_scale, (float)r);
+      if (++c == im.width) {
+        c = 0;
+        ++r;
       }
+    }
+  }
+}
+
+// Nearest centroid among `mask` for the lane's pixels; the distance is the
+// fma chain of (x - c)^2 in dimension order, strict < in ascending k (ties to
+// the lowest k; label.cu:23-32, :98-105), evaluated on pixel pairs with the
+// packed f32x2 pipe.
+template <int DIM>
+__device__ __forceinline__ void nearest_px(const float (&f)[kPx][DIM],
+                                           const float* __restrict__ cs,
+                                           unsigned long long mask, int (&lab)[kPx]) {
+  constexpr int CS = cstride(DIM);
+  float best[kPx];
+#pragma unroll
+  for (int j = 0; j < kPx; ++j) {
+    best[j] = INFINITY;
+    lab[j] = 0;
+  }
+  while (mask) {
+    const int k = __ffsll((long long)mask) - 1;
+    mask &= mask - 1;
+    const float4 c0 = *reinterpret_cast<const float4*>(cs + k * CS);
+    const float cc[5] = {c0.x, c0.y, c0.z, c0.w, DIM == 5 ? cs[k * CS + 4] : 0.0f};
+#pragma unroll
+    for (int q = 0; q < kPx / 2; ++q) {
+      const int a = 2 * q, b = 2 * q + 1;
+      float2 t = fsub2(make_float2(f[a][0], f[b][0]), make_float2(cc[0], cc[0]));
+      float2 d = fmul2(t, t);
+#pragma unroll
+      for (int dd = 1; dd < DIM; ++dd) {
+        t = fsub2(make_float2(f[a][dd], f[b][dd]), make_float2(cc[dd], cc[dd]));
+        d = ffma2(t, t, d);
+      }
+      if (d.x < best[a]) {
+        best[a] = d.x;
+        lab[a] = k;
+      }
+      if (d.y < best[b]) {
+        best[b] = d.y;
+        lab[b] = k;
+      }
+    }
+  }
+}
+
+// Warp-collective: add the per-lane sums `acc` (label l, warp-uniform) to the
+// warp's shared slot.
+template <int DIM>
+__device__ __forceinline__ void flush_acc(Smem& sm, int warp, int l, const float (&acc)[DIM],
+                                          int n) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int d = 0; d < DIM; ++d) {
+    const float s = warp_sum(acc[d]);
+    if (lane == 0) sm.acc[warp][l * kMaxDim + d] = __fadd_rn(sm.acc[warp][l * kMaxDim + d], s);
+  }
+  const int c = __reduce_add_sync(0xffffffffu, n);
+  if (lane == 0) sm.cnt[warp][l] += c;
+}
+
+// Process one unit: assign (unless update-only) and accumulate per-warp sums
+// of (x - c_label).  Each lane holds kPx consecutive pixels of a 128-pixel
+// warp batch.  While consecutive batches carry one label, every lane keeps a
+// register running sum; a batch with several labels is reduced label by label
+// in ascending order.  All orders depend only on the data.
+template <int LAYOUT, int DIM, int MODE>
+__device__ void process_unit(const Image& im, int unit, Smem& sm, bool write_labels) {
+  const unsigned full = 0xffffffffu;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  constexpr int CS = cstride(DIM);
+  int64_t px0 = (int64_t)unit * kUnit + (int64_t)warp * kWarpSpan + (int64_t)lane * kPx;
+  int row = 0, col = 0;
+  if (DIM == 5 && LAYOUT != SPLIT_LAYOUT_PLANAR) {
+    row = (int)(px0 / im.width);
+    col = (int)(px0 - (int64_t)row * im.width);
+  }
+  const bool vec_labels = (reinterpret_cast<uintptr_t>(MODE == kUpdateOnly ? im.labels_in : im.labels) & 15) == 0;
+  int acc_l = -1, acc_n = 0;
+  float acc[DIM];
+#pragma unroll
+  for (int d = 0; d < DIM; ++d) acc[d] = 0.0f;
+
+  for (int b = 0; b < kWarpSpan / kBatch; ++b, px0 += kBatch) {
+    if (b > 0 && DIM == 5 && LAYOUT != SPLIT_LAYOUT_PLANAR) advance(row, col, kBatch, im.width);
+    if (__all_sync(full, px0 >= im.npoints)) break;
+    float f[kPx][DIM];
+    bool ok[kPx];
+    load_px<LAYOUT, DIM>(im, sm.lut, px0, row, col, f, ok);
+    const bool all_ok = ok[kPx - 1];
+    int lab[kPx];
+    if (MODE == kUpdateOnly) {
+      if (all_ok && vec_labels) {
+        const int4 v = __ldg(reinterpret_cast<const int4*>(im.labels_in + px0));
+        lab[0] = v.x; lab[1] = v.y; lab[2] = v.z; lab[3] = v.w;
+      } else {
+#pragma unroll
+        for (int j = 0; j < kPx; ++j) lab[j] = ok[j] ? __ldg(im.labels_in + px0 + j) : -1;
+      }
+#pragma unroll
+      for (int j = 0; j < kPx; ++j)
+        if (!ok[j] || lab[j] < 0 || lab[j] >= im.K) lab[j] = -1;
     } else {
       // bounding box of the batch, then the candidate clusters
       float lo[DIM], hi[DIM];
       bool nan = false;
 #pragma unroll
       for (int d = 0; d < DIM; ++d) {
-        nan |= valid && (f[d] != f[d]);
-        lo[d] = fkey_inv(__reduce_min_sync(0xffffffffu, fkey(valid ? f[d] : INFINITY)));
-        hi[d] = fkey_inv(__reduce_max_sync(0xffffffffu, fkey(valid ? f[d] : -INFINITY)));
+        float a = INFINITY, z = -INFINITY;
+#pragma unroll
+        for (int j = 0; j < kPx; ++j) {
+          if (ok[j]) {
+            nan |= f[j][d] != f[j][d];
+            a = fminf(a, f[j][d]);
+            z = fmaxf(z, f[j][d]);
+          }
+        }
+        lo[d] = fkey_inv(__reduce_min_sync(full, fkey(a)));
+        hi[d] = fkey_inv(__reduce_max_sync(full, fkey(z)));
       }
       unsigned long long mask;
-      if (__any_sync(0xffffffffu, nan))
+      if (__any_sync(full, nan))
         mask = im.K >= 64 ? ~0ull : ((1ull << im.K) - 1ull);
       else
         mask = candidates<DIM>(lo, hi, sm.cent, im.K);
-      if (valid) {
-        lab = nearest<DIM>(f, sm.cent, mask);
-        if (write_labels) im.labels[px] = lab;
+      nearest_px<DIM>(f, sm.cent, mask, lab);
+      if (write_labels) {
+        if (all_ok && vec_labels) {
+          *reinterpret_cast<int4*>(im.labels + px0) = make_int4(lab[0], lab[1], lab[2], lab[3]);
+        } else {
+#pragma unroll
+          for (int j = 0; j < kPx; ++j)
+            if (ok[j]) im.labels[px0 + j] = lab[j];
+        }
       }
+#pragma unroll
+      for (int j = 0; j < kPx; ++j)
+        if (!ok[j]) lab[j] = -1;
     }
     if (MODE == kAssignOnly) continue;
-    // centred contributions x - c_label
-    float v[DIM];
-    if (lab >= 0) {
+
+    // ---- accumulate x - c_label
+    int mn = INT_MAX, mx = -1;
 #pragma unroll
-      for (int d = 0; d < DIM; ++d) v[d] = __fsub_rn(f[d], sm.cent[lab * CS + d]);
-    }
-    unsigned todo = __ballot_sync(0xffffffffu, lab >= 0);
-    while (todo) {
-      const int leader = __ffs(todo) - 1;
-      const int l = __shfl_sync(0xffffffffu, lab, leader);
-      const bool mine = (lab == l);
-      const unsigned m = __ballot_sync(0xffffffffu, mine);
-      todo &= ~m;
-#pragma unroll
-      for (int d = 0; d < DIM; ++d) {
-        const float s = warp_sum(mine ? v[d] : 0.0f);
-        if (lane == 0) sm.acc[warp][l * kMaxDim + d] = __fadd_rn(sm.acc[warp][l * kMaxDim + d], s);
+    for (int j = 0; j < kPx; ++j) {
+      if (lab[j] >= 0) {
+        mn = min(mn, lab[j]);
+        mx = max(mx, lab[j]);
       }
-      if (lane == 0) sm.cnt[warp][l] += __popc(m);
+    }
+    mn = __reduce_min_sync(full, mn);
+    mx = __reduce_max_sync(full, mx);
+    if (mx < 0) continue;
+    if (mn == mx) {
+      if (mn != acc_l) {
+        if (acc_l >= 0) flush_acc<DIM>(sm, warp, acc_l, acc, acc_n);
+        acc_l = mn;
+        acc_n = 0;
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) acc[d] = 0.0f;
+      }
+#pragma unroll
+      for (int j = 0; j < kPx; ++j) {
+        if (lab[j] >= 0) {
+#pragma unroll
+          for (int d = 0; d < DIM; ++d)
+            acc[d] = __fadd_rn(acc[d], __fsub_rn(f[j][d], sm.cent[mn * CS + d]));
+          ++acc_n;
+        }
+      }
+    } else {
+      if (acc_l >= 0) flush_acc<DIM>(sm, warp, acc_l, acc, acc_n);
+      acc_l = -1;
+      for (int l = mn; l != INT_MAX;) {
+        float s[DIM];
+        int c = 0;
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) s[d] = 0.0f;
+        int nxt = INT_MAX;
+#pragma unroll
+        for (int j = 0; j < kPx; ++j) {
+          if (lab[j] == l) {
+#pragma unroll
+            for (int d = 0; d < DIM; ++d) s[d] = __fadd_rn(s[d], __fsub_rn(f[j][d], sm.cent[l * CS + d]));
+            ++c;
+          } else if (lab[j] > l) {
+            nxt = min(nxt, lab[j]);
+          }
+        }
+        flush_acc<DIM>(sm, warp, l, s, c);
+        l = __reduce_min_sync(full, nxt);
+      }
     }
   }
+  if (MODE != kAssignOnly && acc_l >= 0) flush_acc<DIM>(sm, warp, acc_l, acc, acc_n);
 }
 
 // Sum the warp slots in warp order into a unit record; clear the slots.
@@ -449,7 +650,7 @@ __device__ void finish_image(const Params& p, int img, const Image& im, int it,
 }
 
 template <int LAYOUT, int DIM, int MODE>
-__global__ void __launch_bounds__(kThreads) kmeans_kernel(Params p) {
+__global__ void __launch_bounds__(kThreads, 4) kmeans_kernel(Params p) {
   __shared__ Smem sm;
   for (int i = threadIdx.x; i < kWarps * kMaxK * kMaxDim; i += blockDim.x)
     (&sm.acc[0][0])[i] = 0.0f;
