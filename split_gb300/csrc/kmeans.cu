@@ -302,14 +302,23 @@ __device__ __forceinline__ void load_px(const Image& im, const float* lut, int64
       for (int j = 0; j < kPx; ++j) f[j][d] = ok[j] ? __ldg(p + (int64_t)d * n + px0 + j) : 0.0f;
   }
   if (DIM == 5 && LAYOUT != SPLIT_LAYOUT_PLANAR) {
-    int r = row, c = col;
+    if (col + kPx <= im.width) {
+      const float fy = __fmul_rn(im.xy_scale, (float)row);
 #pragma unroll
-    for (int j = 0; j < kPx; ++j) {
-      f[j][3] = __fmul_rn(im.xy_scale, (float)c);
-      f[j][4] = __fmul_rn(im.xy_scale, (float)r);
-      if (++c == im.width) {
-        c = 0;
-        ++r;
+      for (int j = 0; j < kPx; ++j) {
+        f[j][3] = __fmul_rn(im.xy_scale, (float)(col + j));
+        f[j][4] = fy;
+      }
+    } else {
+      int r = row, c = col;
+#pragma unroll
+      for (int j = 0; j < kPx; ++j) {
+        f[j][3] = __fmul_rn(im.xy_scale, (float)c);
+        f[j][4] = __fmul_rn(im.xy_scale, (float)r);
+        if (++c == im.width) {
+          c = 0;
+          ++r;
+        }
       }
     }
   }
@@ -414,28 +423,53 @@ __device__ void process_unit(const Image& im, int unit, Smem& sm, bool write_lab
       for (int j = 0; j < kPx; ++j)
         if (!ok[j] || lab[j] < 0 || lab[j] >= im.K) lab[j] = -1;
     } else {
-      // bounding box of the batch, then the candidate clusters
+      // Bounding box of the batch, then the candidate clusters.  fminf /
+      // fmaxf skip NaN: a NaN pixel gets label 0 whatever the mask (every
+      // distance compares false), and the box still bounds all other pixels.
       float lo[DIM], hi[DIM];
-      bool nan = false;
+      constexpr bool kXY = DIM == 5 && LAYOUT != SPLIT_LAYOUT_PLANAR;
+      constexpr int kBoxDims = kXY ? 3 : DIM;
+      const bool warp_all_ok = __all_sync(full, all_ok);
 #pragma unroll
-      for (int d = 0; d < DIM; ++d) {
-        float a = INFINITY, z = -INFINITY;
+      for (int d = 0; d < kBoxDims; ++d) {
+        float a, z;
+        if (warp_all_ok) {
+          a = fminf(fminf(f[0][d], f[1][d]), fminf(f[2][d], f[3][d]));
+          z = fmaxf(fmaxf(f[0][d], f[1][d]), fmaxf(f[2][d], f[3][d]));
+        } else {
+          a = INFINITY;
+          z = -INFINITY;
 #pragma unroll
-        for (int j = 0; j < kPx; ++j) {
-          if (ok[j]) {
-            nan |= f[j][d] != f[j][d];
-            a = fminf(a, f[j][d]);
-            z = fmaxf(z, f[j][d]);
+          for (int j = 0; j < kPx; ++j) {
+            if (ok[j]) {
+              a = fminf(a, f[j][d]);
+              z = fmaxf(z, f[j][d]);
+            }
           }
         }
         lo[d] = fkey_inv(__reduce_min_sync(full, fkey(a)));
         hi[d] = fkey_inv(__reduce_max_sync(full, fkey(z)));
       }
-      unsigned long long mask;
-      if (__any_sync(full, nan))
-        mask = im.K >= 64 ? ~0ull : ((1ull << im.K) - 1ull);
-      else
-        mask = candidates<DIM>(lo, hi, sm.cent, im.K);
+      if (kXY) {
+        // the batch's pixels are consecutive: lane 0 holds the first, lane 31
+        // the last; a batch that wraps a row spans whole columns
+        const int r0 = __shfl_sync(full, row, 0), c0 = __shfl_sync(full, col, 0);
+        const int64_t last = min(px0 - (int64_t)lane * kPx + kBatch, im.npoints) - 1;
+        const int64_t first = px0 - (int64_t)lane * kPx;
+        const int c1 = c0 + (int)(last - first);
+        if (c1 < im.width) {
+          lo[3] = __fmul_rn(im.xy_scale, (float)c0);
+          hi[3] = __fmul_rn(im.xy_scale, (float)c1);
+          lo[4] = hi[4] = __fmul_rn(im.xy_scale, (float)r0);
+        } else {
+          const int r1 = (int)(last / im.width);
+          lo[3] = 0.0f;
+          hi[3] = __fmul_rn(im.xy_scale, (float)(im.width - 1));
+          lo[4] = __fmul_rn(im.xy_scale, (float)r0);
+          hi[4] = __fmul_rn(im.xy_scale, (float)r1);
+        }
+      }
+      const unsigned long long mask = candidates<DIM>(lo, hi, sm.cent, im.K);
       nearest_px<DIM>(f, sm.cent, mask, lab);
       if (write_labels) {
         if (all_ok && vec_labels) {
@@ -472,12 +506,14 @@ __device__ void process_unit(const Image& im, int unit, Smem& sm, bool write_lab
 #pragma unroll
         for (int d = 0; d < DIM; ++d) acc[d] = 0.0f;
       }
+      float c[DIM];
+#pragma unroll
+      for (int d = 0; d < DIM; ++d) c[d] = sm.cent[mn * CS + d];
 #pragma unroll
       for (int j = 0; j < kPx; ++j) {
         if (lab[j] >= 0) {
 #pragma unroll
-          for (int d = 0; d < DIM; ++d)
-            acc[d] = __fadd_rn(acc[d], __fsub_rn(f[j][d], sm.cent[mn * CS + d]));
+          for (int d = 0; d < DIM; ++d) acc[d] = __fadd_rn(acc[d], __fsub_rn(f[j][d], c[d]));
           ++acc_n;
         }
       }
@@ -604,20 +640,22 @@ __device__ void finish_image(const Params& p, int img, const Image& im, int it,
   const float* c_old = p.cur + ((size_t)(it & 1) * p.nimages + img) * (kMaxK * 8);
   float* c_new = p.cur + ((size_t)((it + 1) & 1) * p.nimages + img) * (kMaxK * 8);
   const int* cnt = reinterpret_cast<const int*>(total + kMaxK * kMaxDim);
-  if (threadIdx.x == 0) sdelta = 0.0f;
+  __shared__ float sdiff[kMaxK * kMaxDim];
+  for (int idx = threadIdx.x; idx < im.K * DIM; idx += blockDim.x) {
+    const int k = idx / DIM, d = idx % DIM;
+    const float c = __ldcg(c_old + k * 8 + d);
+    const int n = __ldcg(cnt + k);
+    float cn = c;
+    if (n > 0) cn = __fadd_rn(c, __fdiv_rn(__ldcg(total + k * kMaxDim + d), (float)n));
+    __stcg(c_new + k * 8 + d, cn);
+    const float df = __fsub_rn(cn, c);
+    sdiff[idx] = __fmul_rn(df, df);
+  }
   __syncthreads();
   if (threadIdx.x < 32) {
+    // squared centroid shift, summed in a fixed order
     float acc = 0.0f;
-    for (int idx = threadIdx.x; idx < im.K * DIM; idx += 32) {
-      const int k = idx / DIM, d = idx % DIM;
-      const float c = __ldcg(c_old + k * 8 + d);
-      const int n = __ldcg(cnt + k);
-      float cn = c;
-      if (n > 0) cn = __fadd_rn(c, __fdiv_rn(__ldcg(total + k * kMaxDim + d), (float)n));
-      __stcg(c_new + k * 8 + d, cn);
-      const float df = __fsub_rn(cn, c);
-      acc = __fmaf_rn(df, df, acc);
-    }
+    for (int idx = threadIdx.x; idx < im.K * DIM; idx += 32) acc = __fadd_rn(acc, sdiff[idx]);
     acc = warp_sum(acc);
     if (threadIdx.x == 0) sdelta = acc;
   }
