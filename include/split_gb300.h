@@ -54,6 +54,12 @@ enum {
 };
 /* For FLOAT4 and RGB8 layouts, dim is 3 (colour) or 5 (colour plus
  * xy_scale * column and xy_scale * row, synthesised from the pixel index). */
+/* Flag or-ed into a FLOAT4 layout: the caller guarantees every colour feature
+ * lies in [0, 1] (true of split_pack_rgb8 output; always true of RGB8).  The
+ * assignment then bounds colour distances by the unit cube instead of
+ * measuring each batch.  Features outside [0, 1] under this flag may be
+ * mislabelled. */
+#define SPLIT_FEATURES_UNIT_RANGE 0x100
 
 /* ---- label conventions / policies -------------------------------------- */
 enum {

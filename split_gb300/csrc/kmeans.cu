@@ -38,6 +38,7 @@ enum Mode { kCluster = 0, kUpdateOnly = 1, kAssignOnly = 2 };
 
 struct Image {
   const void* points;
+  int unit_range;           // colour features known to lie in [0, 1]
   int64_t npoints;
   int width;
   float xy_scale;
@@ -430,8 +431,14 @@ __device__ void process_unit(const Image& im, int unit, Smem& sm, bool write_lab
       constexpr bool kXY = DIM == 5 && LAYOUT != SPLIT_LAYOUT_PLANAR;
       constexpr int kBoxDims = kXY ? 3 : DIM;
       const bool warp_all_ok = __all_sync(full, all_ok);
+      const bool unit = LAYOUT == SPLIT_LAYOUT_RGB8 || (LAYOUT == SPLIT_LAYOUT_FLOAT4 && im.unit_range);
 #pragma unroll
       for (int d = 0; d < kBoxDims; ++d) {
+        if (unit && d < 3) {
+          lo[d] = 0.0f;
+          hi[d] = 1.0f;
+          continue;
+        }
         float a, z;
         if (warp_all_ok) {
           a = fminf(fminf(f[0][d], f[1][d]), fminf(f[2][d], f[3][d]));
@@ -868,6 +875,7 @@ static int dispatch(int layout, int dim, Params& p, cudaStream_t st) {
 
 static bool valid_features(const void* points, int layout, int dim, int64_t n,
                            int width, int K) {
+  layout &= ~SPLIT_FEATURES_UNIT_RANGE;
   if (!points || n <= 0 || n > 0x7fffffffLL || K < 1 || K > kMaxK) return false;
   if (dim != 3 && dim != 5) return false;
   if (layout < SPLIT_LAYOUT_PLANAR || layout > SPLIT_LAYOUT_RGB8) return false;
@@ -882,6 +890,8 @@ static int run(int mode, const void* points, int layout, int dim, int64_t n,
                const int32_t* labels_in, void* ws, size_t ws_bytes, int max_iter,
                float threshold, int32_t* d_iter, cudaStream_t st) {
   if (!valid_features(points, layout, dim, n, width, K)) return SPLIT_ERR_INVALID;
+  const int unit_range = (layout & SPLIT_FEATURES_UNIT_RANGE) ? 1 : 0;
+  layout &= ~SPLIT_FEATURES_UNIT_RANGE;
   const int units = units_of(n), groups = groups_of(units);
   Layout l = carve(nullptr, units, groups, 1);
   if (!ws || ws_bytes < l.bytes || (reinterpret_cast<uintptr_t>(ws) & 255))
@@ -890,6 +900,7 @@ static int run(int mode, const void* points, int layout, int dim, int64_t n,
   Params p{};
   Image& im = p.img0;
   im.points = points;
+  im.unit_range = unit_range;
   im.npoints = n;
   im.width = width;
   im.xy_scale = xy_scale;

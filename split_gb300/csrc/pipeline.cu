@@ -91,7 +91,10 @@ extern "C" int split_pipeline_run(const uint8_t* rgb, int width, int height,
   SG_TRY(mark(2));
   const void* pts = p.features == SPLIT_LAYOUT_FLOAT4 ? static_cast<const void*>(l.features4)
                                                        : static_cast<const void*>(rgb);
-  SG_TRY(split_kmeans_cluster(pts, p.features, p.dim, n, width, p.xy_scale, centroids,
+  // packed features are byte / 255: inside the unit cube
+  const int layout = p.features == SPLIT_LAYOUT_FLOAT4 ? (SPLIT_LAYOUT_FLOAT4 | SPLIT_FEATURES_UNIT_RANGE)
+                                                        : p.features;
+  SG_TRY(split_kmeans_cluster(pts, layout, p.dim, n, width, p.xy_scale, centroids,
                               p.nclusters, cluster_labels, l.km_ws, l.km_bytes, p.kmeans_iters,
                               p.kmeans_threshold, nullptr, stream));
   SG_TRY(mark(3));

@@ -10,6 +10,7 @@ from . import _native as N
 from ._util import Workspace, ensure_workspace, ptr, require_cuda, stream_handle
 
 PLANAR, FLOAT4, RGB8 = N.LAYOUT_PLANAR, N.LAYOUT_FLOAT4, N.LAYOUT_RGB8
+UNIT_RANGE = 0x100  # or into FLOAT4: colour features promised in [0, 1]
 
 
 def cluster_workspace(npoints: int, nclusters: int, dim: int) -> int:
@@ -30,6 +31,7 @@ def calculate_centroids_workspace(npoints: int, ncentroids: int, dim: int = 3) -
 def _features(points: torch.Tensor, layout: int, dim: int | None):
     """Returns (npoints, dim) for a points tensor in the given layout."""
     require_cuda(points, "points")
+    layout &= ~UNIT_RANGE
     if layout == PLANAR:
         if points.dtype != torch.float32 or points.dim() != 2:
             raise ValueError("planar points must be a float32 (dim, npoints) tensor")

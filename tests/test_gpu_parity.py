@@ -173,3 +173,25 @@ def test_kmeans_assign_pruning_exact(cuda, k):
     lab = torch.empty(n, dtype=torch.int32, device=cuda)
     kmeans.label_points(_t(cent, cuda), _t(pts, cuda), lab, None, dim=5)
     assert np.array_equal(lab.cpu().numpy(), oracle.kmeans_assign_f32(pts, cent))
+
+
+def test_kmeans_unit_range_flag(cuda):
+    """The unit-range promise on packed features changes no label."""
+    import torch
+    from split_gb300 import color, kmeans
+    w, h = 333, 211
+    rgb = synth.voronoi_rgb8(21, w, h, 40, npalette=8, illum_gradient=True, sigma=3.0)
+    d_rgb = _t(rgb, cuda)
+    f4 = torch.empty((w * h, 4), dtype=torch.float32, device=cuda)
+    color.pack_rgb8(d_rgb, f4)
+    c0 = _t(synth.pick_centroids(21, rgb, 12, 5), cuda)
+    out = []
+    for layout in (kmeans.FLOAT4, kmeans.FLOAT4 | kmeans.UNIT_RANGE, kmeans.RGB8):
+        cent = c0.clone()
+        lab = torch.empty(w * h, dtype=torch.int32, device=cuda)
+        pts = d_rgb.view(-1, 3) if layout == kmeans.RGB8 else f4
+        kmeans.cluster(pts, cent, lab, None, max_iter=5, threshold=-1.0, layout=layout, dim=5,
+                       width=w)
+        out.append((lab.cpu().numpy(), cent.cpu().numpy()))
+    for lab, cent in out[1:]:
+        assert np.array_equal(lab, out[0][0]) and np.array_equal(cent, out[0][1])
