@@ -26,8 +26,8 @@ namespace km {
 
 constexpr int kThreads = 256;
 constexpr int kWarps = kThreads / 32;
-constexpr int kUnit = 4096;            // pixels per unit
-constexpr int kWarpSpan = kUnit / kWarps;  // 512 pixels per warp per unit
+constexpr int kUnit = 8192;            // pixels per unit
+constexpr int kWarpSpan = kUnit / kWarps;  // 1024 pixels per warp per unit
 constexpr int kGroup = 32;             // units per group
 constexpr int kMaxK = 64;
 constexpr int kMaxDim = 5;
@@ -219,13 +219,16 @@ constexpr int kChunk = 8;     // records summed per thread in one pass
 constexpr int kChunks = 8;    // chunks per pass (64 records per pass)
 constexpr int kVals = kMaxK * kMaxDim + kMaxK;
 
+// Warp slots are double-buffered by unit parity: warp 0 reduces a finished
+// unit's slots while the other warps already accumulate the next unit.
 struct Smem {
   alignas(16) float cent[kMaxK * 8];
   float scratch[kChunks][kVals];
-  float acc[kWarps][kMaxK * kMaxDim];
-  int cnt[kWarps][kMaxK];
+  float acc[2][kWarps][kMaxK * kMaxDim];
+  int cnt[2][kWarps][kMaxK];
   float lut[256];
-  int unit;
+  int next[2];   // prefetched work-counter values
+  int pend[2];   // unit whose group became complete, per buffer parity
   int flag;
 };
 
@@ -370,16 +373,17 @@ __device__ __forceinline__ void nearest_px(const float (&f)[kPx][DIM],
 // Warp-collective: add the per-lane sums `acc` (label l, warp-uniform) to the
 // warp's shared slot.
 template <int DIM>
-__device__ __forceinline__ void flush_acc(Smem& sm, int warp, int l, const float (&acc)[DIM],
-                                          int n) {
+__device__ __forceinline__ void flush_acc(Smem& sm, int buf, int warp, int l,
+                                          const float (&acc)[DIM], int n) {
   const int lane = threadIdx.x & 31;
 #pragma unroll
   for (int d = 0; d < DIM; ++d) {
     const float s = warp_sum(acc[d]);
-    if (lane == 0) sm.acc[warp][l * kMaxDim + d] = __fadd_rn(sm.acc[warp][l * kMaxDim + d], s);
+    if (lane == 0)
+      sm.acc[buf][warp][l * kMaxDim + d] = __fadd_rn(sm.acc[buf][warp][l * kMaxDim + d], s);
   }
   const int c = __reduce_add_sync(0xffffffffu, n);
-  if (lane == 0) sm.cnt[warp][l] += c;
+  if (lane == 0) sm.cnt[buf][warp][l] += c;
 }
 
 // Process one unit: assign (unless update-only) and accumulate per-warp sums
@@ -388,10 +392,16 @@ __device__ __forceinline__ void flush_acc(Smem& sm, int warp, int l, const float
 // register running sum; a batch with several labels is reduced label by label
 // in ascending order.  All orders depend only on the data.
 template <int LAYOUT, int DIM, int MODE>
-__device__ void process_unit(const Image& im, int unit, Smem& sm, bool write_labels) {
+__device__ void process_unit(const Image& im, int unit, Smem& sm, int buf, bool write_labels) {
   const unsigned full = 0xffffffffu;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   constexpr int CS = cstride(DIM);
+  if (MODE != kAssignOnly) {
+    // this warp's slot of buffer `buf` (read by warp 0 two units ago)
+    for (int i = lane; i < im.K * kMaxDim; i += 32) sm.acc[buf][warp][i] = 0.0f;
+    for (int i = lane; i < im.K; i += 32) sm.cnt[buf][warp][i] = 0;
+    __syncwarp();
+  }
   int64_t px0 = (int64_t)unit * kUnit + (int64_t)warp * kWarpSpan + (int64_t)lane * kPx;
   int row = 0, col = 0;
   if (DIM == 5 && LAYOUT != SPLIT_LAYOUT_PLANAR) {
@@ -507,7 +517,7 @@ __device__ void process_unit(const Image& im, int unit, Smem& sm, bool write_lab
     if (mx < 0) continue;
     if (mn == mx) {
       if (mn != acc_l) {
-        if (acc_l >= 0) flush_acc<DIM>(sm, warp, acc_l, acc, acc_n);
+        if (acc_l >= 0) flush_acc<DIM>(sm, buf, warp, acc_l, acc, acc_n);
         acc_l = mn;
         acc_n = 0;
 #pragma unroll
@@ -525,7 +535,7 @@ __device__ void process_unit(const Image& im, int unit, Smem& sm, bool write_lab
         }
       }
     } else {
-      if (acc_l >= 0) flush_acc<DIM>(sm, warp, acc_l, acc, acc_n);
+      if (acc_l >= 0) flush_acc<DIM>(sm, buf, warp, acc_l, acc, acc_n);
       acc_l = -1;
       for (int l = mn; l != INT_MAX;) {
         float s[DIM];
@@ -543,33 +553,30 @@ __device__ void process_unit(const Image& im, int unit, Smem& sm, bool write_lab
             nxt = min(nxt, lab[j]);
           }
         }
-        flush_acc<DIM>(sm, warp, l, s, c);
+        flush_acc<DIM>(sm, buf, warp, l, s, c);
         l = __reduce_min_sync(full, nxt);
       }
     }
   }
-  if (MODE != kAssignOnly && acc_l >= 0) flush_acc<DIM>(sm, warp, acc_l, acc, acc_n);
+  if (MODE != kAssignOnly && acc_l >= 0) flush_acc<DIM>(sm, buf, warp, acc_l, acc, acc_n);
 }
 
-// Sum the warp slots in warp order into a unit record; clear the slots.
-__device__ void block_to_record(Smem& sm, float* rec, int K, int dim) {
-  __syncthreads();
-  for (int idx = threadIdx.x; idx < K * kMaxDim; idx += blockDim.x) {
+// Warp 0: sum the 8 warp slots of buffer `buf` in warp order into a unit
+// record.
+__device__ __forceinline__ void warp_to_record(const Smem& sm, int buf, float* rec, int K,
+                                               int dim) {
+  const int lane = threadIdx.x & 31;
+  for (int idx = lane; idx < K * kMaxDim; idx += 32) {
+    if ((idx % kMaxDim) >= dim) continue;
     float s = 0.0f;
 #pragma unroll
-    for (int w = 0; w < kWarps; ++w) {
-      s = __fadd_rn(s, sm.acc[w][idx]);
-      sm.acc[w][idx] = 0.0f;
-    }
-    if ((idx % kMaxDim) < dim) __stcg(rec + idx, s);
+    for (int w = 0; w < kWarps; ++w) s = __fadd_rn(s, sm.acc[buf][w][idx]);
+    __stcg(rec + idx, s);
   }
-  for (int k = threadIdx.x; k < K; k += blockDim.x) {
+  for (int k = lane; k < K; k += 32) {
     int c = 0;
 #pragma unroll
-    for (int w = 0; w < kWarps; ++w) {
-      c += sm.cnt[w][k];
-      sm.cnt[w][k] = 0;
-    }
+    for (int w = 0; w < kWarps; ++w) c += sm.cnt[buf][w][k];
     __stcg(reinterpret_cast<int*>(rec + kMaxK * kMaxDim) + k, c);
   }
 }
@@ -694,32 +701,71 @@ __device__ void finish_image(const Params& p, int img, const Image& im, int it,
   }
 }
 
+// Sums the group of unit u (whose last unit just completed); the last group
+// of the image then forms the image total and the new centroids.
+template <int DIM, int MODE>
+__device__ void group_task(const Params& p, Smem& sm, int u, int it) {
+  const int img = find_image(p, u);
+  const Image& im = image_of(p, img);
+  const int lu = u - im.unit_begin;
+  const int g = lu / kGroup;
+  const int gbeg = g * kGroup;
+  const int gcount = min(kGroup, im.nunits - gbeg);
+  __threadfence();
+  float* grec = p.group_part + (size_t)(im.group_begin + g) * kRec;
+  sum_records(sm, p.unit_part + (size_t)(im.unit_begin + gbeg) * kRec, gcount, grec, im.K, DIM);
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const unsigned prev = atomicAdd(&p.image_cnt[img], 1u);
+    sm.flag = (prev == (unsigned)im.ngroups - 1);
+    if (sm.flag) p.image_cnt[img] = 0;
+  }
+  __syncthreads();
+  if (!sm.flag) return;
+  __threadfence();
+  // image total into the record slot of the image's first unit (its partial
+  // was consumed by the first group's sum)
+  float* tot = p.unit_part + (size_t)im.unit_begin * kRec;
+  sum_records(sm, p.group_part + (size_t)im.group_begin * kRec, im.ngroups, tot, im.K, DIM);
+  __threadfence();
+  __syncthreads();
+  finish_image<DIM, MODE>(p, img, im, it, tot);
+  __syncthreads();
+}
+
 template <int LAYOUT, int DIM, int MODE>
 __global__ void __launch_bounds__(kThreads, 4) kmeans_kernel(Params p) {
   __shared__ Smem sm;
-  for (int i = threadIdx.x; i < kWarps * kMaxK * kMaxDim; i += blockDim.x)
-    (&sm.acc[0][0])[i] = 0.0f;
-  for (int i = threadIdx.x; i < kWarps * kMaxK; i += blockDim.x) (&sm.cnt[0][0])[i] = 0;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (LAYOUT == SPLIT_LAYOUT_RGB8)
     for (int i = threadIdx.x; i < 256; i += blockDim.x) sm.lut[i] = (float)i / 255.0f;
-  __syncthreads();
 
   for (int it = 0; it < p.max_iter; ++it) {
-    if (blockIdx.x == 0 && threadIdx.x == 0) p.hdr->work_counter[(it + 1) & 1] = 0;
-    int cached = -1;
-    for (;;) {
-      if (threadIdx.x == 0) sm.unit = (int)atomicAdd(&p.hdr->work_counter[it & 1], 1u);
-      __syncthreads();
-      const int raw = sm.unit;
-      __syncthreads();
-      if (raw >= p.total_units) break;
+    unsigned* counter = &p.hdr->work_counter[it & 1];
+    if (threadIdx.x == 0) {
+      if (blockIdx.x == 0) p.hdr->work_counter[(it + 1) & 1] = 0;
+      sm.next[0] = (int)atomicAdd(counter, 1u);
+      sm.pend[0] = sm.pend[1] = -1;
+    }
+    __syncthreads();
+    int cached = -1, npar = 0, buf = 0;
+    int raw = sm.next[0];
+    while (raw < p.total_units) {
       // odd iterations walk the units backwards: they start on the units the
       // previous iteration touched last, which are still resident in L2
       const int u = (it & 1) ? p.total_units - 1 - raw : raw;
       const int img = find_image(p, u);
       const Image& im = image_of(p, img);
-      if (MODE != kAssignOnly && *(volatile int*)&p.state[img].done) continue;
+      if (threadIdx.x == 0) sm.next[npar ^ 1] = (int)atomicAdd(counter, 1u);
+      if (MODE != kAssignOnly && *(volatile int*)&p.state[img].done) {
+        __syncthreads();
+        raw = sm.next[npar ^ 1];
+        npar ^= 1;
+        continue;
+      }
       if (img != cached) {
+        // every warp is past the previous unit (its end-of-unit barrier)
         if (MODE == kAssignOnly)
           load_centroids<DIM>(p.cur + (size_t)img * (kMaxK * 8), im.K, sm.cent);
         else
@@ -731,48 +777,36 @@ __global__ void __launch_bounds__(kThreads, 4) kmeans_kernel(Params p) {
       const int lu = u - im.unit_begin;
       const bool wl = (MODE == kAssignOnly) ||
                       (MODE == kCluster && (im.threshold >= 0.0f || it == im.max_iter - 1));
-      process_unit<LAYOUT, DIM, MODE>(im, lu, sm, wl);
+      process_unit<LAYOUT, DIM, MODE>(im, lu, sm, buf, wl);
+      __syncthreads();  // the unit's slots are complete; next[] and pend[] visible
+      raw = sm.next[npar ^ 1];
+      npar ^= 1;
       if (MODE == kAssignOnly) continue;
-      float* rec = p.unit_part + (size_t)u * kRec;
-      block_to_record(sm, rec, im.K, DIM);
-      // publish the unit partial; the last unit of a group sums the group
-      __threadfence();
-      __syncthreads();
-      const int g = lu / kGroup;
-      const int gbeg = g * kGroup;
-      const int gcount = min(kGroup, im.nunits - gbeg);
-      if (threadIdx.x == 0) {
-        const unsigned prev = atomicAdd(&p.group_cnt[im.group_begin + g], 1u);
-        sm.flag = (prev == (unsigned)gcount - 1);
-        if (sm.flag) p.group_cnt[im.group_begin + g] = 0;
+      const int task = sm.pend[buf ^ 1];
+      if (task >= 0) {
+        group_task<DIM, MODE>(p, sm, task, it);
+        if (threadIdx.x == 0) sm.pend[buf ^ 1] = -1;
       }
-      __syncthreads();
-      if (!sm.flag) continue;
-      __threadfence();
-      float* grec = p.group_part + (size_t)(im.group_begin + g) * kRec;
-      sum_records(sm, p.unit_part + (size_t)(im.unit_begin + gbeg) * kRec, gcount, grec,
-                  im.K, DIM);
-      __threadfence();
-      __syncthreads();
-      if (threadIdx.x == 0) {
-        const unsigned prev = atomicAdd(&p.image_cnt[img], 1u);
-        sm.flag = (prev == (unsigned)im.ngroups - 1);
-        if (sm.flag) p.image_cnt[img] = 0;
+      if (warp == 0) {
+        warp_to_record(sm, buf, p.unit_part + (size_t)u * kRec, im.K, DIM);
+        __threadfence();
+        __syncwarp();
+        if (lane == 0) {
+          const int g = lu / kGroup;
+          const int gcount = min(kGroup, im.nunits - g * kGroup);
+          const unsigned prev = atomicAdd(&p.group_cnt[im.group_begin + g], 1u);
+          if (prev == (unsigned)gcount - 1) {
+            p.group_cnt[im.group_begin + g] = 0;
+            sm.pend[buf] = u;
+          }
+        }
       }
-      __syncthreads();
-      if (!sm.flag) continue;
-      __threadfence();
-      // image total into the unit record slot of the image's first unit
-      // (its partial was consumed by the group sum above)
-      float* tot = p.unit_part + (size_t)im.unit_begin * kRec;
-      __syncthreads();
-      sum_records(sm, p.group_part + (size_t)im.group_begin * kRec, im.ngroups, tot, im.K, DIM);
-      __threadfence();
-      __syncthreads();
-      finish_image<DIM, MODE>(p, img, im, it, tot);
-      __syncthreads();
+      buf ^= 1;
     }
     if (MODE == kAssignOnly) break;
+    __syncthreads();
+    const int task = sm.pend[buf ^ 1];
+    if (task >= 0) group_task<DIM, MODE>(p, sm, task, it);
     if (!grid_barrier(p.hdr)) return;
   }
 }
