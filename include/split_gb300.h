@@ -84,9 +84,14 @@ int split_workspace_status(void* workspace, void* stream, int* out_status);
 /* ======================================================================== */
 
 /* Replaces split::device::kmeans::cluster_workspace
- * (split/include/split/device/kmeans/cluster.cuh:46-47). */
+ * (split/include/split/device/kmeans/cluster.cuh:46-47).  Points are
+ * processed in 64 x 64 pixel tiles of the image; without the width this
+ * bound covers any width (the tile count peaks at width 1). */
 size_t split_kmeans_cluster_workspace_size(int64_t npoints, int nclusters,
                                            int dim);
+/* The same for a known image width (what the call's `width` will be). */
+size_t split_kmeans_cluster_workspace_size_2d(int64_t npoints, int width,
+                                              int nclusters, int dim);
 
 /* Replaces split::device::kmeans::cluster (cluster.cuh:31-37,
  * split/src/split/device/kmeans/cluster.cu:27-93).

@@ -28,6 +28,7 @@ _SIGS = {
     "split_status_string": (C.c_char_p, [_i32]),
     "split_workspace_status": (_i32, [_vp, _vp, C.POINTER(C.c_int)]),
     "split_kmeans_cluster_workspace_size": (_sz, [_i64, _i32, _i32]),
+    "split_kmeans_cluster_workspace_size_2d": (_sz, [_i64, _i32, _i32, _i32]),
     "split_kmeans_cluster": (_i32, [_vp, _i32, _i32, _i64, _i32, _f32, _vp, _i32, _vp, _vp, _sz,
                                     _i32, _f32, _vp, _vp]),
     "split_kmeans_assign_workspace_size": (_sz, [_i64, _i32]),

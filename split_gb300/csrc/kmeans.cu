@@ -24,11 +24,19 @@
 namespace sg {
 namespace km {
 
+#ifndef SG_KM_GROUP
+#define SG_KM_GROUP 32
+#endif
+#ifndef SG_KM_MINBLOCKS
+#define SG_KM_MINBLOCKS 4
+#endif
 constexpr int kThreads = 256;
 constexpr int kWarps = kThreads / 32;
-constexpr int kUnit = 8192;            // pixels per unit
-constexpr int kWarpSpan = kUnit / kWarps;  // 1024 pixels per warp per unit
-constexpr int kGroup = 32;             // units per group
+// A unit is a kTile x kTile pixel tile; warp w owns rows [8w, 8w + 8) of it.
+constexpr int kTile = 64;
+constexpr int kUnit = kTile * kTile;   // pixels per unit
+constexpr int kWarpRows = kTile / kWarps;
+constexpr int kGroup = SG_KM_GROUP;    // units per group
 constexpr int kMaxK = 64;
 constexpr int kMaxDim = 5;
 // partial record: kMaxK * kMaxDim float sums then kMaxK int counts
@@ -53,6 +61,8 @@ struct Image {
   int nunits;
   int group_begin;
   int ngroups;
+  int height;               // rows (ceil(npoints / width))
+  int ntx;                  // tiles per row of tiles
 };
 
 struct ImageState {
@@ -219,16 +229,13 @@ constexpr int kChunk = 8;     // records summed per thread in one pass
 constexpr int kChunks = 8;    // chunks per pass (64 records per pass)
 constexpr int kVals = kMaxK * kMaxDim + kMaxK;
 
-// Warp slots are double-buffered by unit parity: warp 0 reduces a finished
-// unit's slots while the other warps already accumulate the next unit.
 struct Smem {
   alignas(16) float cent[kMaxK * 8];
   float scratch[kChunks][kVals];
-  float acc[2][kWarps][kMaxK * kMaxDim];
-  int cnt[2][kWarps][kMaxK];
+  float acc[kWarps][kMaxK * kMaxDim];
+  int cnt[kWarps][kMaxK];
   float lut[256];
-  int next[2];   // prefetched work-counter values
-  int pend[2];   // unit whose group became complete, per buffer parity
+  int unit;
   int flag;
 };
 
@@ -273,16 +280,19 @@ __device__ __forceinline__ float2 ffma2(float2 a, float2 b, float2 c) {
 }
 
 constexpr int kPx = 4;                 // consecutive pixels per lane
-constexpr int kBatch = 32 * kPx;       // pixels per warp batch
-static_assert(kWarpSpan % kBatch == 0, "whole batches per warp span");
+constexpr int kLanesPerRow = kTile / kPx;  // 16 lanes cover a tile row
+constexpr int kBatchRows = 32 / kLanesPerRow;
+static_assert(kWarpRows % kBatchRows == 0, "whole batches per warp span");
 
-// The lane's kPx consecutive pixels starting at px0 (row, col of px0).
+// The lane's kPx consecutive pixels of image row `row` starting at column
+// `col`; ok[j] marks pixels inside the image.
 template <int LAYOUT, int DIM>
-__device__ __forceinline__ void load_px(const Image& im, const float* lut, int64_t px0, int row,
-                                        int col, float (&f)[kPx][DIM], bool (&ok)[kPx]) {
+__device__ __forceinline__ void load_px(const Image& im, const float* lut, int row, int col,
+                                        float (&f)[kPx][DIM], bool (&ok)[kPx]) {
   const int64_t n = im.npoints;
+  const int64_t px0 = (int64_t)row * im.width + col;
 #pragma unroll
-  for (int j = 0; j < kPx; ++j) ok[j] = px0 + j < n;
+  for (int j = 0; j < kPx; ++j) ok[j] = row < im.height && col + j < im.width && px0 + j < n;
   if (LAYOUT == SPLIT_LAYOUT_FLOAT4) {
     const float4* p = static_cast<const float4*>(im.points) + px0;
 #pragma unroll
@@ -306,24 +316,11 @@ __device__ __forceinline__ void load_px(const Image& im, const float* lut, int64
       for (int j = 0; j < kPx; ++j) f[j][d] = ok[j] ? __ldg(p + (int64_t)d * n + px0 + j) : 0.0f;
   }
   if (DIM == 5 && LAYOUT != SPLIT_LAYOUT_PLANAR) {
-    if (col + kPx <= im.width) {
-      const float fy = __fmul_rn(im.xy_scale, (float)row);
+    const float fy = __fmul_rn(im.xy_scale, (float)row);
 #pragma unroll
-      for (int j = 0; j < kPx; ++j) {
-        f[j][3] = __fmul_rn(im.xy_scale, (float)(col + j));
-        f[j][4] = fy;
-      }
-    } else {
-      int r = row, c = col;
-#pragma unroll
-      for (int j = 0; j < kPx; ++j) {
-        f[j][3] = __fmul_rn(im.xy_scale, (float)c);
-        f[j][4] = __fmul_rn(im.xy_scale, (float)r);
-        if (++c == im.width) {
-          c = 0;
-          ++r;
-        }
-      }
+    for (int j = 0; j < kPx; ++j) {
+      f[j][3] = __fmul_rn(im.xy_scale, (float)(col + j));
+      f[j][4] = fy;
     }
   }
 }
@@ -373,54 +370,78 @@ __device__ __forceinline__ void nearest_px(const float (&f)[kPx][DIM],
 // Warp-collective: add the per-lane sums `acc` (label l, warp-uniform) to the
 // warp's shared slot.
 template <int DIM>
-__device__ __forceinline__ void flush_acc(Smem& sm, int buf, int warp, int l,
-                                          const float (&acc)[DIM], int n) {
+__device__ __forceinline__ void flush_acc(Smem& sm, int warp, int l, const float (&acc)[DIM],
+                                          int n) {
   const int lane = threadIdx.x & 31;
 #pragma unroll
   for (int d = 0; d < DIM; ++d) {
     const float s = warp_sum(acc[d]);
-    if (lane == 0)
-      sm.acc[buf][warp][l * kMaxDim + d] = __fadd_rn(sm.acc[buf][warp][l * kMaxDim + d], s);
+    if (lane == 0) sm.acc[warp][l * kMaxDim + d] = __fadd_rn(sm.acc[warp][l * kMaxDim + d], s);
   }
   const int c = __reduce_add_sync(0xffffffffu, n);
-  if (lane == 0) sm.cnt[buf][warp][l] += c;
+  if (lane == 0) sm.cnt[warp][l] += c;
 }
 
-// Process one unit: assign (unless update-only) and accumulate per-warp sums
-// of (x - c_label).  Each lane holds kPx consecutive pixels of a 128-pixel
-// warp batch.  While consecutive batches carry one label, every lane keeps a
-// register running sum; a batch with several labels is reduced label by label
-// in ascending order.  All orders depend only on the data.
+// Process one unit (a 64 x 64 tile): assign (unless update-only) and
+// accumulate per-warp sums of (x - c_label).  Warp w owns 8 tile rows; a batch
+// is 2 rows x 64 columns, each lane holding kPx consecutive pixels of a row.
+//
+// Candidate clusters: with xy features and colour features known to lie in
+// [0, 1] the box of the warp's 8 x 64 span is exact without touching the
+// pixels, so one candidate mask serves all its batches.  Otherwise the colour
+// box of every batch is measured (warp min / max) and joined with the batch's
+// xy extent.
+//
+// While consecutive batches carry one label, every lane keeps a register
+// running sum; a batch with several labels is reduced label by label in
+// ascending order.  All orders depend only on the data.
 template <int LAYOUT, int DIM, int MODE>
-__device__ void process_unit(const Image& im, int unit, Smem& sm, int buf, bool write_labels) {
+__device__ void process_unit(const Image& im, int unit, Smem& sm, bool write_labels) {
   const unsigned full = 0xffffffffu;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   constexpr int CS = cstride(DIM);
-  if (MODE != kAssignOnly) {
-    // this warp's slot of buffer `buf` (read by warp 0 two units ago)
-    for (int i = lane; i < im.K * kMaxDim; i += 32) sm.acc[buf][warp][i] = 0.0f;
-    for (int i = lane; i < im.K; i += 32) sm.cnt[buf][warp][i] = 0;
-    __syncwarp();
+  constexpr bool kXY = DIM == 5 && LAYOUT != SPLIT_LAYOUT_PLANAR;
+  const int ty = unit / im.ntx, tx = unit - ty * im.ntx;
+  const int row0 = ty * kTile + warp * kWarpRows;
+  const int col0 = tx * kTile;
+  if (row0 >= im.height) return;
+  const int lrow = lane / kLanesPerRow, lcol = (lane % kLanesPerRow) * kPx;
+  const int rows_in = min(kWarpRows, im.height - row0);
+  const int cols_in = min(kTile, im.width - col0);
+  const bool unit_box = kXY && (LAYOUT == SPLIT_LAYOUT_RGB8 || im.unit_range);
+  const bool vec_labels =
+      (reinterpret_cast<uintptr_t>(MODE == kUpdateOnly ? im.labels_in : im.labels) & 15) == 0 &&
+      (im.width % kPx) == 0;
+
+  unsigned long long span_mask = 0;
+  if (MODE != kUpdateOnly && unit_box) {
+    float lo[DIM], hi[DIM];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      lo[d] = 0.0f;
+      hi[d] = 1.0f;
+    }
+    lo[3] = __fmul_rn(im.xy_scale, (float)col0);
+    hi[3] = __fmul_rn(im.xy_scale, (float)(col0 + cols_in - 1));
+    lo[4] = __fmul_rn(im.xy_scale, (float)row0);
+    hi[4] = __fmul_rn(im.xy_scale, (float)(row0 + rows_in - 1));
+    span_mask = candidates<DIM>(lo, hi, sm.cent, im.K);
   }
-  int64_t px0 = (int64_t)unit * kUnit + (int64_t)warp * kWarpSpan + (int64_t)lane * kPx;
-  int row = 0, col = 0;
-  if (DIM == 5 && LAYOUT != SPLIT_LAYOUT_PLANAR) {
-    row = (int)(px0 / im.width);
-    col = (int)(px0 - (int64_t)row * im.width);
-  }
-  const bool vec_labels = (reinterpret_cast<uintptr_t>(MODE == kUpdateOnly ? im.labels_in : im.labels) & 15) == 0;
+
   int acc_l = -1, acc_n = 0;
   float acc[DIM];
 #pragma unroll
   for (int d = 0; d < DIM; ++d) acc[d] = 0.0f;
 
-  for (int b = 0; b < kWarpSpan / kBatch; ++b, px0 += kBatch) {
-    if (b > 0 && DIM == 5 && LAYOUT != SPLIT_LAYOUT_PLANAR) advance(row, col, kBatch, im.width);
-    if (__all_sync(full, px0 >= im.npoints)) break;
+  for (int b = 0; b < kWarpRows / kBatchRows; ++b) {
+    if (b * kBatchRows >= rows_in) break;
+    const int row = row0 + b * kBatchRows + lrow;
+    const int col = col0 + lcol;
     float f[kPx][DIM];
     bool ok[kPx];
-    load_px<LAYOUT, DIM>(im, sm.lut, px0, row, col, f, ok);
+    load_px<LAYOUT, DIM>(im, sm.lut, row, col, f, ok);
     const bool all_ok = ok[kPx - 1];
+    const int64_t px0 = (int64_t)row * im.width + col;
     int lab[kPx];
     if (MODE == kUpdateOnly) {
       if (all_ok && vec_labels) {
@@ -434,28 +455,16 @@ __device__ void process_unit(const Image& im, int unit, Smem& sm, int buf, bool 
       for (int j = 0; j < kPx; ++j)
         if (!ok[j] || lab[j] < 0 || lab[j] >= im.K) lab[j] = -1;
     } else {
-      // Bounding box of the batch, then the candidate clusters.  fminf /
-      // fmaxf skip NaN: a NaN pixel gets label 0 whatever the mask (every
-      // distance compares false), and the box still bounds all other pixels.
-      float lo[DIM], hi[DIM];
-      constexpr bool kXY = DIM == 5 && LAYOUT != SPLIT_LAYOUT_PLANAR;
-      constexpr int kBoxDims = kXY ? 3 : DIM;
-      const bool warp_all_ok = __all_sync(full, all_ok);
-      const bool unit = LAYOUT == SPLIT_LAYOUT_RGB8 || (LAYOUT == SPLIT_LAYOUT_FLOAT4 && im.unit_range);
+      unsigned long long mask = span_mask;
+      if (!unit_box) {
+        // Box of the batch.  fminf / fmaxf skip NaN: a NaN pixel gets label
+        // 0 whatever the mask (every distance compares false), and the box
+        // still bounds all other pixels.
+        float lo[DIM], hi[DIM];
+        constexpr int kBoxDims = kXY ? 3 : DIM;
 #pragma unroll
-      for (int d = 0; d < kBoxDims; ++d) {
-        if (unit && d < 3) {
-          lo[d] = 0.0f;
-          hi[d] = 1.0f;
-          continue;
-        }
-        float a, z;
-        if (warp_all_ok) {
-          a = fminf(fminf(f[0][d], f[1][d]), fminf(f[2][d], f[3][d]));
-          z = fmaxf(fmaxf(f[0][d], f[1][d]), fmaxf(f[2][d], f[3][d]));
-        } else {
-          a = INFINITY;
-          z = -INFINITY;
+        for (int d = 0; d < kBoxDims; ++d) {
+          float a = INFINITY, z = -INFINITY;
 #pragma unroll
           for (int j = 0; j < kPx; ++j) {
             if (ok[j]) {
@@ -463,30 +472,18 @@ __device__ void process_unit(const Image& im, int unit, Smem& sm, int buf, bool 
               z = fmaxf(z, f[j][d]);
             }
           }
+          lo[d] = fkey_inv(__reduce_min_sync(full, fkey(a)));
+          hi[d] = fkey_inv(__reduce_max_sync(full, fkey(z)));
         }
-        lo[d] = fkey_inv(__reduce_min_sync(full, fkey(a)));
-        hi[d] = fkey_inv(__reduce_max_sync(full, fkey(z)));
-      }
-      if (kXY) {
-        // the batch's pixels are consecutive: lane 0 holds the first, lane 31
-        // the last; a batch that wraps a row spans whole columns
-        const int r0 = __shfl_sync(full, row, 0), c0 = __shfl_sync(full, col, 0);
-        const int64_t last = min(px0 - (int64_t)lane * kPx + kBatch, im.npoints) - 1;
-        const int64_t first = px0 - (int64_t)lane * kPx;
-        const int c1 = c0 + (int)(last - first);
-        if (c1 < im.width) {
-          lo[3] = __fmul_rn(im.xy_scale, (float)c0);
-          hi[3] = __fmul_rn(im.xy_scale, (float)c1);
-          lo[4] = hi[4] = __fmul_rn(im.xy_scale, (float)r0);
-        } else {
-          const int r1 = (int)(last / im.width);
-          lo[3] = 0.0f;
-          hi[3] = __fmul_rn(im.xy_scale, (float)(im.width - 1));
+        if (kXY) {
+          const int r0 = row0 + b * kBatchRows;
+          lo[3] = __fmul_rn(im.xy_scale, (float)col0);
+          hi[3] = __fmul_rn(im.xy_scale, (float)(col0 + cols_in - 1));
           lo[4] = __fmul_rn(im.xy_scale, (float)r0);
-          hi[4] = __fmul_rn(im.xy_scale, (float)r1);
+          hi[4] = __fmul_rn(im.xy_scale, (float)min(r0 + kBatchRows - 1, im.height - 1));
         }
+        mask = candidates<DIM>(lo, hi, sm.cent, im.K);
       }
-      const unsigned long long mask = candidates<DIM>(lo, hi, sm.cent, im.K);
       nearest_px<DIM>(f, sm.cent, mask, lab);
       if (write_labels) {
         if (all_ok && vec_labels) {
@@ -517,7 +514,7 @@ __device__ void process_unit(const Image& im, int unit, Smem& sm, int buf, bool 
     if (mx < 0) continue;
     if (mn == mx) {
       if (mn != acc_l) {
-        if (acc_l >= 0) flush_acc<DIM>(sm, buf, warp, acc_l, acc, acc_n);
+        if (acc_l >= 0) flush_acc<DIM>(sm, warp, acc_l, acc, acc_n);
         acc_l = mn;
         acc_n = 0;
 #pragma unroll
@@ -535,7 +532,7 @@ __device__ void process_unit(const Image& im, int unit, Smem& sm, int buf, bool 
         }
       }
     } else {
-      if (acc_l >= 0) flush_acc<DIM>(sm, buf, warp, acc_l, acc, acc_n);
+      if (acc_l >= 0) flush_acc<DIM>(sm, warp, acc_l, acc, acc_n);
       acc_l = -1;
       for (int l = mn; l != INT_MAX;) {
         float s[DIM];
@@ -553,30 +550,33 @@ __device__ void process_unit(const Image& im, int unit, Smem& sm, int buf, bool 
             nxt = min(nxt, lab[j]);
           }
         }
-        flush_acc<DIM>(sm, buf, warp, l, s, c);
+        flush_acc<DIM>(sm, warp, l, s, c);
         l = __reduce_min_sync(full, nxt);
       }
     }
   }
-  if (MODE != kAssignOnly && acc_l >= 0) flush_acc<DIM>(sm, buf, warp, acc_l, acc, acc_n);
+  if (MODE != kAssignOnly && acc_l >= 0) flush_acc<DIM>(sm, warp, acc_l, acc, acc_n);
 }
 
-// Warp 0: sum the 8 warp slots of buffer `buf` in warp order into a unit
-// record.
-__device__ __forceinline__ void warp_to_record(const Smem& sm, int buf, float* rec, int K,
-                                               int dim) {
-  const int lane = threadIdx.x & 31;
-  for (int idx = lane; idx < K * kMaxDim; idx += 32) {
-    if ((idx % kMaxDim) >= dim) continue;
+// Sum the warp slots in warp order into a unit record; clear the slots.
+__device__ void block_to_record(Smem& sm, float* rec, int K, int dim) {
+  __syncthreads();
+  for (int idx = threadIdx.x; idx < K * kMaxDim; idx += blockDim.x) {
     float s = 0.0f;
 #pragma unroll
-    for (int w = 0; w < kWarps; ++w) s = __fadd_rn(s, sm.acc[buf][w][idx]);
-    __stcg(rec + idx, s);
+    for (int w = 0; w < kWarps; ++w) {
+      s = __fadd_rn(s, sm.acc[w][idx]);
+      sm.acc[w][idx] = 0.0f;
+    }
+    if ((idx % kMaxDim) < dim) __stcg(rec + idx, s);
   }
-  for (int k = lane; k < K; k += 32) {
+  for (int k = threadIdx.x; k < K; k += blockDim.x) {
     int c = 0;
 #pragma unroll
-    for (int w = 0; w < kWarps; ++w) c += sm.cnt[buf][w][k];
+    for (int w = 0; w < kWarps; ++w) {
+      c += sm.cnt[w][k];
+      sm.cnt[w][k] = 0;
+    }
     __stcg(reinterpret_cast<int*>(rec + kMaxK * kMaxDim) + k, c);
   }
 }
@@ -701,71 +701,32 @@ __device__ void finish_image(const Params& p, int img, const Image& im, int it,
   }
 }
 
-// Sums the group of unit u (whose last unit just completed); the last group
-// of the image then forms the image total and the new centroids.
-template <int DIM, int MODE>
-__device__ void group_task(const Params& p, Smem& sm, int u, int it) {
-  const int img = find_image(p, u);
-  const Image& im = image_of(p, img);
-  const int lu = u - im.unit_begin;
-  const int g = lu / kGroup;
-  const int gbeg = g * kGroup;
-  const int gcount = min(kGroup, im.nunits - gbeg);
-  __threadfence();
-  float* grec = p.group_part + (size_t)(im.group_begin + g) * kRec;
-  sum_records(sm, p.unit_part + (size_t)(im.unit_begin + gbeg) * kRec, gcount, grec, im.K, DIM);
-  __threadfence();
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    const unsigned prev = atomicAdd(&p.image_cnt[img], 1u);
-    sm.flag = (prev == (unsigned)im.ngroups - 1);
-    if (sm.flag) p.image_cnt[img] = 0;
-  }
-  __syncthreads();
-  if (!sm.flag) return;
-  __threadfence();
-  // image total into the record slot of the image's first unit (its partial
-  // was consumed by the first group's sum)
-  float* tot = p.unit_part + (size_t)im.unit_begin * kRec;
-  sum_records(sm, p.group_part + (size_t)im.group_begin * kRec, im.ngroups, tot, im.K, DIM);
-  __threadfence();
-  __syncthreads();
-  finish_image<DIM, MODE>(p, img, im, it, tot);
-  __syncthreads();
-}
-
 template <int LAYOUT, int DIM, int MODE>
-__global__ void __launch_bounds__(kThreads, 4) kmeans_kernel(Params p) {
+__global__ void __launch_bounds__(kThreads, SG_KM_MINBLOCKS) kmeans_kernel(Params p) {
   __shared__ Smem sm;
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int i = threadIdx.x; i < kWarps * kMaxK * kMaxDim; i += blockDim.x)
+    (&sm.acc[0][0])[i] = 0.0f;
+  for (int i = threadIdx.x; i < kWarps * kMaxK; i += blockDim.x) (&sm.cnt[0][0])[i] = 0;
   if (LAYOUT == SPLIT_LAYOUT_RGB8)
     for (int i = threadIdx.x; i < 256; i += blockDim.x) sm.lut[i] = (float)i / 255.0f;
+  __syncthreads();
 
   for (int it = 0; it < p.max_iter; ++it) {
-    unsigned* counter = &p.hdr->work_counter[it & 1];
-    if (threadIdx.x == 0) {
-      if (blockIdx.x == 0) p.hdr->work_counter[(it + 1) & 1] = 0;
-      sm.next[0] = (int)atomicAdd(counter, 1u);
-      sm.pend[0] = sm.pend[1] = -1;
-    }
-    __syncthreads();
-    int cached = -1, npar = 0, buf = 0;
-    int raw = sm.next[0];
-    while (raw < p.total_units) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) p.hdr->work_counter[(it + 1) & 1] = 0;
+    int cached = -1;
+    for (;;) {
+      if (threadIdx.x == 0) sm.unit = (int)atomicAdd(&p.hdr->work_counter[it & 1], 1u);
+      __syncthreads();
+      const int raw = sm.unit;
+      __syncthreads();
+      if (raw >= p.total_units) break;
       // odd iterations walk the units backwards: they start on the units the
       // previous iteration touched last, which are still resident in L2
       const int u = (it & 1) ? p.total_units - 1 - raw : raw;
       const int img = find_image(p, u);
       const Image& im = image_of(p, img);
-      if (threadIdx.x == 0) sm.next[npar ^ 1] = (int)atomicAdd(counter, 1u);
-      if (MODE != kAssignOnly && *(volatile int*)&p.state[img].done) {
-        __syncthreads();
-        raw = sm.next[npar ^ 1];
-        npar ^= 1;
-        continue;
-      }
+      if (MODE != kAssignOnly && *(volatile int*)&p.state[img].done) continue;
       if (img != cached) {
-        // every warp is past the previous unit (its end-of-unit barrier)
         if (MODE == kAssignOnly)
           load_centroids<DIM>(p.cur + (size_t)img * (kMaxK * 8), im.K, sm.cent);
         else
@@ -777,36 +738,48 @@ __global__ void __launch_bounds__(kThreads, 4) kmeans_kernel(Params p) {
       const int lu = u - im.unit_begin;
       const bool wl = (MODE == kAssignOnly) ||
                       (MODE == kCluster && (im.threshold >= 0.0f || it == im.max_iter - 1));
-      process_unit<LAYOUT, DIM, MODE>(im, lu, sm, buf, wl);
-      __syncthreads();  // the unit's slots are complete; next[] and pend[] visible
-      raw = sm.next[npar ^ 1];
-      npar ^= 1;
+      process_unit<LAYOUT, DIM, MODE>(im, lu, sm, wl);
       if (MODE == kAssignOnly) continue;
-      const int task = sm.pend[buf ^ 1];
-      if (task >= 0) {
-        group_task<DIM, MODE>(p, sm, task, it);
-        if (threadIdx.x == 0) sm.pend[buf ^ 1] = -1;
+      float* rec = p.unit_part + (size_t)u * kRec;
+      block_to_record(sm, rec, im.K, DIM);
+      // publish the unit partial; the last unit of a group sums the group
+      __threadfence();
+      __syncthreads();
+      const int g = lu / kGroup;
+      const int gbeg = g * kGroup;
+      const int gcount = min(kGroup, im.nunits - gbeg);
+      if (threadIdx.x == 0) {
+        const unsigned prev = atomicAdd(&p.group_cnt[im.group_begin + g], 1u);
+        sm.flag = (prev == (unsigned)gcount - 1);
+        if (sm.flag) p.group_cnt[im.group_begin + g] = 0;
       }
-      if (warp == 0) {
-        warp_to_record(sm, buf, p.unit_part + (size_t)u * kRec, im.K, DIM);
-        __threadfence();
-        __syncwarp();
-        if (lane == 0) {
-          const int g = lu / kGroup;
-          const int gcount = min(kGroup, im.nunits - g * kGroup);
-          const unsigned prev = atomicAdd(&p.group_cnt[im.group_begin + g], 1u);
-          if (prev == (unsigned)gcount - 1) {
-            p.group_cnt[im.group_begin + g] = 0;
-            sm.pend[buf] = u;
-          }
-        }
+      __syncthreads();
+      if (!sm.flag) continue;
+      __threadfence();
+      float* grec = p.group_part + (size_t)(im.group_begin + g) * kRec;
+      sum_records(sm, p.unit_part + (size_t)(im.unit_begin + gbeg) * kRec, gcount, grec,
+                  im.K, DIM);
+      __threadfence();
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        const unsigned prev = atomicAdd(&p.image_cnt[img], 1u);
+        sm.flag = (prev == (unsigned)im.ngroups - 1);
+        if (sm.flag) p.image_cnt[img] = 0;
       }
-      buf ^= 1;
+      __syncthreads();
+      if (!sm.flag) continue;
+      __threadfence();
+      // image total into the unit record slot of the image's first unit
+      // (its partial was consumed by the group sum above)
+      float* tot = p.unit_part + (size_t)im.unit_begin * kRec;
+      __syncthreads();
+      sum_records(sm, p.group_part + (size_t)im.group_begin * kRec, im.ngroups, tot, im.K, DIM);
+      __threadfence();
+      __syncthreads();
+      finish_image<DIM, MODE>(p, img, im, it, tot);
+      __syncthreads();
     }
     if (MODE == kAssignOnly) break;
-    __syncthreads();
-    const int task = sm.pend[buf ^ 1];
-    if (task >= 0) group_task<DIM, MODE>(p, sm, task, it);
     if (!grid_barrier(p.hdr)) return;
   }
 }
@@ -827,7 +800,11 @@ struct Layout {
   size_t bytes;
 };
 
-inline int units_of(int64_t n) { return (int)((n + kUnit - 1) / kUnit); }
+inline int height_of(int64_t n, int width) { return (int)((n + width - 1) / width); }
+inline int tiles_x(int width) { return (width + kTile - 1) / kTile; }
+inline int units_of(int64_t n, int width) {
+  return tiles_x(width) * ((height_of(n, width) + kTile - 1) / kTile);
+}
 inline int groups_of(int units) { return (units + kGroup - 1) / kGroup; }
 
 static Layout carve(void* ws, int total_units, int total_groups, int nimages) {
@@ -926,7 +903,7 @@ static int run(int mode, const void* points, int layout, int dim, int64_t n,
   if (!valid_features(points, layout, dim, n, width, K)) return SPLIT_ERR_INVALID;
   const int unit_range = (layout & SPLIT_FEATURES_UNIT_RANGE) ? 1 : 0;
   layout &= ~SPLIT_FEATURES_UNIT_RANGE;
-  const int units = units_of(n), groups = groups_of(units);
+  const int units = units_of(n, width), groups = groups_of(units);
   Layout l = carve(nullptr, units, groups, 1);
   if (!ws || ws_bytes < l.bytes || (reinterpret_cast<uintptr_t>(ws) & 255))
     return SPLIT_ERR_WORKSPACE;
@@ -947,6 +924,8 @@ static int run(int mode, const void* points, int layout, int dim, int64_t n,
   im.d_iterations = d_iter;
   im.unit_begin = 0;
   im.nunits = units;
+  im.height = height_of(n, width);
+  im.ntx = tiles_x(width);
   im.group_begin = 0;
   im.ngroups = groups;
   p.nimages = 1;
@@ -980,12 +959,18 @@ static int run(int mode, const void* points, int layout, int dim, int64_t n,
 
 using namespace sg;
 
-extern "C" size_t split_kmeans_cluster_workspace_size(int64_t npoints, int nclusters, int dim) {
+extern "C" size_t split_kmeans_cluster_workspace_size_2d(int64_t npoints, int width,
+                                                         int nclusters, int dim) {
   (void)nclusters;
   (void)dim;
-  if (npoints <= 0) return 0;
-  const int u = km::units_of(npoints);
+  if (npoints <= 0 || width < 1) return 0;
+  const int u = km::units_of(npoints, width);
   return km::carve(nullptr, u, km::groups_of(u), 1).bytes;
+}
+
+extern "C" size_t split_kmeans_cluster_workspace_size(int64_t npoints, int nclusters, int dim) {
+  // without the image width: the largest tile count, reached at width 1
+  return split_kmeans_cluster_workspace_size_2d(npoints, 1, nclusters, dim);
 }
 
 extern "C" int split_kmeans_cluster(const void* points, int layout, int dim, int64_t npoints,

@@ -29,7 +29,7 @@ static Layout carve(void* ws, int W, int H, const split_pipeline_params& p) {
   l.features4 = p.features == SPLIT_LAYOUT_FLOAT4 ? c.take<float>((size_t)n * 4) : nullptr;
   l.seg = c.take<int32_t>((size_t)n);
   l.sizes = c.take<int32_t>((size_t)n);
-  l.km_bytes = split_kmeans_cluster_workspace_size(n, p.nclusters, p.dim);
+  l.km_bytes = split_kmeans_cluster_workspace_size_2d(n, W, p.nclusters, p.dim);
   l.km_ws = c.take<char>(l.km_bytes);
   l.ccl_bytes = split_ccl_workspace_size(W, H);
   l.ccl_ws = c.take<char>(l.ccl_bytes);

@@ -18,6 +18,10 @@ def cluster_workspace(npoints: int, nclusters: int, dim: int) -> int:
     return N.load().split_kmeans_cluster_workspace_size(npoints, nclusters, dim)
 
 
+def cluster_workspace_2d(npoints: int, width: int, nclusters: int, dim: int) -> int:
+    return N.load().split_kmeans_cluster_workspace_size_2d(npoints, width, nclusters, dim)
+
+
 def label_points_workspace(npoints: int, nclusters: int) -> int:
     """label.cuh:39-40."""
     return N.load().split_kmeans_assign_workspace_size(npoints, nclusters)
@@ -68,7 +72,7 @@ def cluster(points: torch.Tensor, centroids: torch.Tensor, labels: torch.Tensor,
     if labels.numel() != n:
         raise ValueError("labels must hold one entry per point")
     k = centroids.shape[1]
-    ws = ensure_workspace(temp, cluster_workspace(n, k, d), points.device)
+    ws = ensure_workspace(temp, cluster_workspace_2d(n, width, k, d), points.device)
     st = N.load().split_kmeans_cluster(
         ptr(points), layout, d, n, width, xy_scale, ptr(centroids), k, ptr(labels), ws.ptr,
         ws.nbytes, max_iter, threshold, ptr(iterations_out), stream_handle(stream))
@@ -84,7 +88,7 @@ def label_points(centroids: torch.Tensor, points: torch.Tensor, labels: torch.Te
     require_cuda(centroids, "centroids", torch.float32)
     require_cuda(labels, "labels", torch.int32)
     k = centroids.shape[1]
-    ws = ensure_workspace(temp, label_points_workspace(n, k), points.device)
+    ws = ensure_workspace(temp, cluster_workspace_2d(n, width, k, d), points.device)
     st = N.load().split_kmeans_assign(ptr(points), layout, d, n, width, xy_scale,
                                       ptr(centroids), k, ptr(labels), ws.ptr, ws.nbytes,
                                       stream_handle(stream))
@@ -103,7 +107,7 @@ def calculate_centroids(labels: torch.Tensor, points: torch.Tensor, centroids: t
     require_cuda(centroids, "centroids", torch.float32)
     require_cuda(labels, "labels", torch.int32)
     k = centroids.shape[1]
-    ws = ensure_workspace(temp, calculate_centroids_workspace(n, k, d), points.device)
+    ws = ensure_workspace(temp, cluster_workspace_2d(n, width, k, d), points.device)
     st = N.load().split_kmeans_update(ptr(labels), ptr(points), layout, d, n, width, xy_scale,
                                       ptr(centroids), k, ws.ptr, ws.nbytes,
                                       stream_handle(stream))
