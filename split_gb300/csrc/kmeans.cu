@@ -235,7 +235,6 @@ struct Smem {
   float acc[kWarps][kMaxK * kMaxDim];
   int cnt[kWarps][kMaxK];
   float lut[256];
-  float total[kRec];   // record sums (group or image) in record layout
   int unit;
   int flag;
 };
@@ -582,68 +581,58 @@ __device__ void block_to_record(Smem& sm, float* rec, int K, int dim) {
   }
 }
 
-// Sum `count` records (stride kRec) in record order into shared `out`
-// (kVals entries: K*kMaxDim float sums then K int counts).  Records are staged
-// through shared memory a chunk at a time with every load of a chunk issued
-// at once, so a chunk costs one L2 round trip; the sums run in record order.
-constexpr int kStage = kChunks * kVals;   // staging floats (12 KB)
-constexpr int kStageItems = (kStage + kThreads - 1) / kThreads;
-
-__device__ __forceinline__ int rec_off(int v, int K, int dim) {
-  return v < K * dim ? (v / dim) * kMaxDim + (v % dim) : kMaxK * kMaxDim + (v - K * dim);
-}
-
-__device__ void sum_records(Smem& sm, const float* src, int count, float* out, int K, int dim) {
+// Sum `count` records (stride kRec) into `out` with one fixed shape: records
+// are summed 8 at a time in order (all 8 loads in flight), the chunk sums of a
+// pass are then summed in chunk order, and the passes in pass order.  Value v
+// enumerates the K*dim float sums followed by the K counts.
+__device__ void sum_records(Smem& sm, const float* src, int count, float* out,
+                            int K, int dim) {
   const int nv = K * dim + K;
-  const int per = kStage / nv;
-  float* stage = &sm.scratch[0][0];
-  float accf[2] = {0.0f, 0.0f};
-  int acci[2] = {0, 0};
-  for (int r0 = 0; r0 < count; r0 += per) {
-    const int items = min(per, count - r0) * nv;
-    float tmp[kStageItems];
-#pragma unroll
-    for (int q = 0; q < kStageItems; ++q) {
-      const int i = threadIdx.x + q * kThreads;
-      if (i < items) {
-        const int r = i / nv, v = i - r * nv;
-        tmp[q] = __ldcg(src + (size_t)(r0 + r) * kRec + rec_off(v, K, dim));
-      }
-    }
-#pragma unroll
-    for (int q = 0; q < kStageItems; ++q) {
-      const int i = threadIdx.x + q * kThreads;
-      if (i < items) stage[i] = tmp[q];
-    }
+  for (int pass0 = 0; pass0 < count; pass0 += kChunk * kChunks) {
+    const int in_pass = min(count - pass0, kChunk * kChunks);
+    const int nch = (in_pass + kChunk - 1) / kChunk;
     __syncthreads();
-    const int rn = items / nv;
+    for (int w = threadIdx.x; w < nv * nch; w += blockDim.x) {
+      const int v = w % nv, c = w / nv;
+      const int r0 = pass0 + c * kChunk;
+      const int rn = min(kChunk, count - r0);
+      const bool is_cnt = v >= K * dim;
+      const int off = is_cnt ? kMaxK * kMaxDim + (v - K * dim)
+                             : (v / dim) * kMaxDim + (v % dim);
+      const float* s = src + (size_t)r0 * kRec + off;
+      float x[kChunk];
 #pragma unroll
-    for (int h = 0; h < 2; ++h) {
-      const int v = threadIdx.x + h * kThreads;
-      if (v >= nv) continue;
-      if (v < K * dim) {
-        for (int r = 0; r < rn; ++r) accf[h] = __fadd_rn(accf[h], stage[r * nv + v]);
+      for (int r = 0; r < kChunk; ++r) x[r] = r < rn ? __ldcg(s + (size_t)r * kRec) : 0.0f;
+      if (is_cnt) {
+        int a = 0;
+#pragma unroll
+        for (int r = 0; r < kChunk; ++r) a += __float_as_int(x[r]);
+        sm.scratch[c][v] = __int_as_float(a);
       } else {
-        for (int r = 0; r < rn; ++r) acci[h] += __float_as_int(stage[r * nv + v]);
+        float a = x[0];
+#pragma unroll
+        for (int r = 1; r < kChunk; ++r) a = __fadd_rn(a, x[r]);
+        sm.scratch[c][v] = a;
       }
     }
     __syncthreads();
-  }
-#pragma unroll
-  for (int h = 0; h < 2; ++h) {
-    const int v = threadIdx.x + h * kThreads;
-    if (v >= nv) continue;
-    out[rec_off(v, K, dim)] = v < K * dim ? accf[h] : __int_as_float(acci[h]);
+    for (int v = threadIdx.x; v < nv; v += blockDim.x) {
+      const bool is_cnt = v >= K * dim;
+      const int off = is_cnt ? kMaxK * kMaxDim + (v - K * dim)
+                             : (v / dim) * kMaxDim + (v % dim);
+      if (is_cnt) {
+        int a = pass0 ? __float_as_int(__ldcg(out + off)) : 0;
+        for (int c = 0; c < nch; ++c) a += __float_as_int(sm.scratch[c][v]);
+        __stcg(reinterpret_cast<int*>(out + off), a);
+      } else {
+        float a = sm.scratch[0][v];
+        for (int c = 1; c < nch; ++c) a = __fadd_rn(a, sm.scratch[c][v]);
+        if (pass0) a = __fadd_rn(__ldcg(out + off), a);
+        __stcg(out + off, a);
+      }
+    }
   }
   __syncthreads();
-}
-
-// Device-scope acquire-release increment: the block's earlier stores (made
-// visible to thread 0 by the preceding barrier) are published before the
-// increment, and whoever sees the final count sees them.
-__device__ __forceinline__ unsigned arrive(unsigned* counter) {
-  return cuda::atomic_ref<unsigned, cuda::thread_scope_device>(*counter).fetch_add(
-      1u, cuda::memory_order_acq_rel);
 }
 
 template <int DIM>
@@ -660,18 +649,18 @@ __device__ __forceinline__ void load_centroids(const float* src, int K,
 // convergence test of cluster.cu:71-88, outputs on the last iteration.
 template <int DIM, int MODE>
 __device__ void finish_image(const Params& p, int img, const Image& im, int it,
-                             const float* total, const float* cent) {
+                             const float* total) {
   __shared__ float sdelta;
+  const float* c_old = p.cur + ((size_t)(it & 1) * p.nimages + img) * (kMaxK * 8);
   float* c_new = p.cur + ((size_t)((it + 1) & 1) * p.nimages + img) * (kMaxK * 8);
   const int* cnt = reinterpret_cast<const int*>(total + kMaxK * kMaxDim);
   __shared__ float sdiff[kMaxK * kMaxDim];
-  constexpr int CS = cstride(DIM);
   for (int idx = threadIdx.x; idx < im.K * DIM; idx += blockDim.x) {
     const int k = idx / DIM, d = idx % DIM;
-    const float c = cent[k * CS + d];
-    const int n = cnt[k];
+    const float c = __ldcg(c_old + k * 8 + d);
+    const int n = __ldcg(cnt + k);
     float cn = c;
-    if (n > 0) cn = __fadd_rn(c, __fdiv_rn(total[k * kMaxDim + d], (float)n));
+    if (n > 0) cn = __fadd_rn(c, __fdiv_rn(__ldcg(total + k * kMaxDim + d), (float)n));
     __stcg(c_new + k * 8 + d, cn);
     const float df = __fsub_rn(cn, c);
     sdiff[idx] = __fmul_rn(df, df);
@@ -754,40 +743,40 @@ __global__ void __launch_bounds__(kThreads, SG_KM_MINBLOCKS) kmeans_kernel(Param
       float* rec = p.unit_part + (size_t)u * kRec;
       block_to_record(sm, rec, im.K, DIM);
       // publish the unit partial; the last unit of a group sums the group
+      __threadfence();
       __syncthreads();
       const int g = lu / kGroup;
       const int gbeg = g * kGroup;
       const int gcount = min(kGroup, im.nunits - gbeg);
       if (threadIdx.x == 0) {
-        const unsigned prev = arrive(&p.group_cnt[im.group_begin + g]);
+        const unsigned prev = atomicAdd(&p.group_cnt[im.group_begin + g], 1u);
         sm.flag = (prev == (unsigned)gcount - 1);
         if (sm.flag) p.group_cnt[im.group_begin + g] = 0;
       }
       __syncthreads();
       if (!sm.flag) continue;
+      __threadfence();
       float* grec = p.group_part + (size_t)(im.group_begin + g) * kRec;
-      sum_records(sm, p.unit_part + (size_t)(im.unit_begin + gbeg) * kRec, gcount, sm.total,
+      sum_records(sm, p.unit_part + (size_t)(im.unit_begin + gbeg) * kRec, gcount, grec,
                   im.K, DIM);
-      {
-        const int nv = im.K * DIM + im.K;
-        for (int v = threadIdx.x; v < nv; v += blockDim.x) {
-          const int o = rec_off(v, im.K, DIM);
-          __stcg(grec + o, sm.total[o]);
-        }
-      }
+      __threadfence();
       __syncthreads();
       if (threadIdx.x == 0) {
-        const unsigned prev = arrive(&p.image_cnt[img]);
+        const unsigned prev = atomicAdd(&p.image_cnt[img], 1u);
         sm.flag = (prev == (unsigned)im.ngroups - 1);
         if (sm.flag) p.image_cnt[img] = 0;
       }
       __syncthreads();
       if (!sm.flag) continue;
-      // image total (smem) -> new centroids; sm.cent still holds this image's
-      // centroids of the iteration
-      sum_records(sm, p.group_part + (size_t)im.group_begin * kRec, im.ngroups, sm.total, im.K,
-                  DIM);
-      finish_image<DIM, MODE>(p, img, im, it, sm.total, sm.cent);
+      __threadfence();
+      // image total into the unit record slot of the image's first unit
+      // (its partial was consumed by the group sum above)
+      float* tot = p.unit_part + (size_t)im.unit_begin * kRec;
+      __syncthreads();
+      sum_records(sm, p.group_part + (size_t)im.group_begin * kRec, im.ngroups, tot, im.K, DIM);
+      __threadfence();
+      __syncthreads();
+      finish_image<DIM, MODE>(p, img, im, it, tot);
       __syncthreads();
     }
     if (MODE == kAssignOnly) break;
