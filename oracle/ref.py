@@ -1,0 +1,117 @@
+"""ctypes wrapper of the reference's own code built for the CPU (Thrust OMP),
+see oracle/refbuild.py.  Test infrastructure only: golden-fixture generation,
+pinning the oracle restatement, and the timed CPU reference."""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+_lib = None
+
+
+def available() -> bool:
+    from . import refbuild
+    return os.path.exists(refbuild.LIB) or refbuild.build() is not None
+
+
+def load():
+    global _lib
+    if _lib is None:
+        from . import refbuild
+        path = refbuild.build()
+        if path is None:
+            raise RuntimeError("reference sources unavailable")
+        lib = C.CDLL(path)
+        vp, i32, f32 = C.c_void_p, C.c_int, C.c_float
+        sigs = {
+            "ref_kmeans_cluster": [vp, i32, i32, vp, i32, vp, i32],
+            "ref_label_points": [vp, i32, i32, vp, i32, vp],
+            "ref_calculate_centroids": [vp, vp, i32, i32, vp, i32],
+            "ref_connected_components": [vp, i32, i32, vp, i32],
+            "ref_compress_labels": [vp, i32],
+            "ref_merge_small_segments": [vp, vp, i32, i32, i32],
+            "ref_erode": [vp, i32, i32, i32],
+            "ref_sobel_normals": [vp, i32, i32, f32, vp],
+            "ref_propagate_centroids": [vp, i32, vp, i32, i32, vp],
+        }
+        for name, args in sigs.items():
+            fn = getattr(lib, name)
+            fn.restype = i32
+            fn.argtypes = args
+        _lib = lib
+    return _lib
+
+
+def _p(a):
+    return C.c_void_p(a.ctypes.data)
+
+
+def kmeans_cluster(points, centroids, iters):
+    p = np.ascontiguousarray(points, np.float32)
+    c = np.ascontiguousarray(centroids, np.float32).copy()
+    lab = np.empty(p.shape[1], np.int32)
+    load().ref_kmeans_cluster(_p(p), p.shape[0], p.shape[1], _p(c), c.shape[1], _p(lab), iters)
+    return lab, c
+
+
+def label_points(points, centroids):
+    p = np.ascontiguousarray(points, np.float32)
+    c = np.ascontiguousarray(centroids, np.float32)
+    lab = np.empty(p.shape[1], np.int32)
+    load().ref_label_points(_p(p), p.shape[0], p.shape[1], _p(c), c.shape[1], _p(lab))
+    return lab
+
+
+def calculate_centroids(labels, points, k):
+    p = np.ascontiguousarray(points, np.float32)
+    lab = np.ascontiguousarray(labels, np.int32)
+    c = np.zeros((p.shape[0], k), np.float32)
+    load().ref_calculate_centroids(_p(lab), _p(p), p.shape[0], p.shape[1], _p(c), k)
+    return c
+
+
+def connected_components(labels, max_iter=100000):
+    a = np.ascontiguousarray(labels, np.int32)
+    h, w = a.shape
+    out = np.empty(a.size, np.int32)
+    load().ref_connected_components(_p(a), w, h, _p(out), max_iter)
+    return out.reshape(h, w)
+
+
+def compress_labels(labels):
+    a = np.ascontiguousarray(labels, np.int32).copy()
+    n = load().ref_compress_labels(_p(a), a.size)
+    return a, n
+
+
+def merge_small_segments(chroma, labels, P):
+    ch = np.ascontiguousarray(chroma, np.float32)
+    a = np.ascontiguousarray(labels, np.int32).copy()
+    h, w = a.shape
+    load().ref_merge_small_segments(_p(ch), _p(a), w, h, P)
+    return a
+
+
+def erode(labels, niter=1):
+    a = np.ascontiguousarray(labels, np.int32).copy()
+    h, w = a.shape
+    load().ref_erode(_p(a), w, h, niter)
+    return a
+
+
+def sobel_normals(heights, depth=1.0):
+    hgt = np.ascontiguousarray(heights, np.float32)
+    h, w = hgt.shape
+    out = np.empty((3, h * w), np.float32)
+    load().ref_sobel_normals(_p(hgt), w, h, depth, _p(out))
+    return out
+
+
+def propagate_centroids(labels, centroids):
+    lab = np.ascontiguousarray(labels, np.int32)
+    c = np.ascontiguousarray(centroids, np.float32)
+    out = np.empty((c.shape[0], lab.size), np.float32)
+    load().ref_propagate_centroids(_p(lab), lab.size, _p(c), c.shape[0], c.shape[1], _p(out))
+    return out

@@ -1,0 +1,156 @@
+// extern "C" driver over the reference's own segmentation entry points,
+// compiled for the CPU with Thrust's OMP device system (oracle/refbuild.py).
+// Test infrastructure only: used to generate golden fixtures, to pin the
+// oracle restatement, and as the timed CPU reference.  Host arrays in, host
+// arrays out; all layouts follow the reference (planar D x N features,
+// row-major H x W labels, planar 3 x N normals).
+#include <cstdint>
+#include <cstring>
+#include <vector>
+
+#include <thrust/copy.h>
+#include <thrust/device_malloc.h>
+#include <thrust/device_free.h>
+
+#include "split/device/ccl/compress_labels.cuh"
+#include "split/device/ccl/connected_components.cuh"
+#include "split/device/ccl/merge_small_segments.cuh"
+#include "split/device/kmeans/centroids.cuh"
+#include "split/device/kmeans/cluster.cuh"
+#include "split/device/kmeans/label.cuh"
+#include "split/device/kmeans/propagation.cuh"
+#include "split/device/morph/erode.cuh"
+#include "split/device/sfs/sobel_normals.cuh"
+
+// The one CUDA kernel in these sources (segment_adjacency.cu, never launched)
+// declares an extern shared array; under the host build it needs a symbol.
+namespace split {
+namespace device {
+namespace ccl {
+int s_labels[1];
+}
+}  // namespace device
+}  // namespace split
+
+using split::real;
+using Mat = cusp::array2d<real, cusp::device_memory>;
+using IMat = cusp::array2d<int, cusp::device_memory>;
+using IVec = cusp::array1d<int, cusp::device_memory>;
+
+namespace {
+struct Temp {
+  explicit Temp(std::size_t n) : p(thrust::device_malloc(n > 0 ? n : 1)) {}
+  ~Temp() { thrust::device_free(p); }
+  thrust::device_ptr<void> p;
+};
+template <class A, class T>
+void to_dev(A& a, const T* h, std::size_t n) {
+  thrust::copy(h, h + n, a.values.begin());
+}
+template <class A, class T>
+void to_host(const A& a, T* h, std::size_t n) {
+  thrust::copy(a.values.begin(), a.values.begin() + n, h);
+}
+}  // namespace
+
+extern "C" {
+
+int ref_kmeans_cluster(const float* pts, int dim, int n, float* cent, int k, int32_t* labels,
+                       int iters) {
+  Mat P(dim, n), Cc(dim, k);
+  IVec L(n);
+  to_dev(P, pts, (std::size_t)dim * n);
+  to_dev(Cc, cent, (std::size_t)dim * k);
+  Temp t(split::device::kmeans::cluster_workspace(n, k, dim));
+  split::device::kmeans::cluster(P, Cc, L, t.p, iters, -1.0f);
+  to_host(Cc, cent, (std::size_t)dim * k);
+  thrust::copy(L.begin(), L.end(), labels);
+  return 0;
+}
+
+int ref_label_points(const float* pts, int dim, int n, const float* cent, int k,
+                     int32_t* labels) {
+  Mat P(dim, n), Cc(dim, k);
+  IVec L(n);
+  to_dev(P, pts, (std::size_t)dim * n);
+  to_dev(Cc, cent, (std::size_t)dim * k);
+  Temp t(split::device::kmeans::label_points_workspace(n, k));
+  split::device::kmeans::label_points(Cc, P, L, t.p);
+  thrust::copy(L.begin(), L.end(), labels);
+  return 0;
+}
+
+int ref_calculate_centroids(const int32_t* labels, const float* pts, int dim, int n, float* cent,
+                            int k) {
+  Mat P(dim, n), Cc(dim, k);
+  IVec L(n);
+  to_dev(P, pts, (std::size_t)dim * n);
+  thrust::copy(labels, labels + n, L.begin());
+  Temp t(split::device::kmeans::calculate_centroids_workspace(n, k));
+  split::device::kmeans::calculate_centroids(L, P, Cc, t.p);
+  to_host(Cc, cent, (std::size_t)dim * k);
+  return 0;
+}
+
+int ref_connected_components(const int32_t* in, int w, int h, int32_t* out, int max_iter) {
+  IMat A(h, w);
+  IVec O((std::size_t)w * h);
+  to_dev(A, in, (std::size_t)w * h);
+  Temp t(sizeof(int) * (std::size_t)w * h * 2);
+  split::device::ccl::connected_components(A, t.p, O, max_iter);
+  thrust::copy(O.begin(), O.end(), out);
+  return 0;
+}
+
+int ref_compress_labels(int32_t* labels, int n) {
+  IVec L(n);
+  thrust::copy(labels, labels + n, L.begin());
+  Temp t(sizeof(int) * (std::size_t)n);
+  const int c = split::device::ccl::compress_labels(L, t.p);
+  thrust::copy(L.begin(), L.end(), labels);
+  return c;
+}
+
+int ref_merge_small_segments(const float* chroma, int32_t* labels, int w, int h, int P) {
+  const std::size_t n = (std::size_t)w * h;
+  Mat Ch(2, n);
+  IMat L(h, w);
+  to_dev(Ch, chroma, 2 * n);
+  to_dev(L, labels, n);
+  int mx = 0;
+  for (std::size_t i = 0; i < n; ++i) mx = std::max(mx, (int)labels[i]);
+  Temp t(split::device::ccl::merge_small_segments_workspace((int)n, mx + 1));
+  split::device::ccl::merge_small_segments(Ch, L, t.p, P);
+  to_host(L, labels, n);
+  return 0;
+}
+
+int ref_erode(int32_t* labels, int w, int h, int niter) {
+  IMat L(h, w);
+  to_dev(L, labels, (std::size_t)w * h);
+  split::device::morph::erode(L, niter);
+  to_host(L, labels, (std::size_t)w * h);
+  return 0;
+}
+
+int ref_sobel_normals(const float* heights, int w, int h, float depth, float* normals) {
+  const std::size_t n = (std::size_t)w * h;
+  Mat H(h, w), Nn(3, n);
+  to_dev(H, heights, n);
+  split::device::sfs::sobel_normals(H, Nn, depth);
+  to_host(Nn, normals, 3 * n);
+  return 0;
+}
+
+int ref_propagate_centroids(const int32_t* labels, int n, const float* cent, int dim, int k,
+                            float* out) {
+  IVec L(n);
+  Mat Cc(dim, k), O(dim, n);
+  thrust::copy(labels, labels + n, L.begin());
+  to_dev(Cc, cent, (std::size_t)dim * k);
+  split::device::kmeans::propagate_centroids(L, Cc, O);
+  to_host(O, out, (std::size_t)dim * n);
+  return 0;
+}
+
+}  // extern "C"

@@ -1,0 +1,187 @@
+"""Recipe: build the reference's own segmentation code for the CPU.
+
+Test infrastructure only.  Compiles nitronoid/split's hot-path sources
+(k-means, connected components, label compression, small-segment merge,
+erosion, Sobel normals) with g++ against CUDA 13's Thrust using the OpenMP
+device system, through the CUSP container subset in oracle/cusp_shim, and
+links them with oracle/ref_driver.cpp into oracle/_ref/libsplitref.so.
+
+The reference sources are read from REF_ROOT (default /root/reference) and
+copied into the git-ignored oracle/_ref/src, where two mechanical edits are
+applied to the copies (the reference itself is never modified and nothing of
+it is committed):
+  1. member ``x.get<N>()`` becomes ``thrust::get<N>(x)``: CCCL 3's
+     thrust::tuple is cuda::std::tuple, which has no member get;
+  2. oracle/ref_prelude.h is force-included (host min/max, stand-ins that let
+     g++ parse the one never-launched kernel).
+When the copied sources are present but the reference is not (another
+machine), the copies are compiled as they are.
+"""
+from __future__ import annotations
+
+import concurrent.futures as cf
+import os
+import platform
+import re
+import shutil
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REF_ROOT = os.environ.get("SPLIT_REF_ROOT", "/root/reference")
+OUT = os.path.join(HERE, "_ref")
+SRC = os.path.join(OUT, "src")
+BUILD = os.path.join(OUT, "build", platform.machine())
+LIB = os.path.join(BUILD, "libsplitref.so")
+
+SOURCES = [
+    "split/src/split/device/kmeans/cluster.cu",
+    "split/src/split/device/kmeans/label.cu",
+    "split/src/split/device/kmeans/centroids.cu",
+    "split/src/split/device/kmeans/propagation.cu",
+    "split/src/split/device/ccl/connected_components.cu",
+    "split/src/split/device/ccl/compress_labels.cu",
+    "split/src/split/device/ccl/segment_adjacency.cu",
+    "split/src/split/device/ccl/merge_small_segments.cu",
+    "split/src/split/device/morph/erode.cu",
+    "split/src/split/device/sfs/sobel_normals.cu",
+    "split/src/split/device/detail/normalize_vectors.cu",
+]
+
+_GET = re.compile(r"\.get<(\d+)>\(\)")
+_IDENT = re.compile(r"[A-Za-z0-9_]")
+
+
+def _receiver_start(s: str, end: int) -> int:
+    """Start index of the postfix expression ending just before `end`."""
+    i = end
+    while True:
+        # trailing call / subscript groups
+        while i > 0 and s[i - 1] in ")]":
+            close = s[i - 1]
+            open_ = "(" if close == ")" else "["
+            depth = 0
+            j = i - 1
+            while j >= 0:
+                if s[j] == close:
+                    depth += 1
+                elif s[j] == open_:
+                    depth -= 1
+                    if depth == 0:
+                        break
+                j -= 1
+            i = j
+        # template argument list directly before (e.g. get<0>)
+        if i > 0 and s[i - 1] == ">":
+            depth = 0
+            j = i - 1
+            while j >= 0:
+                if s[j] == ">":
+                    depth += 1
+                elif s[j] == "<":
+                    depth -= 1
+                    if depth == 0:
+                        break
+                j -= 1
+            i = j
+        while i > 0 and _IDENT.match(s[i - 1]):
+            i -= 1
+        if i >= 2 and s[i - 2:i] == "::":
+            i -= 2
+            continue
+        if i >= 1 and s[i - 1] == "." and not (i >= 2 and s[i - 2].isdigit()):
+            i -= 1
+            continue
+        if i >= 2 and s[i - 2:i] == "->":
+            i -= 2
+            continue
+        return i
+
+
+def rewrite_get(text: str) -> str:
+    """Rewrite every member ``.get<N>()`` to ``thrust::get<N>(receiver)``."""
+    while True:
+        m = _GET.search(text)
+        if not m:
+            return text
+        start = _receiver_start(text, m.start())
+        recv = text[start:m.start()]
+        text = text[:start] + f"thrust::get<{m.group(1)}>({recv})" + text[m.end():]
+
+
+def stage_sources(verbose: bool = False) -> bool:
+    """Copy + patch the reference sources into oracle/_ref/src.  Returns False
+    when neither the reference nor an earlier copy is available."""
+    ref_split = os.path.join(REF_ROOT, "split")
+    if not os.path.isdir(ref_split):
+        return os.path.isdir(os.path.join(SRC, "include"))
+    if os.path.isdir(SRC):
+        shutil.rmtree(SRC)
+    os.makedirs(SRC)
+    shutil.copytree(os.path.join(ref_split, "include"), os.path.join(SRC, "include"))
+    for rel in SOURCES:
+        dst = os.path.join(SRC, os.path.basename(rel)[:-3] + ".cpp")
+        with open(os.path.join(REF_ROOT, rel)) as f:
+            text = f.read()
+        with open(dst, "w") as f:
+            f.write(rewrite_get(text))
+    for root, _, files in os.walk(os.path.join(SRC, "include")):
+        for name in files:
+            p = os.path.join(root, name)
+            with open(p) as f:
+                text = f.read()
+            new = rewrite_get(text)
+            if new != text:
+                with open(p, "w") as f:
+                    f.write(new)
+    if verbose:
+        print(f"staged reference sources in {SRC}")
+    return True
+
+
+def _cxx_flags() -> list[str]:
+    cuda_inc = os.path.join(os.environ.get("CUDA_HOME", "/usr/local/cuda"), "include")
+    return ["-O2", "-std=c++17", "-fPIC", "-fopenmp", "-w",
+            "-DTHRUST_DEVICE_SYSTEM=THRUST_DEVICE_SYSTEM_OMP",
+            "-DTHRUST_HOST_SYSTEM=THRUST_HOST_SYSTEM_CPP",
+            "-include", os.path.join(HERE, "ref_prelude.h"),
+            "-I", os.path.join(HERE, "cusp_shim"), "-I", os.path.join(SRC, "include"),
+            "-I", os.path.join(cuda_inc, "cccl"), "-I", cuda_inc]
+
+
+def _compile(args):
+    src, obj = args
+    r = subprocess.run(["g++", *_cxx_flags(), "-c", "-o", obj, src], capture_output=True, text=True)
+    if r.returncode:
+        raise RuntimeError(f"g++ failed on {os.path.basename(src)}:\n{r.stderr[-4000:]}")
+    return obj
+
+
+def build(verbose: bool = False, force: bool = False) -> str | None:
+    """Build oracle/_ref/build/<machine>/libsplitref.so; None when the
+    reference sources are unavailable."""
+    if not stage_sources(verbose) and not os.path.exists(LIB):
+        if verbose:
+            print("reference sources unavailable: CPU reference not built")
+        return None
+    if os.path.exists(LIB) and not force:
+        newest = max(os.path.getmtime(os.path.join(r, f)) for r, _, fs in os.walk(SRC) for f in fs)
+        if os.path.getmtime(LIB) >= max(newest, os.path.getmtime(os.path.join(HERE, "ref_driver.cpp"))):
+            return LIB
+    os.makedirs(BUILD, exist_ok=True)
+    srcs = sorted(os.path.join(SRC, f) for f in os.listdir(SRC) if f.endswith(".cpp"))
+    srcs.append(os.path.join(HERE, "ref_driver.cpp"))
+    jobs = [(s, os.path.join(BUILD, os.path.basename(s)[:-4] + ".o")) for s in srcs]
+    with cf.ThreadPoolExecutor(max_workers=min(16, os.cpu_count() or 4)) as ex:
+        objs = list(ex.map(_compile, jobs))
+    r = subprocess.run(["g++", "-shared", "-fopenmp", "-o", LIB, *objs], capture_output=True,
+                       text=True)
+    if r.returncode:
+        raise RuntimeError("link failed:\n" + r.stderr[-4000:])
+    if verbose:
+        print(f"built {LIB}")
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(verbose=True, force="--force" in sys.argv))

@@ -1,0 +1,92 @@
+"""Generate tests/golden/reference_golden.npz from the reference's own code.
+
+Runs nitronoid/split's segmentation entry points, compiled for the CPU by
+oracle/refbuild.py (needs the reference sources), on seeded synthetic inputs
+and stores their outputs.  Inputs are not stored: they are regenerated from
+the seeds by split_gb300.synth, and a SHA-256 of each generated input is kept
+so a generator change is caught.
+
+    python tests/golden/make_golden.py
+
+Known limit of the CPU build: CCCL 3.0.1's host sort orders negative int keys
+after non-negative ones, so compress_labels is only recorded on non-negative
+labels (the reference's GPU build sorts with CUB and is not affected).
+"""
+from __future__ import annotations
+
+import hashlib
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+OUT = os.path.join(HERE, "reference_golden.npz")
+
+
+def sha(a: np.ndarray) -> str:
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+def inputs():
+    """Seeded inputs shared by make_golden and the tests (same recipe)."""
+    from split_gb300 import synth
+    d = {}
+    # k-means case: the 512 x 512 Voronoi + noise recipe, 32 cells, sigma 4
+    rgb = synth.voronoi_rgb8(0x51, 512, 512, 32, sigma=4.0)
+    d["km_rgb"] = rgb
+    d["km_points"] = synth.features(rgb, 3)
+    d["km_c0"] = synth.pick_centroids(0x51, rgb, 8, 3)
+    # labelling: a maze image and a blocky random label image
+    d["maze"] = synth.maze_labels(0x52, 256, 192)
+    rng = np.random.default_rng(0x53)
+    blk = rng.integers(0, 4, size=(50, 70)).repeat(4, 0).repeat(4, 1)
+    blk[rng.random(blk.shape) < 0.04] = 9
+    d["blocks"] = blk.astype(np.int32)
+    # chroma for the merge: multiples of 1/256, so float sums are exact
+    d["chroma"] = (rng.integers(0, 256, size=(2, blk.size)) / 256.0).astype(np.float32)
+    # heights for the normals
+    d["heights"] = rng.random((48, 64), dtype=np.float32)
+    return d
+
+
+def main():
+    from oracle import ref
+    d = inputs()
+    g = {}
+    for k in ("km_rgb", "maze", "blocks", "chroma", "heights"):
+        g["sha_" + k] = np.array(sha(d[k]))
+    pts, c0 = d["km_points"], d["km_c0"]
+    # one assignment step and one update step
+    lab1 = ref.label_points(pts, c0)
+    g["km_label_points"] = lab1.astype(np.uint8)
+    g["km_calculate_centroids"] = ref.calculate_centroids(lab1, pts, c0.shape[1])
+    # the full 10-iteration clustering (threshold < 0: exactly 10)
+    lab10, c10 = ref.kmeans_cluster(pts, c0, 10)
+    g["km_cluster10_labels"] = lab10.astype(np.uint8)
+    g["km_cluster10_centroids"] = c10
+    # connected components (4-connected, converged max-index labels)
+    km_img = lab10.reshape(512, 512)
+    g["ccl_km"] = ref.connected_components(km_img)
+    g["ccl_maze"] = ref.connected_components(d["maze"])
+    g["ccl_blocks"] = ref.connected_components(d["blocks"])
+    # compression of the component labels (non-negative)
+    comp, ncomp = ref.compress_labels(g["ccl_blocks"])
+    g["compress_blocks"] = comp
+    g["compress_blocks_count"] = np.array(ncomp)
+    # merge of segments < 24 px, reference chroma rule, on compressed labels
+    g["merge_blocks_P24"] = ref.merge_small_segments(d["chroma"], comp, 24)
+    # erosion of the component labels, n = 1 and n = 2
+    g["erode1_km"] = ref.erode(g["ccl_km"], 1)
+    g["erode2_blocks"] = ref.erode(g["ccl_blocks"], 2)
+    # Sobel normals of a height map, depth 1
+    g["sobel_normals"] = ref.sobel_normals(d["heights"], 1.0)
+    np.savez_compressed(OUT, **g)
+    print(f"wrote {OUT} ({os.path.getsize(OUT) / 1024:.0f} KiB)")
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,90 @@
+"""The C-ABI library loads on a machine without a GPU and exports every
+entry point declared in include/*.h; host-only queries work.  CPU only."""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+from split_gb300 import _native, synth
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    names = []
+    for h in ("split_gb300.h", "split_synth.h"):
+        text = open(os.path.join(ROOT, "include", h)).read()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        names += re.findall(r"\b(split_[a-z0-9_]+)\s*\(", text)
+    return sorted(set(names))
+
+
+def test_every_declared_symbol_is_exported():
+    lib = _native.load()
+    names = declared_functions()
+    assert len(names) >= 25
+    for n in names:
+        assert hasattr(lib, n), n
+        assert n in _native.exported_symbols(), f"{n} has no ctypes signature"
+
+
+def test_version_and_status_strings():
+    lib = _native.load()
+    assert b"sm_103a" in lib.split_version()
+    for s in range(8):
+        assert lib.split_status_string(s)
+
+
+def test_workspace_queries():
+    lib = _native.load()
+    assert lib.split_ccl_workspace_size(3840, 2160) >= 256
+    ws = lib.split_kmeans_cluster_workspace_size_2d(3840 * 2160, 3840, 16, 5)
+    assert 256 < ws < 64 << 20
+    # without the width the bound covers the worst case (width 1)
+    assert lib.split_kmeans_cluster_workspace_size(3840 * 2160, 16, 5) >= ws
+    assert lib.split_merge_small_workspace_size(3840, 2160) > 3840 * 2160 * 16
+    assert lib.split_compress_labels_workspace_size(1000) >= 4 * 1001
+    p = _native.PipelineParams(16, 5, 0.1, 20, -1.0, 1, 8, 0, 256, 0, 1, 1, 1.0)
+    assert lib.split_pipeline_workspace_size(3840, 2160, C.byref(p)) > 0
+    bad = _native.PipelineParams(65, 5, 0.1, 20, -1.0, 1, 8, 0, 256, 0, 1, 1, 1.0)
+    assert lib.split_pipeline_workspace_size(3840, 2160, C.byref(bad)) == 0
+
+
+def test_invalid_arguments_rejected_on_host():
+    lib = _native.load()
+    # null pointers and bad sizes fail before touching the device
+    assert lib.split_ccl(None, 4, 4, 4, 0, None, None, None, 0, None) == _native.ERR_INVALID
+    assert lib.split_erode(None, None, 4, 4, 1, None) == _native.ERR_INVALID
+    assert lib.split_kmeans_cluster(None, 0, 3, 10, 1, 0.1, None, 4, None, None, 0, 1, -1.0,
+                                    None, None) == _native.ERR_INVALID
+
+
+def test_synth_deterministic():
+    a = synth.voronoi_rgb8(11, 97, 61, 12, npalette=5, illum_gradient=True, sigma=3.0)
+    b = synth.voronoi_rgb8(11, 97, 61, 12, npalette=5, illum_gradient=True, sigma=3.0)
+    assert np.array_equal(a, b)
+    assert not np.array_equal(a, synth.voronoi_rgb8(12, 97, 61, 12, npalette=5,
+                                                    illum_gradient=True, sigma=3.0))
+    c = synth.pick_centroids(11, a, 8, 5)
+    assert c.shape == (5, 8) and np.isfinite(c).all()
+    # distinct picks
+    assert len({tuple(c[:, k]) for k in range(8)}) == 8
+
+
+def test_maze_shape():
+    m = synth.maze_labels(5, 512, 512)
+    frac = (m == 0).mean()
+    assert 0.4 < frac < 0.55            # the serpentine covers about half
+    assert len(np.unique(m)) > 500      # plus many small blobs
+
+
+def test_python_layer_rejects_cpu_tensors():
+    torch = pytest.importorskip("torch")
+    from split_gb300 import ccl, kmeans
+    x = torch.zeros((4, 4), dtype=torch.int32)
+    with pytest.raises(ValueError):
+        ccl.connected_components(x, None, x)
+    with pytest.raises(ValueError):
+        kmeans.cluster(torch.zeros((3, 8)), torch.zeros((3, 2)), torch.zeros(8, dtype=torch.int32))

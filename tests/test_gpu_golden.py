@@ -1,0 +1,111 @@
+"""The CUDA path (through the C ABI) against the reference's own outputs
+(tests/golden/reference_golden.npz)."""
+import os
+import sys
+
+import numpy as np
+import pytest
+
+import oracle
+
+pytestmark = pytest.mark.gpu
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(HERE, "golden"))
+import make_golden  # noqa: E402
+
+G = np.load(os.path.join(HERE, "golden", "reference_golden.npz"))
+
+
+@pytest.fixture(scope="module")
+def inp():
+    return make_golden.inputs()
+
+
+def _t(a, dev):
+    import torch
+    return torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+
+
+@pytest.mark.parametrize("name,src", [("ccl_maze", "maze"), ("ccl_blocks", "blocks"),
+                                      ("ccl_km", None)])
+def test_ccl_reference_convention(cuda, inp, name, src):
+    import torch
+    from split_gb300 import ccl
+    lab = inp[src] if src else G["km_cluster10_labels"].astype(np.int32).reshape(512, 512)
+    out = torch.empty(lab.shape, dtype=torch.int32, device=cuda)
+    ccl.connected_components(_t(lab, cuda), None, out, connectivity=4, convention=ccl.MAX_INDEX)
+    assert np.array_equal(out.cpu().numpy(), G[name])
+
+
+def test_compress_labels(cuda):
+    from split_gb300 import ccl
+    lab = _t(G["ccl_blocks"], cuda).view(-1)
+    n = ccl.compress_labels(lab)
+    assert n == int(G["compress_blocks_count"])
+    assert np.array_equal(lab.view(200, 280).cpu().numpy(), G["compress_blocks"])
+
+
+def test_compress_labels_with_eroded_pixels(cuda):
+    # -1 (eroded) ranks first, as the sample expects (main.cu:302-314)
+    from split_gb300 import ccl
+    lab = G["erode2_blocks"]
+    want, n = oracle.compress_labels(lab)
+    g = _t(lab, cuda).view(-1)
+    assert ccl.compress_labels(g) == n
+    assert np.array_equal(g.cpu().numpy(), want.reshape(-1))
+
+
+def test_merge_reference_chroma(cuda, inp):
+    from split_gb300 import ccl
+    g = _t(G["compress_blocks"], cuda)
+    ccl.merge_small_segments(_t(inp["chroma"], cuda), g, None, 24, policy=ccl.REF_CHROMA)
+    assert np.array_equal(g.cpu().numpy(), G["merge_blocks_P24"])
+
+
+@pytest.mark.parametrize("name,src,r", [("erode1_km", "ccl_km", 1), ("erode2_blocks", "ccl_blocks", 2)])
+def test_erode(cuda, name, src, r):
+    import torch
+    from split_gb300 import morph
+    lab = G[src]
+    out = morph.erode(_t(lab, cuda), r, out=torch.empty(lab.shape, dtype=torch.int32, device=cuda))
+    assert np.array_equal(out.cpu().numpy(), G[name])
+
+
+def test_sobel_normals(cuda, inp):
+    import torch
+    from split_gb300 import sfs
+    h = inp["heights"]
+    out = torch.empty((3, h.size), dtype=torch.float32, device=cuda)
+    sfs.sobel_normals(_t(h, cuda), out, 1.0)
+    got = out.cpu().numpy().astype(np.float64)
+    ref = G["sobel_normals"].astype(np.float64)
+    ang = np.arccos(np.clip((got * ref).sum(0) / np.linalg.norm(got, axis=0), -1, 1))
+    assert ang.max() <= 1e-3       # the reference's own FP32 drift
+    f64 = oracle.sobel_normals_f64(h, 1.0)
+    ang = np.arccos(np.clip((got * f64).sum(0) / np.linalg.norm(got, axis=0), -1, 1))
+    assert ang.max() <= 1e-4
+
+
+def test_label_points(cuda, inp):
+    import torch
+    from split_gb300 import kmeans
+    pts, c0 = inp["km_points"], inp["km_c0"]
+    lab = torch.empty(pts.shape[1], dtype=torch.int32, device=cuda)
+    kmeans.label_points(_t(c0, cuda), _t(pts, cuda), lab, None, width=512)
+    _, d1, d2 = oracle.kmeans_assign_f64(pts, c0)
+    near = (d2 - d1) <= 1e-5 * d2
+    ref = G["km_label_points"].astype(np.int32)
+    assert ((lab.cpu().numpy() != ref) & ~near).sum() == 0
+
+
+def test_cluster_10_iterations(cuda, inp):
+    import torch
+    from split_gb300 import kmeans
+    pts, c0 = inp["km_points"], inp["km_c0"]
+    cent = _t(c0, cuda)
+    lab = torch.empty(pts.shape[1], dtype=torch.int32, device=cuda)
+    kmeans.cluster(_t(pts, cuda), cent, lab, None, max_iter=10, threshold=-1.0, width=512)
+    assert (lab.cpu().numpy() != G["km_cluster10_labels"]).mean() <= 1e-3
+    rc = G["km_cluster10_centroids"]
+    assert (np.abs(cent.cpu().numpy() - rc) / np.abs(rc)).max() <= 1e-3

@@ -1,0 +1,105 @@
+"""The oracle restatement pinned against the reference's own outputs
+(tests/golden/reference_golden.npz, made by tests/golden/make_golden.py from
+the reference compiled for the CPU).  CPU only."""
+import os
+import sys
+
+import numpy as np
+import pytest
+
+import oracle
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(HERE, "golden"))
+import make_golden  # noqa: E402
+
+GOLDEN = np.load(os.path.join(HERE, "golden", "reference_golden.npz"))
+
+
+@pytest.fixture(scope="module")
+def inp():
+    return make_golden.inputs()
+
+
+def test_generated_inputs_unchanged(inp):
+    for k in ("km_rgb", "maze", "blocks", "chroma", "heights"):
+        assert make_golden.sha(inp[k]) == str(GOLDEN["sha_" + k]), k
+
+
+def test_label_points(inp):
+    # reference: float (x-c)^2 sums; oracle f32 fma chain.  Identical except
+    # where the best-vs-second gap is below 1e-5 relative.
+    lab, d1, d2 = oracle.kmeans_assign_f64(inp["km_points"], inp["km_c0"])
+    ref = GOLDEN["km_label_points"].astype(np.int32)
+    near = (d2 - d1) <= 1e-5 * d2
+    assert ((lab != ref) & ~near).sum() == 0
+    f32 = oracle.kmeans_assign_f32(inp["km_points"], inp["km_c0"])
+    assert ((f32 != ref) & ~near).sum() == 0
+
+
+def test_calculate_centroids(inp):
+    ref_lab = GOLDEN["km_label_points"].astype(np.int32)
+    c, cnt = oracle.kmeans_update_f64(ref_lab, inp["km_points"], inp["km_c0"])
+    assert (cnt > 0).all()
+    ref = GOLDEN["km_calculate_centroids"].astype(np.float64)
+    # The reference sums up to 57k members per cluster sequentially in FP32
+    # (reduce_by_key, centroids.cu:78-90): it sits up to a few 1e-4 from the
+    # exact mean.  A sequential FP32 sum times the FP32 reciprocal count
+    # (centroids.cu:60-63, :96-100) reproduces it to within 2 ulp.
+    assert (np.abs(ref - c) / np.abs(c)).max() <= 1e-3
+    pts = inp["km_points"]
+    for k in range(ref.shape[1]):
+        m = ref_lab == k
+        for d in range(pts.shape[0]):
+            s = np.cumsum(pts[d, m], dtype=np.float32)[-1]
+            emu = np.float32(s * (np.float32(1) / np.float32(m.sum())))
+            assert abs(np.float32(ref[d, k]) - emu) <= 2 * np.spacing(emu)
+
+
+def test_cluster_10_iterations(inp):
+    pts, c = inp["km_points"], inp["km_c0"].copy()
+    for _ in range(10):
+        lab = oracle.kmeans_assign_f32(pts, c)
+        c64, _ = oracle.kmeans_update_f64(lab, pts, c)
+        c = c64.astype(np.float32)
+    ref_lab = GOLDEN["km_cluster10_labels"].astype(np.int32)
+    # two trajectories (reference: FP32 sequential sums; oracle: FP64 means)
+    # through 10 iterations: labels differ only where rounding moved a
+    # near-tie pixel, centroids by the reference's accumulation error
+    assert (lab != ref_lab).mean() <= 1e-3
+    ref_c = GOLDEN["km_cluster10_centroids"]
+    assert (np.abs(ref_c - c) / np.abs(c)).max() <= 1e-3
+
+
+@pytest.mark.parametrize("name,key", [("ccl_maze", "maze"), ("ccl_blocks", "blocks")])
+def test_connected_components(inp, name, key):
+    assert np.array_equal(oracle.ccl(inp[key], 4, 1), GOLDEN[name])
+
+
+def test_connected_components_on_kmeans_labels():
+    km = GOLDEN["km_cluster10_labels"].astype(np.int32).reshape(512, 512)
+    assert np.array_equal(oracle.ccl(km, 4, 1), GOLDEN["ccl_km"])
+
+
+def test_compress_labels():
+    comp, n = oracle.compress_labels(GOLDEN["ccl_blocks"])
+    assert n == int(GOLDEN["compress_blocks_count"])
+    assert np.array_equal(comp, GOLDEN["compress_blocks"])
+
+
+def test_merge_reference_chroma(inp):
+    out = oracle.merge_small(GOLDEN["compress_blocks"], 24, 1, inp["chroma"])
+    assert np.array_equal(out, GOLDEN["merge_blocks_P24"])
+
+
+def test_erode():
+    assert np.array_equal(oracle.erode(GOLDEN["ccl_km"], 1), GOLDEN["erode1_km"])
+    assert np.array_equal(oracle.erode(GOLDEN["ccl_blocks"], 2), GOLDEN["erode2_blocks"])
+
+
+def test_sobel_normals(inp):
+    o = oracle.sobel_normals_f64(inp["heights"], 1.0)
+    r = GOLDEN["sobel_normals"].astype(np.float64)
+    ang = np.arccos(np.clip((o * r).sum(0) / np.linalg.norm(r, axis=0), -1, 1))
+    # the reference's FP32 prefix-scan formulation drifts from FP64
+    assert ang.max() <= 1e-3
