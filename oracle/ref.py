@@ -35,6 +35,7 @@ def load():
             "ref_erode": [vp, i32, i32, i32],
             "ref_sobel_normals": [vp, i32, i32, f32, vp],
             "ref_propagate_centroids": [vp, i32, vp, i32, i32, vp],
+            "ref_rgb_to_lab": [vp, i32, vp],
         }
         for name, args in sigs.items():
             fn = getattr(lib, name)
@@ -115,3 +116,31 @@ def propagate_centroids(labels, centroids):
     out = np.empty((c.shape[0], lab.size), np.float32)
     load().ref_propagate_centroids(_p(lab), lab.size, _p(c), c.shape[0], c.shape[1], _p(out))
     return out
+
+
+def rgb_to_lab(rgb_planar):
+    """(3, N) float RGB in [0, 1] -> (3, N) L*a*b* (conversion.inl:88-92)."""
+    a = np.ascontiguousarray(rgb_planar, np.float32)
+    out = np.empty_like(a)
+    load().ref_rgb_to_lab(_p(a), a.shape[1], _p(out))
+    return out
+
+
+class quiet:
+    """Silences the reference's progress prints (std::cout / printf) on the
+    process's stdout for the duration of a block."""
+
+    def __enter__(self):
+        import sys
+        sys.stdout.flush()
+        self._fd = os.dup(1)
+        self._null = os.open(os.devnull, os.O_WRONLY)
+        os.dup2(self._null, 1)
+        return self
+
+    def __exit__(self, *exc):
+        libc = C.CDLL(None)
+        libc.fflush(None)
+        os.dup2(self._fd, 1)
+        os.close(self._fd)
+        os.close(self._null)

@@ -13,6 +13,7 @@
 #include <thrust/device_free.h>
 
 #include "split/device/ccl/compress_labels.cuh"
+#include "split/device/color/conversion.cuh"
 #include "split/device/ccl/connected_components.cuh"
 #include "split/device/ccl/merge_small_segments.cuh"
 #include "split/device/kmeans/centroids.cuh"
@@ -139,6 +140,14 @@ int ref_sobel_normals(const float* heights, int w, int h, float depth, float* no
   to_dev(H, heights, n);
   split::device::sfs::sobel_normals(H, Nn, depth);
   to_host(Nn, normals, 3 * n);
+  return 0;
+}
+
+int ref_rgb_to_lab(const float* rgb, int n, float* lab) {
+  Mat A(3, n), B(3, n);
+  to_dev(A, rgb, 3 * (std::size_t)n);
+  split::device::color::convert_color_space(A, B, split::device::color::rgb_to_lab<>());
+  to_host(B, lab, 3 * (std::size_t)n);
   return 0;
 }
 
