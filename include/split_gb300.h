@@ -111,6 +111,31 @@ int split_kmeans_cluster(const void* points, int layout, int dim,
                          void* workspace, size_t workspace_bytes, int max_iter,
                          float threshold, int32_t* d_iterations, void* stream);
 
+/* Allocation-free variant of split_kmeans_cluster (same arguments and
+ * results, no workspace).  It has no counterpart in the reference.  It is for
+ * callers that cannot allocate device memory where they cluster: code running
+ * during CUDA graph capture or inside a latency-critical serving loop (where
+ * cudaMalloc / cudaFree would synchronise the device), and host plugins whose
+ * device memory belongs to a pool they may not touch.  Its scratch is one
+ * fixed-size device array in the library, held by every GPU that loads the
+ * library until the process exits.
+ *   - Limit: the image may span at most 2048 tiles of 64 x 64 pixels (for
+ *     example 3840 x 2160); larger images return SPLIT_ERR_WORKSPACE before
+ *     any work is queued.
+ *   - The first call on each device looks up the array's device address
+ *     (cudaGetSymbolAddress) with that device current; make that first call
+ *     before any stream capture.
+ *   - All calls share the array and overwrite it: calls whose work overlaps
+ *     on the GPU race.  Order them on one stream.
+ *   - d_status (device int, optional) receives the device-side status word
+ *     (0, or e.g. SPLIT_ERR_TIMEOUT) when the work completes. */
+int split_kmeans_cluster_noalloc(const void* points, int layout, int dim,
+                                 int64_t npoints, int width, float xy_scale,
+                                 float* centroids, int nclusters,
+                                 int32_t* labels, int max_iter,
+                                 float threshold, int32_t* d_iterations,
+                                 int32_t* d_status, void* stream);
+
 /* Replaces split::device::kmeans::label_points_workspace (label.cuh:39-40). */
 size_t split_kmeans_assign_workspace_size(int64_t npoints, int nclusters);
 

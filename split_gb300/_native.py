@@ -31,6 +31,8 @@ _SIGS = {
     "split_kmeans_cluster_workspace_size_2d": (_sz, [_i64, _i32, _i32, _i32]),
     "split_kmeans_cluster": (_i32, [_vp, _i32, _i32, _i64, _i32, _f32, _vp, _i32, _vp, _vp, _sz,
                                     _i32, _f32, _vp, _vp]),
+    "split_kmeans_cluster_noalloc": (_i32, [_vp, _i32, _i32, _i64, _i32, _f32, _vp, _i32, _vp,
+                                            _i32, _f32, _vp, _vp, _vp]),
     "split_kmeans_assign_workspace_size": (_sz, [_i64, _i32]),
     "split_kmeans_assign": (_i32, [_vp, _i32, _i32, _i64, _i32, _f32, _vp, _i32, _vp, _vp, _sz,
                                    _vp]),

@@ -1039,3 +1039,94 @@ extern "C" int split_kmeans_propagate(const int32_t* labels, int64_t npoints,
                                                                 nclusters, dim, out);
   return launch_status();
 }
+
+// ---------------------------------------------------------------------------
+// Allocation-free clustering.  Some callers cannot allocate device memory at
+// the point where they cluster: code running while a CUDA graph is being
+// captured or inside a latency-critical serving loop (cudaMalloc and
+// cudaFree synchronise the device), and host plugins whose device memory is
+// owned by a pool they may not touch.  This variant keeps its scratch in one
+// file-scope device array of fixed size, so a call needs no workspace.
+//
+// Limits and sharing rules:
+//   - the image may span at most kStaticTiles 64 x 64 tiles (2048: a
+//     3840 x 2160 frame fits); larger images are rejected with
+//     SPLIT_ERR_WORKSPACE before anything is launched;
+//   - every GPU that loads the library holds the array until the process
+//     exits; its device address is looked up once per device, on the first
+//     call made with that device current;
+//   - all calls share the array: two calls whose work overlaps on the GPU
+//     (different streams, or different host threads without ordering) race
+//     and corrupt each other's results.  Order them on one stream.
+// ---------------------------------------------------------------------------
+#include <mutex>
+
+namespace sg {
+namespace km {
+
+constexpr int kStaticTiles = 2048;
+constexpr int kStaticGroups = (kStaticTiles + kGroup - 1) / kGroup;
+
+// Size of carve(ws, kStaticTiles, kStaticGroups, 1), evaluated at compile time.
+constexpr size_t round256(size_t v) { return (v + 255) & ~size_t(255); }
+constexpr size_t kStaticBytes =
+    round256(round256(round256(round256(round256(round256(round256(sizeof(WsHeader)) +
+                                                          (size_t)kStaticTiles * kRec * 4) +
+                                                 (size_t)kStaticGroups * kRec * 4) +
+                                        (size_t)2 * kMaxK * 8 * 4) +
+                               (size_t)kStaticGroups * 4) +
+                      4) +
+             sizeof(ImageState));
+
+static __device__ __align__(256) unsigned char g_static_scratch[kStaticBytes];
+
+// Device address of g_static_scratch on the current device (looked up once).
+static int static_scratch(void** out) {
+  static std::mutex mu;
+  static void* addr[64] = {nullptr};
+  int dev = 0;
+  SG_CUDA_TRY(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) return SPLIT_ERR_CUDA;
+  std::lock_guard<std::mutex> lock(mu);
+  if (!addr[dev]) {
+    void* p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_static_scratch) != cudaSuccess || !p) return SPLIT_ERR_CUDA;
+    addr[dev] = p;
+  }
+  *out = addr[dev];
+  return SPLIT_OK;
+}
+
+}  // namespace km
+}  // namespace sg
+
+extern "C" int split_kmeans_cluster_noalloc(const void* points, int layout, int dim,
+                                            int64_t npoints, int width, float xy_scale,
+                                            float* centroids, int nclusters, int32_t* labels,
+                                            int max_iter, float threshold,
+                                            int32_t* d_iterations, int32_t* d_status,
+                                            void* stream) {
+  using namespace sg::km;
+  if (!centroids || !labels || npoints <= 0 || width < 1) return SPLIT_ERR_INVALID;
+  const int units = units_of(npoints, width), groups = groups_of(units);
+  if (units > kStaticTiles) return SPLIT_ERR_WORKSPACE;
+  const size_t need = carve(nullptr, units, groups, 1).bytes;
+  if (need > kStaticBytes) return SPLIT_ERR_WORKSPACE;
+  void* ws = nullptr;
+  SG_TRY(static_scratch(&ws));
+  cudaStream_t st = as_stream(stream);
+  // The array keeps the previous call's contents: the header (status word,
+  // barrier words, work counters) and the group / image arrival counters
+  // must start at zero.
+  Layout l = carve(ws, units, groups, 1);
+  SG_CUDA_TRY(cudaMemsetAsync(l.hdr, 0, sizeof(WsHeader), st));
+  SG_CUDA_TRY(cudaMemsetAsync(l.group_cnt, 0, sizeof(unsigned) * (size_t)groups, st));
+  SG_CUDA_TRY(cudaMemsetAsync(l.image_cnt, 0, sizeof(unsigned), st));
+  SG_TRY(run(kCluster, points, layout, dim, npoints, width, xy_scale, centroids, centroids,
+             nclusters, labels, nullptr, ws, kStaticBytes, max_iter, threshold, d_iterations,
+             st));
+  if (d_status)
+    SG_CUDA_TRY(cudaMemcpyAsync(d_status, &l.hdr->status, sizeof(int), cudaMemcpyDeviceToDevice,
+                                st));
+  return SPLIT_OK;
+}
