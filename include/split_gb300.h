@@ -299,6 +299,49 @@ int split_pipeline_run(const uint8_t* rgb, int width, int height,
                        float* normals, void* workspace, size_t workspace_bytes,
                        void* const* stage_events, void* stream);
 
+/* ======================================================================== */
+/* batches                                                                   */
+/* ======================================================================== */
+
+/* Many images of uneven size and per-image K / iteration count through the
+ * segmentation path in one fixed launch sequence (about 16 launches whatever
+ * the image count; the k-means stage is one cooperative launch over every
+ * image's tiles).  Each image's results are identical to running it alone. */
+typedef struct split_batch_image {
+  int width, height;
+  int nclusters;    /* K <= 64 */
+  int kmeans_iters;
+} split_batch_image;
+
+typedef struct split_batch split_batch; /* opaque host-side plan */
+
+/* params: as for split_pipeline_run; nclusters and kmeans_iters come from the
+ * images instead; erode_radius must be >= 1. */
+int split_batch_create(const split_batch_image* images, int nimages,
+                       const split_pipeline_params* params, split_batch** out);
+void split_batch_destroy(split_batch* batch);
+size_t split_batch_workspace_size(const split_batch* batch);
+/* Arena layout: image i's pixels start at pixel_offset(i) (a multiple of 64);
+ * the RGB8 arena holds 3 bytes, the label arenas one int32 and the normals
+ * arena 3 planes of floats (image i's planes start at 3 * pixel_offset(i))
+ * per arena pixel.  Centroids: image i's dim x K planar block starts at
+ * centroid_offset(i) (in floats). */
+int64_t split_batch_arena_pixels(const split_batch* batch);
+int64_t split_batch_pixel_offset(const split_batch* batch, int image);
+int64_t split_batch_centroid_floats(const split_batch* batch);
+int64_t split_batch_centroid_offset(const split_batch* batch, int image);
+/* Binds device buffers and a zero-filled workspace: uploads the image
+ * descriptors and tensor maps (synchronises `stream`; not capturable). */
+int split_batch_bind(split_batch* batch, const uint8_t* rgb, float* centroids,
+                     int32_t* cluster_labels, int32_t* segment_labels,
+                     float* normals, void* workspace, size_t workspace_bytes,
+                     void* stream);
+/* Runs the bound batch: kernel launches and memsets only, so the call can be
+ * captured into a CUDA graph.  `centroids` must hold the initial centroids;
+ * segment labels come out image-local (minimum linear index within the
+ * image, -1 = eroded). */
+int split_batch_run(split_batch* batch, void* stream);
+
 /* Kernels launched by this library since it was loaded (all entry points). */
 unsigned long long split_launch_count(void);
 

@@ -54,6 +54,15 @@ _SIGS = {
     "split_pipeline_workspace_size": (_sz, [_i32, _i32, _vp]),
     "split_pipeline_run": (_i32, [_vp, _i32, _i32, _vp, _vp, _vp, _vp, _vp, _vp, _sz, _vp, _vp]),
     "split_launch_count": (C.c_ulonglong, []),
+    "split_batch_create": (_i32, [_vp, _i32, _vp, _vp]),
+    "split_batch_destroy": (None, [_vp]),
+    "split_batch_workspace_size": (_sz, [_vp]),
+    "split_batch_arena_pixels": (_i64, [_vp]),
+    "split_batch_pixel_offset": (_i64, [_vp, _i32]),
+    "split_batch_centroid_floats": (_i64, [_vp]),
+    "split_batch_centroid_offset": (_i64, [_vp, _i32]),
+    "split_batch_bind": (_i32, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _sz, _vp]),
+    "split_batch_run": (_i32, [_vp, _vp]),
     "split_synth_voronoi_rgb8": (_i32, [_u64, _i32, _i32, _i32, _i32, _i32, C.c_double, _vp]),
     "split_synth_pick_centroids": (_i32, [_u64, _vp, _i32, _i32, _i32, _i32, _f32, _vp]),
     "split_synth_feature_u8": (_f32, [C.c_uint8]),
@@ -71,6 +80,12 @@ class PipelineParams(C.Structure):
 
 
 PIPELINE_STAGES = ("pack", "kmeans", "ccl", "merge", "erode", "normals")
+
+
+class BatchImage(C.Structure):
+    """split_batch_image (include/split_gb300.h)."""
+    _fields_ = [("width", C.c_int), ("height", C.c_int), ("nclusters", C.c_int),
+                ("kmeans_iters", C.c_int)]
 
 
 class SplitError(RuntimeError):

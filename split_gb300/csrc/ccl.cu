@@ -22,12 +22,12 @@
 //
 // compress_labels (compress_labels.cu:10-35) is a flag / scan / gather over
 // the label range [-1, n).
-#include "common.cuh"
+#include "geom.cuh"
 
 namespace sg {
 namespace ccl {
 
-constexpr int TH = 32, TW = 64, kThreads = 256;
+constexpr int TH = kTileH, TW = kTileW, kThreads = 256;
 constexpr unsigned kUnionCap = 1u << 22;
 
 template <bool MAXC>
@@ -106,16 +106,18 @@ __device__ void gunite(int* P, int a, int b, int* status) {
 //        either (E's own N link covers NE).
 template <bool MAXC, int CONN>
 __global__ void __launch_bounds__(kThreads)
-tile_kernel(const int32_t* __restrict__ in, int W, int H, int* __restrict__ P,
+tile_kernel(const int32_t* __restrict__ in, Geoms gs, int* __restrict__ P,
             int32_t* __restrict__ sizes, int* status) {
   static_assert(TW == 64 && TH * TW == kThreads * 8, "8 pixels per thread");
   __shared__ int lab[TH * TW];
   __shared__ int par[TH * TW];
-  const int tx0 = blockIdx.x * TW, ty0 = blockIdx.y * TH;
+  const TileRef t = tile_ref(gs, blockIdx.x);
+  const int W = t.W, H = t.H, tx0 = t.tx0, ty0 = t.ty0;
+  const long long off = t.off;
   const int tw = min(TW, W - tx0), th = min(TH, H - ty0);
   for (int i = threadIdx.x; i < TH * TW; i += kThreads) {
     const int r = i / TW, c = i % TW;
-    lab[i] = (r < th && c < tw) ? __ldg(in + (size_t)(ty0 + r) * W + tx0 + c) : 0;
+    lab[i] = (r < th && c < tw) ? __ldg(in + off + (long long)(ty0 + r) * W + tx0 + c) : 0;
   }
   __syncthreads();
   const int r = threadIdx.x >> 3, c0 = (threadIdx.x & 7) * 8;
@@ -175,8 +177,8 @@ tile_kernel(const int32_t* __restrict__ in, int W, int H, int* __restrict__ P,
       if (c >= tw) break;
       const int i = base + j;
       const int root = sfind(par, i);
-      const int g = (ty0 + r) * W + tx0 + c;
-      P[g] = (ty0 + root / TW) * W + tx0 + root % TW;
+      const long long g = off + (long long)(ty0 + r) * W + tx0 + c;
+      P[g] = (int)(off + (long long)(ty0 + root / TW) * W + tx0 + root % TW);
       if (sizes && root == i) sizes[g] = 0;
     }
   }
@@ -184,9 +186,11 @@ tile_kernel(const int32_t* __restrict__ in, int W, int H, int* __restrict__ P,
 
 template <bool MAXC, int CONN>
 __global__ void __launch_bounds__(kThreads)
-border_kernel(const int32_t* __restrict__ in, int W, int H, int* P, int* status) {
-  const int tx0 = blockIdx.x * TW, ty0 = blockIdx.y * TH;
-  const int tw = min(TW, W - tx0), th = min(TH, H - ty0);
+border_kernel(const int32_t* __restrict__ in, Geoms gs, int* P, int* status) {
+  const TileRef t = tile_ref(gs, blockIdx.x);
+  const int W = t.W, tx0 = t.tx0, ty0 = t.ty0;
+  const long long off = t.off;
+  const int tw = min(TW, W - tx0), th = min(TH, t.H - ty0);
   // top row (tw pixels), left column (th - 1 pixels), right column (th - 1)
   const int nb = tw + 2 * (th - 1);
   for (int j = threadIdx.x; j < nb; j += kThreads) {
@@ -195,7 +199,7 @@ border_kernel(const int32_t* __restrict__ in, int W, int H, int* P, int* status)
     else if (j < tw + th - 1) { r = j - tw + 1; c = 0; }
     else { r = j - tw - th + 2; c = tw - 1; }
     const int x = tx0 + c, y = ty0 + r;
-    const int g = y * W + x;
+    const int g = (int)(off + (long long)y * W + x);
     const int v = __ldg(in + g);
     // backward neighbours that lie in another tile
     if (c == 0 && x > 0 && __ldg(in + g - 1) == v) gunite<MAXC>(P, g, g - 1, status);
@@ -211,14 +215,17 @@ border_kernel(const int32_t* __restrict__ in, int W, int H, int* P, int* status)
   }
 }
 
+// Flatten pass, one block per tile (only image pixels are touched, so batch
+// arenas may carry padding between images).
 __global__ void __launch_bounds__(kThreads)
-flatten_kernel(int* P, int64_t n, int32_t* __restrict__ sizes, int* status) {
+flatten_kernel(int* P, Geoms gs, int32_t* __restrict__ sizes, int* status) {
   const unsigned full = 0xffffffffu;
-  for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < n;
-       base += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t g = base + threadIdx.x;
+  const TileRef t = tile_ref(gs, blockIdx.x);
+  for (int q = threadIdx.x; q < TH * TW; q += kThreads) {
+    const int x = t.tx0 + q % TW, y = t.ty0 + q / TW;
     int root = -1;
-    if (g < n) {
+    if (x < t.W && y < t.H) {
+      const long long g = t.off + (long long)y * t.W + x;
       unsigned budget = kUnionCap;
       const int lr = __ldcg(P + g);
       root = gfind(P, lr, budget);
@@ -248,23 +255,29 @@ static Layout carve(void* ws) {
 }
 
 template <bool MAXC, int CONN>
-static int run(const int32_t* in, int W, int H, int32_t* out, int32_t* sizes, WsHeader* hdr,
+static int run(const int32_t* in, const Geoms& gs, int32_t* out, int32_t* sizes, WsHeader* hdr,
                cudaStream_t st) {
-  dim3 grid((W + TW - 1) / TW, (H + TH - 1) / TH);
-  tile_kernel<MAXC, CONN><<<grid, kThreads, 0, st>>>(in, W, H, out, sizes, &hdr->status);
+  tile_kernel<MAXC, CONN><<<gs.total_tiles, kThreads, 0, st>>>(in, gs, out, sizes, &hdr->status);
   SG_TRY(launch_status());
-  border_kernel<MAXC, CONN><<<grid, kThreads, 0, st>>>(in, W, H, out, &hdr->status);
+  border_kernel<MAXC, CONN><<<gs.total_tiles, kThreads, 0, st>>>(in, gs, out, &hdr->status);
   SG_TRY(launch_status());
-  DeviceInfo di;
-  SG_TRY(device_info(&di));
-  const int64_t n = (int64_t)W * H;
-  int64_t blocks = (n + kThreads - 1) / kThreads;
-  if (blocks > (int64_t)di.sm_count * 16) blocks = (int64_t)di.sm_count * 16;
-  flatten_kernel<<<(int)blocks, kThreads, 0, st>>>(out, n, sizes, &hdr->status);
+  flatten_kernel<<<gs.total_tiles, kThreads, 0, st>>>(out, gs, sizes, &hdr->status);
   return launch_status();
 }
 
 }  // namespace ccl
+
+// Labelling over a geometry table (one image or a batch arena).  Labels are
+// arena-global linear indices.
+int ccl_geoms(const int32_t* in, const Geoms& gs, int connectivity, int convention, int32_t* out,
+              int32_t* sizes, WsHeader* hdr, cudaStream_t st) {
+  const bool mx = convention == SPLIT_LABEL_MAX_INDEX;
+  if (connectivity == 4)
+    return mx ? ccl::run<true, 4>(in, gs, out, sizes, hdr, st)
+              : ccl::run<false, 4>(in, gs, out, sizes, hdr, st);
+  return mx ? ccl::run<true, 8>(in, gs, out, sizes, hdr, st)
+            : ccl::run<false, 8>(in, gs, out, sizes, hdr, st);
+}
 
 // ---- label compression ----------------------------------------------------
 namespace cmp {
@@ -415,13 +428,8 @@ extern "C" int split_ccl(const int32_t* labels_in, int width, int height, int co
   if (!workspace || workspace_bytes < l.bytes || (reinterpret_cast<uintptr_t>(workspace) & 255))
     return SPLIT_ERR_WORKSPACE;
   l = ccl::carve(workspace);
-  cudaStream_t st = as_stream(stream);
-  const bool mx = convention == SPLIT_LABEL_MAX_INDEX;
-  if (connectivity == 4)
-    return mx ? ccl::run<true, 4>(labels_in, width, height, labels_out, d_sizes, l.hdr, st)
-              : ccl::run<false, 4>(labels_in, width, height, labels_out, d_sizes, l.hdr, st);
-  return mx ? ccl::run<true, 8>(labels_in, width, height, labels_out, d_sizes, l.hdr, st)
-            : ccl::run<false, 8>(labels_in, width, height, labels_out, d_sizes, l.hdr, st);
+  return ccl_geoms(labels_in, single_geom(width, height), connectivity, convention, labels_out,
+                   d_sizes, l.hdr, as_stream(stream));
 }
 
 extern "C" size_t split_compress_labels_workspace_size(int64_t n) {

@@ -18,6 +18,7 @@
 // have one fixed shape: the update is bit-reproducible.
 #include <limits.h>
 #include <math.h>
+#include <string.h>
 
 #include "common.cuh"
 
@@ -90,7 +91,7 @@ struct Params {
 constexpr int cstride(int dim) { return dim == 3 ? 4 : 8; }
 
 __device__ __forceinline__ const Image& image_of(const Params& p, int i) {
-  return p.nimages == 1 ? p.img0 : p.images[i];
+  return p.images ? p.images[i] : p.img0;
 }
 
 __device__ __forceinline__ int find_image(const Params& p, int unit) {
@@ -1130,3 +1131,119 @@ extern "C" int split_kmeans_cluster_noalloc(const void* points, int layout, int 
                                 st));
   return SPLIT_OK;
 }
+
+// ---------------------------------------------------------------------------
+// Batches: one cooperative launch clusters every image of a batch (per-image
+// K, iteration count and threshold); each image keeps its own tiles, groups,
+// reduction tree and convergence test, so its result does not depend on what
+// else shares the launch.
+// ---------------------------------------------------------------------------
+#include "kmeans_batch.h"
+
+namespace sg {
+
+namespace kmb {
+struct BatchCounts {
+  int units, groups;
+};
+BatchCounts batch_counts(const KmBatchImage* imgs, int n) {
+  BatchCounts c{0, 0};
+  for (int i = 0; i < n; ++i) {
+    const int u = km::units_of(imgs[i].npoints, imgs[i].width);
+    c.units += u;
+    c.groups += km::groups_of(u);
+  }
+  return c;
+}
+}  // namespace kmb
+using kmb::BatchCounts;
+using kmb::batch_counts;
+
+size_t kmeans_batch_workspace(const KmBatchImage* imgs, int nimages) {
+  const BatchCounts c = batch_counts(imgs, nimages);
+  return km::carve(nullptr, c.units, c.groups, nimages > 1 ? nimages : 2).bytes;
+}
+
+int kmeans_batch_prepare(const KmBatchImage* imgs, int nimages, int layout, int dim,
+                         float xy_scale, void* ws, size_t ws_bytes, cudaStream_t st,
+                         KmBatchPlan* plan) {
+  using namespace km;
+  if (!imgs || nimages < 1 || (dim != 3 && dim != 5)) return SPLIT_ERR_INVALID;
+  const int unit_range = (layout & SPLIT_FEATURES_UNIT_RANGE) ? 1 : 0;
+  layout &= ~SPLIT_FEATURES_UNIT_RANGE;
+  const BatchCounts c = batch_counts(imgs, nimages);
+  const int slots = nimages > 1 ? nimages : 2;
+  Layout l = carve(nullptr, c.units, c.groups, slots);
+  if (!ws || ws_bytes < l.bytes || (reinterpret_cast<uintptr_t>(ws) & 255))
+    return SPLIT_ERR_WORKSPACE;
+  l = carve(ws, c.units, c.groups, slots);
+  std::vector<Image> host(nimages);
+  int ub = 0, gb = 0, max_iter = 0;
+  for (int i = 0; i < nimages; ++i) {
+    const KmBatchImage& b = imgs[i];
+    if (!valid_features(b.points, layout, dim, b.npoints, b.width, b.nclusters) || !b.centroids ||
+        !b.labels)
+      return SPLIT_ERR_INVALID;
+    Image& im = host[i];
+    memset(&im, 0, sizeof(im));
+    im.points = b.points;
+    im.unit_range = unit_range;
+    im.npoints = b.npoints;
+    im.width = b.width;
+    im.xy_scale = xy_scale;
+    im.centroids = b.centroids;
+    im.labels = b.labels;
+    im.K = b.nclusters;
+    im.max_iter = b.iters;
+    im.threshold = b.threshold;
+    im.unit_begin = ub;
+    im.nunits = units_of(b.npoints, b.width);
+    im.group_begin = gb;
+    im.ngroups = groups_of(im.nunits);
+    im.height = height_of(b.npoints, b.width);
+    im.ntx = tiles_x(b.width);
+    ub += im.nunits;
+    gb += im.ngroups;
+    max_iter = max_iter > b.iters ? max_iter : b.iters;
+  }
+  SG_CUDA_TRY(cudaMemcpyAsync(l.images, host.data(), sizeof(Image) * nimages,
+                              cudaMemcpyHostToDevice, st));
+  // the host copy must outlive the transfer
+  SG_CUDA_TRY(cudaStreamSynchronize(st));
+  plan->nimages = nimages;
+  plan->units = c.units;
+  plan->groups = c.groups;
+  plan->max_iter = max_iter;
+  plan->layout = layout;
+  plan->dim = dim;
+  return SPLIT_OK;
+}
+
+int kmeans_batch_run(const KmBatchPlan& plan, void* ws, cudaStream_t st) {
+  using namespace km;
+  const int slots = plan.nimages > 1 ? plan.nimages : 2;
+  Layout l = carve(ws, plan.units, plan.groups, slots);
+  Params p{};
+  p.nimages = plan.nimages;
+  p.images = l.images;  // a one-image batch reads its descriptor from the table too
+  p.total_units = plan.units;
+  p.max_iter = plan.max_iter;
+  p.unit_part = l.unit_part;
+  p.group_part = l.group_part;
+  p.cur = l.cur;
+  p.group_cnt = l.group_cnt;
+  p.image_cnt = l.image_cnt;
+  p.state = l.state;
+  p.hdr = l.hdr;
+  SG_CUDA_TRY(cudaMemsetAsync(reinterpret_cast<char*>(l.hdr) + sizeof(int), 0,
+                              sizeof(unsigned) * 4, st));
+  init_kernel<<<1, 256, 0, st>>>(p);
+  SG_TRY(launch_status());
+  if (plan.dim == 3) load_user_centroids<3><<<1, 256, 0, st>>>(p);
+  else load_user_centroids<5><<<1, 256, 0, st>>>(p);
+  SG_TRY(launch_status());
+  if (plan.max_iter <= 0) return SPLIT_OK;
+  return dispatch<kCluster>(plan.layout, plan.dim, p, st);
+}
+
+}  // namespace sg

@@ -17,6 +17,7 @@
 //   best[n]                            zero outside a call
 // Per-call arrays: size[n] (unless the caller passes component sizes),
 // map[n], fin[n] (final target of every small segment), sum[n] (chroma).
+#include "geom.cuh"
 #include "merge_state.cuh"
 
 namespace sg {
@@ -121,18 +122,21 @@ size_kernel(const int32_t* __restrict__ lab, int64_t n, Layout L, bool count_siz
   }
 }
 
-// boundary histogram of small segments
+// boundary histogram of small segments, one block per 32 x 64 tile
 __global__ void __launch_bounds__(kThreads)
-pair_kernel(const int32_t* __restrict__ lab, int W, int H, Layout L, const int32_t* sizes,
-            int P, int* status) {
-  const int64_t n = (int64_t)W * H;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
-       i += (int64_t)gridDim.x * blockDim.x) {
+pair_kernel(const int32_t* __restrict__ lab, Geoms gs, Layout L, const int32_t* sizes, int P,
+            int* status) {
+  const long long n = gs.total_px;
+  const TileRef tr = tile_ref(gs, blockIdx.x);
+  const int W = tr.W, H = tr.H;
+  for (int q = threadIdx.x; q < kTileH * kTileW; q += blockDim.x) {
+    const int x = tr.tx0 + q % kTileW, y = tr.ty0 + q / kTileW;
+    if (x >= W || y >= H) continue;
+    const long long i = tr.off + (long long)y * W + x;
     const int s = __ldg(lab + i);
     if (s < 0 || s >= n) continue;
     if (__ldg(sizes + s) >= P) continue;
     L.fin[s] = s;
-    const int y = (int)(i / W), x = (int)(i - (int64_t)y * W);
     int t[8];
     int nt = 0;
 #pragma unroll
@@ -141,7 +145,7 @@ pair_kernel(const int32_t* __restrict__ lab, int W, int H, Layout L, const int32
       const int dy = d < 3 ? -1 : d > 4 ? 1 : 0;
       const int nx = x + dx, ny = y + dy;
       int v = -1;
-      if (nx >= 0 && ny >= 0 && nx < W && ny < H) v = __ldg(lab + (int64_t)ny * W + nx);
+      if (nx >= 0 && ny >= 0 && nx < W && ny < H) v = __ldg(lab + tr.off + (long long)ny * W + nx);
       if (v >= n) {
         set_status(status, SPLIT_ERR_INVALID);
         v = -1;
@@ -266,6 +270,14 @@ __global__ void set_state_kernel(State* st, const int32_t* sizes, int P, int pol
 
 }  // namespace mrg
 
+int merge_view_n(const void* ws, int64_t n, MergeView* out) {
+  if (!ws || n < 1) return SPLIT_ERR_INVALID;
+  mrg::Layout l = mrg::carve(const_cast<void*>(ws), n);
+  out->state = l.state;
+  out->fin = l.fin;
+  return SPLIT_OK;
+}
+
 int merge_view(const void* ws, int width, int height, MergeView* out) {
   if (!ws || width < 1 || height < 1) return SPLIT_ERR_INVALID;
   mrg::Layout l = mrg::carve(const_cast<void*>(ws), (int64_t)width * height);
@@ -283,14 +295,14 @@ extern "C" size_t split_merge_small_workspace_size(int width, int height) {
   return mrg::carve(nullptr, (int64_t)width * height).bytes;
 }
 
-// Runs the decision passes; the caller's labels are relabelled unless
-// `relabel_labels` is false (the fused erosion relabels instead).
-static int merge_decide(int32_t* labels, int width, int height, int P, int policy,
-                        const float* chroma, const int32_t* d_sizes, void* workspace,
-                        size_t workspace_bytes, cudaStream_t st, bool relabel_labels) {
-  if (!labels || width < 1 || height < 1) return SPLIT_ERR_INVALID;
-  const int64_t n = (int64_t)width * height;
-  if (n > 0x7fffffffLL) return SPLIT_ERR_INVALID;
+// Runs the decision passes over a geometry table (labels are arena-global
+// segment ids); the labels are relabelled unless `relabel_labels` is false
+// (the fused erosion relabels instead).
+static int merge_run(int32_t* labels, const Geoms& gs, int P, int policy, const float* chroma,
+                     const int32_t* d_sizes, void* workspace, size_t workspace_bytes,
+                     cudaStream_t st, bool relabel_labels) {
+  const int64_t n = gs.total_px;
+  if (!labels || n < 1 || n > 0x7fffffffLL) return SPLIT_ERR_INVALID;
   if (policy != SPLIT_MERGE_MOST_BOUNDARY && policy != SPLIT_MERGE_REF_CHROMA)
     return SPLIT_ERR_INVALID;
   if (policy == SPLIT_MERGE_REF_CHROMA && !chroma) return SPLIT_ERR_INVALID;
@@ -314,8 +326,8 @@ static int merge_decide(int32_t* labels, int width, int height, int P, int polic
                                                       ref ? chroma : nullptr, &l.hdr->status);
     SG_TRY(launch_status());
   }
-  mrg::pair_kernel<<<grid, mrg::kThreads, 0, st>>>(labels, width, height, l, sizes, P,
-                                                    &l.hdr->status);
+  mrg::pair_kernel<<<gs.total_tiles, mrg::kThreads, 0, st>>>(labels, gs, l, sizes, P,
+                                                              &l.hdr->status);
   SG_TRY(launch_status());
   mrg::bid_kernel<<<grid, mrg::kThreads, 0, st>>>(l, sizes, policy);
   SG_TRY(launch_status());
@@ -333,6 +345,24 @@ static int merge_decide(int32_t* labels, int width, int height, int P, int polic
   }
   return SPLIT_OK;
 }
+
+static int merge_decide(int32_t* labels, int width, int height, int P, int policy,
+                        const float* chroma, const int32_t* d_sizes, void* workspace,
+                        size_t workspace_bytes, cudaStream_t st, bool relabel_labels) {
+  if (!labels || width < 1 || height < 1) return SPLIT_ERR_INVALID;
+  if ((int64_t)width * height > 0x7fffffffLL) return SPLIT_ERR_INVALID;
+  return merge_run(labels, single_geom(width, height), P, policy, chroma, d_sizes, workspace,
+                   workspace_bytes, st, relabel_labels);
+}
+
+namespace sg {
+int merge_geoms(const int32_t* labels, const Geoms& gs, int P, int policy, const int32_t* d_sizes,
+                void* workspace, size_t workspace_bytes, cudaStream_t st) {
+  return merge_run(const_cast<int32_t*>(labels), gs, P, policy, nullptr, d_sizes, workspace,
+                   workspace_bytes, st, false);
+}
+size_t merge_workspace_bytes(int64_t n) { return mrg::carve(nullptr, n).bytes; }
+}  // namespace sg
 
 extern "C" int split_merge_small(int32_t* labels, int width, int height, int P, int policy,
                                  const float* chroma, const int32_t* d_sizes, void* workspace,

@@ -36,6 +36,12 @@ struct MergeView {
   const int32_t* fin;
 };
 int merge_view(const void* ws, int width, int height, MergeView* out);
+int merge_view_n(const void* ws, int64_t n, MergeView* out);
+struct Geoms;
+// Merge decision over a geometry table (relabel left to the fused erosion).
+int merge_geoms(const int32_t* labels, const Geoms& gs, int P, int policy, const int32_t* d_sizes,
+                void* workspace, size_t workspace_bytes, cudaStream_t st);
+size_t merge_workspace_bytes(int64_t n);
 int merge_decide_only(const int32_t* labels, int width, int height, int P, int policy,
                       const float* chroma, const int32_t* d_sizes, void* workspace,
                       size_t workspace_bytes, cudaStream_t st);

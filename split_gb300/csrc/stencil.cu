@@ -8,6 +8,7 @@
 //   - RGB8 feature packing (float4 features, luminance).
 #include <math.h>
 
+#include "geom.cuh"
 #include "merge_state.cuh"
 #include "tma.cuh"
 
@@ -47,7 +48,7 @@ int make_tmap_2d(CUtensorMap* map, CUtensorMapDataType dtype, int elem_bytes, co
 
 namespace stn {
 
-constexpr int TH = 32, TW = 64, kThreads = 256;
+constexpr int TH = kTileH, TW = kTileW, kThreads = 256;
 constexpr unsigned kWaitLimit = 1u << 24;
 
 // Stage a box of `sw` x `sh` elements starting at (x0, y0) into `dst`: TMA
@@ -80,42 +81,55 @@ __device__ __forceinline__ bool stage(T* dst, const CUtensorMap* map, const T* s
 
 // ---- erosion ---------------------------------------------------------------
 struct ErodeArgs {
-  const int32_t* in;
-  int32_t* out;
-  int W, H, R, XP;
+  const int32_t* in;    // arena
+  int32_t* out;         // arena
+  int R, XP;
   const mrg::State* mstate;  // fused relabel when not null
   const int32_t* mfin;
+  int local_labels;     // write labels minus the image's arena offset
   int* status;
 };
 
+// TMA bits of ImgGeom::tma_ok
+constexpr int kTmaLabels = 1, kTmaRgb = 2;
+
+__device__ __forceinline__ const CUtensorMap* pick_map(const Geoms& gs, const TileRef& t,
+                                                       const CUtensorMap* single, int bit) {
+  if (gs.n == 1) return single;
+  return (gs.maps && (t.tma_ok & bit)) ? gs.maps + t.img : nullptr;
+}
+
 template <bool R1>
 __global__ void __launch_bounds__(kThreads)
-erode_kernel(const __grid_constant__ CUtensorMap tmap, bool use_tma, ErodeArgs a) {
+erode_kernel(const __grid_constant__ CUtensorMap tmap, bool use_tma, ErodeArgs a, Geoms gs) {
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ __align__(8) uint64_t bar;
   const int R = R1 ? 1 : a.R, XP = R1 ? 4 : a.XP;
   const int SW = TW + 2 * XP, SH = TH + 2 * R;
   int32_t* lab = reinterpret_cast<int32_t*>(smem);
-  const int tx0 = blockIdx.x * TW, ty0 = blockIdx.y * TH;
-  if (!stage<int32_t>(lab, use_tma ? &tmap : nullptr, a.in, a.W, a.H, tx0 - XP, ty0 - R, SW, SH,
-                      &bar, a.status))
+  const TileRef t = tile_ref(gs, blockIdx.x);
+  const int W = t.W, H = t.H, tx0 = t.tx0, ty0 = t.ty0;
+  const CUtensorMap* map = pick_map(gs, t, use_tma ? &tmap : nullptr, kTmaLabels);
+  if (!stage<int32_t>(lab, map, a.in + t.off, W, H, tx0 - XP, ty0 - R, SW, SH, &bar, a.status))
     return;
   if (a.mstate) {
     const mrg::State ms = *a.mstate;
     for (int i = threadIdx.x; i < SW * SH; i += blockDim.x) lab[i] = mrg::relabel(ms, a.mfin, lab[i]);
     __syncthreads();
   }
+  const int base = a.local_labels ? (int)t.off : 0;
+  int32_t* out = a.out + t.off;
   if (R1) {
     for (int i = threadIdx.x; i < TH * TW; i += blockDim.x) {
       const int r = i / TW, c = i % TW;
       const int x = tx0 + c, y = ty0 + r;
-      if (x >= a.W || y >= a.H) continue;
+      if (x >= W || y >= H) continue;
       const int* p = lab + (r + 1) * SW + (c + XP);
       const int v = p[0];
-      bool keep = x >= 1 && y >= 1 && x + 1 < a.W && y + 1 < a.H;
+      bool keep = x >= 1 && y >= 1 && x + 1 < W && y + 1 < H;
       keep = keep && p[-SW - 1] == v && p[-SW] == v && p[-SW + 1] == v && p[-1] == v &&
              p[1] == v && p[SW - 1] == v && p[SW] == v && p[SW + 1] == v;
-      a.out[(size_t)y * a.W + x] = keep ? v : -1;
+      out[(size_t)y * W + x] = keep ? v - base : -1;
     }
     return;
   }
@@ -134,38 +148,47 @@ erode_kernel(const __grid_constant__ CUtensorMap tmap, bool use_tma, ErodeArgs a
   for (int i = threadIdx.x; i < TH * TW; i += blockDim.x) {
     const int r = i / TW, c = i % TW;
     const int x = tx0 + c, y = ty0 + r;
-    if (x >= a.W || y >= a.H) continue;
+    if (x >= W || y >= H) continue;
     const int* p = lab + (r + R) * SW + (c + XP);
     const unsigned char* f = vert + r * SW + (c + XP);
     const int v = p[0];
-    bool keep = x >= R && y >= R && x + R < a.W && y + R < a.H;
+    bool keep = x >= R && y >= R && x + R < W && y + R < H;
     for (int dx = -R; dx <= R && keep; ++dx) keep = p[dx] == v && f[dx];
-    a.out[(size_t)y * a.W + x] = keep ? v : -1;
+    out[(size_t)y * W + x] = keep ? v - base : -1;
   }
 }
 
-static int erode_launch(const int32_t* in, int32_t* out, int W, int H, int R,
-                        const mrg::State* ms, const int32_t* mfin, int* status, cudaStream_t st) {
-  const int XP = (R + 3) / 4 * 4;
+inline int erode_halo(int R) { return (R + 3) / 4 * 4; }
+
+static int erode_geoms_launch(const int32_t* in, int32_t* out, const Geoms& gs, int R,
+                              const mrg::State* ms, const int32_t* mfin, int local_labels,
+                              int* status, cudaStream_t st) {
+  const int XP = erode_halo(R);
   const int SW = TW + 2 * XP, SH = TH + 2 * R;
   CUtensorMap map;
   memset(&map, 0, sizeof(map));
-  const bool use_tma = make_tmap_2d(&map, CU_TENSOR_MAP_DATA_TYPE_INT32, 4, in, (uint64_t)W,
-                                    (uint64_t)H, (uint64_t)W * 4, (uint32_t)SW,
-                                    (uint32_t)SH) == SPLIT_OK;
-  ErodeArgs a{in, out, W, H, R, XP, ms, mfin, status};
-  dim3 grid((W + TW - 1) / TW, (H + TH - 1) / TH);
+  bool use_tma = false;
+  if (gs.n == 1)
+    use_tma = make_tmap_2d(&map, CU_TENSOR_MAP_DATA_TYPE_INT32, 4, in, (uint64_t)gs.one.W,
+                           (uint64_t)gs.one.H, (uint64_t)gs.one.W * 4, (uint32_t)SW,
+                           (uint32_t)SH) == SPLIT_OK;
+  ErodeArgs a{in, out, R, XP, ms, mfin, local_labels, status};
   size_t smem = (size_t)SW * SH * sizeof(int32_t);
   if (R == 1) {
-    erode_kernel<true><<<grid, kThreads, smem, st>>>(map, use_tma, a);
+    erode_kernel<true><<<gs.total_tiles, kThreads, smem, st>>>(map, use_tma, a, gs);
   } else {
     smem += (size_t)TH * SW;
     if (smem > 48 * 1024)
       SG_CUDA_TRY(cudaFuncSetAttribute(erode_kernel<false>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    erode_kernel<false><<<grid, kThreads, smem, st>>>(map, use_tma, a);
+    erode_kernel<false><<<gs.total_tiles, kThreads, smem, st>>>(map, use_tma, a, gs);
   }
   return launch_status();
+}
+
+static int erode_launch(const int32_t* in, int32_t* out, int W, int H, int R,
+                        const mrg::State* ms, const int32_t* mfin, int* status, cudaStream_t st) {
+  return erode_geoms_launch(in, out, single_geom(W, H), R, ms, mfin, 0, status, st);
 }
 
 // ---- luminance ----------------------------------------------------------------
@@ -221,41 +244,43 @@ __device__ __forceinline__ void sobel_tile(const float* h, int hp, int tx0, int 
 }
 
 struct NormArgs {
-  const float* heights;
-  const uint8_t* rgb;
-  float* out;
-  int W, H;
+  const float* heights;  // arena
+  const uint8_t* rgb;    // arena (3 bytes per pixel)
+  float* out;            // per image: 3 planes at 3 * (arena offset)
   float zinv;
   int* status;
 };
 
 // heights (float) -> normals; staged box (TW + 8) x (TH + 2) from (tx0-4, ty0-1)
 __global__ void __launch_bounds__(kThreads)
-normals_kernel(const __grid_constant__ CUtensorMap tmap, bool use_tma, NormArgs a) {
+normals_kernel(const __grid_constant__ CUtensorMap tmap, bool use_tma, NormArgs a, Geoms gs) {
   __shared__ __align__(128) float tile[(TH + 2) * (TW + 8)];
   __shared__ __align__(8) uint64_t bar;
-  const int tx0 = blockIdx.x * TW, ty0 = blockIdx.y * TH;
+  const TileRef t = tile_ref(gs, blockIdx.x);
   constexpr int SW = TW + 8, SH = TH + 2;
-  if (!stage<float>(tile, use_tma ? &tmap : nullptr, a.heights, a.W, a.H, tx0 - 4, ty0 - 1, SW,
-                    SH, &bar, a.status))
+  const CUtensorMap* map = pick_map(gs, t, use_tma ? &tmap : nullptr, kTmaLabels);
+  if (!stage<float>(tile, map, a.heights + t.off, t.W, t.H, t.tx0 - 4, t.ty0 - 1, SW, SH, &bar,
+                    a.status))
     return;
   // shift the view so that column index 0 is x = tx0 - 1
-  sobel_tile(tile + 3, SW, tx0, ty0, a.W, a.H, a.zinv, a.out);
+  sobel_tile(tile + 3, SW, t.tx0, t.ty0, t.W, t.H, a.zinv, a.out + 3 * t.off);
 }
 
 // RGB8 -> luminance tile -> normals; staged bytes (3 TW + 32) x (TH + 2)
 // from byte column 3 tx0 - 16.
 __global__ void __launch_bounds__(kThreads)
-normals_rgb8_kernel(const __grid_constant__ CUtensorMap tmap, bool use_tma, NormArgs a) {
+normals_rgb8_kernel(const __grid_constant__ CUtensorMap tmap, bool use_tma, NormArgs a,
+                    Geoms gs) {
   constexpr int SWB = 3 * TW + 32, SH = TH + 2, HP = TW + 2;
   __shared__ __align__(128) unsigned char bytes[SWB * SH];
   __shared__ float lum[SH * HP];
   __shared__ float lin[256];
   __shared__ __align__(8) uint64_t bar;
-  const int tx0 = blockIdx.x * TW, ty0 = blockIdx.y * TH;
+  const TileRef t = tile_ref(gs, blockIdx.x);
   for (int i = threadIdx.x; i < 256; i += blockDim.x) lin[i] = lin100(i);
-  if (!stage<unsigned char>(bytes, use_tma ? &tmap : nullptr, a.rgb, 3 * a.W, a.H, 3 * tx0 - 16,
-                            ty0 - 1, SWB, SH, &bar, a.status))
+  const CUtensorMap* map = pick_map(gs, t, use_tma ? &tmap : nullptr, kTmaRgb);
+  if (!stage<unsigned char>(bytes, map, a.rgb + 3 * t.off, 3 * t.W, t.H, 3 * t.tx0 - 16,
+                            t.ty0 - 1, SWB, SH, &bar, a.status))
     return;
   for (int i = threadIdx.x; i < SH * HP; i += blockDim.x) {
     const int r = i / HP, c = i % HP;  // pixel x = tx0 - 1 + c
@@ -263,7 +288,7 @@ normals_rgb8_kernel(const __grid_constant__ CUtensorMap tmap, bool use_tma, Norm
     lum[i] = lum_from_lin(lin[p[0]], lin[p[1]], lin[p[2]]);
   }
   __syncthreads();
-  sobel_tile(lum, HP, tx0, ty0, a.W, a.H, a.zinv, a.out);
+  sobel_tile(lum, HP, t.tx0, t.ty0, t.W, t.H, a.zinv, a.out + 3 * t.off);
 }
 
 // ---- feature packing ------------------------------------------------------------
@@ -328,26 +353,59 @@ extern "C" int split_sobel_normals(const float* heights, int width, int height, 
   const bool use_tma =
       make_tmap_2d(&map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, heights, (uint64_t)width,
                    (uint64_t)height, (uint64_t)width * 4, stn::TW + 8, stn::TH + 2) == SPLIT_OK;
-  stn::NormArgs a{heights, nullptr, normals, width, height, 1.0f / fmaxf(0.001f, depth), nullptr};
-  dim3 grid((width + stn::TW - 1) / stn::TW, (height + stn::TH - 1) / stn::TH);
-  stn::normals_kernel<<<grid, stn::kThreads, 0, as_stream(stream)>>>(map, use_tma, a);
+  stn::NormArgs a{heights, nullptr, normals, 1.0f / fmaxf(0.001f, depth), nullptr};
+  const Geoms gs = single_geom(width, height);
+  stn::normals_kernel<<<gs.total_tiles, stn::kThreads, 0, as_stream(stream)>>>(map, use_tma, a,
+                                                                                gs);
   return launch_status();
 }
+
+namespace sg {
+int normals_rgb8_geoms(const uint8_t* rgb, const Geoms& gs, float depth, float* normals,
+                       cudaStream_t st) {
+  CUtensorMap map;
+  memset(&map, 0, sizeof(map));
+  bool use_tma = false;
+  if (gs.n == 1)
+    use_tma = make_tmap_2d(&map, CU_TENSOR_MAP_DATA_TYPE_UINT8, 1, rgb, (uint64_t)gs.one.W * 3,
+                           (uint64_t)gs.one.H, (uint64_t)gs.one.W * 3, 3 * stn::TW + 32,
+                           stn::TH + 2) == SPLIT_OK;
+  stn::NormArgs a{nullptr, rgb, normals, 1.0f / fmaxf(0.001f, depth), nullptr};
+  stn::normals_rgb8_kernel<<<gs.total_tiles, stn::kThreads, 0, st>>>(map, use_tma, a, gs);
+  return launch_status();
+}
+
+int erode_geoms(const int32_t* in, int32_t* out, const Geoms& gs, int radius, const void* mstate,
+                const int32_t* mfin, int local_labels, cudaStream_t st) {
+  return stn::erode_geoms_launch(in, out, gs, radius, static_cast<const mrg::State*>(mstate),
+                                 mfin, local_labels, nullptr, st);
+}
+
+// Tensor maps of one batch image for the batch stencils (labels for the
+// erosion, RGB8 bytes for the normals).  Returns the TMA bits that apply.
+int batch_image_maps(const int32_t* labels, const uint8_t* rgb, int W, int H, int radius,
+                     CUtensorMap* lab_map, CUtensorMap* rgb_map) {
+  int bits = 0;
+  const int XP = stn::erode_halo(radius);
+  memset(lab_map, 0, sizeof(CUtensorMap));
+  memset(rgb_map, 0, sizeof(CUtensorMap));
+  if (labels && make_tmap_2d(lab_map, CU_TENSOR_MAP_DATA_TYPE_INT32, 4, labels, (uint64_t)W,
+                             (uint64_t)H, (uint64_t)W * 4, (uint32_t)(stn::TW + 2 * XP),
+                             (uint32_t)(stn::TH + 2 * radius)) == SPLIT_OK)
+    bits |= stn::kTmaLabels;
+  if (rgb && make_tmap_2d(rgb_map, CU_TENSOR_MAP_DATA_TYPE_UINT8, 1, rgb, (uint64_t)W * 3,
+                          (uint64_t)H, (uint64_t)W * 3, 3 * stn::TW + 32,
+                          stn::TH + 2) == SPLIT_OK)
+    bits |= stn::kTmaRgb;
+  return bits;
+}
+}  // namespace sg
 
 extern "C" int split_sobel_normals_rgb8(const uint8_t* rgb, int width, int height, float depth,
                                         float* normals, void* stream) {
   if (!rgb || !normals || width < 1 || height < 1) return SPLIT_ERR_INVALID;
   if ((int64_t)width * height * 3 > 0x7fffffffLL) return SPLIT_ERR_INVALID;
-  CUtensorMap map;
-  memset(&map, 0, sizeof(map));
-  const bool use_tma =
-      make_tmap_2d(&map, CU_TENSOR_MAP_DATA_TYPE_UINT8, 1, rgb, (uint64_t)width * 3,
-                   (uint64_t)height, (uint64_t)width * 3, 3 * stn::TW + 32,
-                   stn::TH + 2) == SPLIT_OK;
-  stn::NormArgs a{nullptr, rgb, normals, width, height, 1.0f / fmaxf(0.001f, depth), nullptr};
-  dim3 grid((width + stn::TW - 1) / stn::TW, (height + stn::TH - 1) / stn::TH);
-  stn::normals_rgb8_kernel<<<grid, stn::kThreads, 0, as_stream(stream)>>>(map, use_tma, a);
-  return launch_status();
+  return normals_rgb8_geoms(rgb, single_geom(width, height), depth, normals, as_stream(stream));
 }
 
 extern "C" int split_pack_rgb8(const uint8_t* rgb, int64_t npixels, float* features4,

@@ -1,0 +1,77 @@
+"""Batches: every image's results equal the single-image pipeline's, eagerly
+and replayed from a captured CUDA graph; the merge, labelling and erosion
+results also equal the oracle's."""
+import numpy as np
+import pytest
+
+import oracle
+from split_gb300 import synth
+
+pytestmark = pytest.mark.gpu
+
+SHAPES = [(128, 96, 4, 6), (333, 201, 8, 5), (256, 256, 16, 8), (97, 311, 32, 4),
+          (640, 128, 8, 10), (64, 64, 4, 3), (1000, 37, 16, 6), (513, 257, 32, 7),
+          (1, 700, 4, 2), (720, 1, 8, 3)]
+
+
+def _images(shapes, dim):
+    imgs, cents = [], []
+    for i, (w, h, k, _) in enumerate(shapes):
+        rgb = synth.voronoi_rgb8(100 + i, w, h, max(4, (w * h) // 4000), npalette=8,
+                                 illum_gradient=True, sigma=4.0)
+        imgs.append(rgb)
+        cents.append(synth.pick_centroids(100 + i, rgb, k, dim))
+    return imgs, cents
+
+
+def _single(torch, rgb, c0, k, iters, params, dev):
+    from split_gb300 import pipeline
+    p = pipeline.Params(**{**params.__dict__, "nclusters": k, "kmeans_iters": iters})
+    h, w = rgb.shape[:2]
+    pipe = pipeline.Pipeline(w, h, p, dev)
+    pipe.run(torch.from_numpy(rgb).to(dev), torch.from_numpy(c0).to(dev))
+    torch.cuda.synchronize()
+    return (pipe.cluster_labels.cpu().numpy(), pipe.centroids.cpu().numpy(),
+            pipe.segment_labels.cpu().numpy(), pipe.normals.cpu().numpy())
+
+
+@pytest.mark.parametrize("features", [1, 2])
+def test_batch_equals_single_images(cuda, features):
+    import torch
+    from split_gb300 import batch, pipeline
+    params = pipeline.Params(features=features, merge_P=64)
+    imgs, cents = _images(SHAPES, params.dim)
+    b = batch.Batch(SHAPES, params, cuda)
+    b.load(imgs, cents)
+    b.run()
+    torch.cuda.synchronize()
+    for i, (w, h, k, iters) in enumerate(SHAPES):
+        cl, ce, sl, nr = _single(torch, imgs[i], cents[i], k, iters, params, cuda)
+        assert np.array_equal(b.cluster_labels_of(i).cpu().numpy(), cl), f"image {i} labels"
+        assert np.array_equal(b.centroids_of(i).cpu().numpy(), ce), f"image {i} centroids"
+        assert np.array_equal(b.segment_labels_of(i).cpu().numpy(), sl), f"image {i} segments"
+        assert np.array_equal(b.normals_of(i).cpu().numpy(), nr), f"image {i} normals"
+        # integer stages against the oracle, given the device's cluster labels
+        seg = oracle.ccl(cl.reshape(h, w), 8, 0)
+        seg = oracle.merge_small(seg, 64, 0)
+        assert np.array_equal(sl, oracle.erode(seg, 1)), f"image {i} oracle"
+
+
+def test_batch_graph_replay(cuda):
+    import torch
+    from split_gb300 import batch, pipeline
+    params = pipeline.Params(merge_P=64)
+    imgs, cents = _images(SHAPES[:6], params.dim)
+    b = batch.Batch(SHAPES[:6], params, cuda)
+    b.load(imgs, cents)
+    b.run()
+    torch.cuda.synchronize()
+    ref_seg = b.segment_labels.clone()
+    ref_cen = b.centroids.clone()
+    b.capture()
+    for _ in range(3):
+        b.load(imgs, cents)       # the run updates the centroids in place
+        b.replay()
+        torch.cuda.synchronize()
+        assert torch.equal(b.segment_labels, ref_seg)
+        assert torch.equal(b.centroids, ref_cen)
