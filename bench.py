@@ -231,6 +231,102 @@ def run_reference(args, rank):
     print(json.dumps(line), flush=True)
 
 
+# ------------------------------------------------------------------ batches
+def batch_shapes(n, seed):
+    """Batching configuration: sides uniform in [128, 2048] per axis, K from
+    {4, 8, 16, 32}, 10..20 k-means iterations, per-image seeds."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    return [(int(rng.integers(128, 2049)), int(rng.integers(128, 2049)),
+             int(rng.choice([4, 8, 16, 32])), int(rng.integers(10, 21))) for _ in range(n)]
+
+
+def batch_images(shapes, seed):
+    from split_gb300 import synth
+    imgs, cents = [], []
+    for i, (w, h, k, _) in enumerate(shapes):
+        rgb = synth.voronoi_rgb8(seed + i, w, h, 32, sigma=4.0)
+        imgs.append(rgb)
+        cents.append(synth.pick_centroids(seed + i, rgb, k, 5, 0.1))
+    return imgs, cents
+
+
+def run_batched(dev, nimages, steps, seed=SEED + 1000):
+    """The batch as one graph-replayed launch sequence vs a loop of plain
+    per-image pipeline calls (same images, device-resident)."""
+    import torch
+    from split_gb300 import batch, pipeline
+    shapes = batch_shapes(nimages, seed)
+    imgs, cents = batch_images(shapes, seed)
+    total_px = sum(w * h for w, h, _, _ in shapes)
+    params = pipeline.Params()
+    b = batch.Batch(shapes, params, dev)
+    b.load(imgs, cents)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    c0_all = b.centroids.clone()
+    b.capture()
+    torch.cuda.synchronize()
+    launches0 = pipeline.launch_count()
+    t_batch = []
+    for s in range(steps + 1):
+        b.centroids.copy_(c0_all)
+        flush.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        b.replay()
+        e1.record()
+        torch.cuda.synchronize()
+        if s:
+            t_batch.append(e0.elapsed_time(e1))
+    # plain per-image launch sequence (one pipeline workspace sized for the
+    # largest image, reused)
+    maxw = max(s[0] for s in shapes)
+    maxh = max(s[1] for s in shapes)
+    pipe = pipeline.Pipeline(maxw, maxh, params, dev)
+    import ctypes as C
+    from split_gb300 import _native as N
+    from split_gb300._util import ptr, stream_handle
+    lib = N.load()
+    views = [(b.rgb_of(i), b.centroids_of(i).clone()) for i in range(nimages)]
+    outs = [(torch.empty(w * h, dtype=torch.int32, device=dev),
+             torch.empty(w * h, dtype=torch.int32, device=dev),
+             torch.empty(3 * w * h, dtype=torch.float32, device=dev)) for w, h, _, _ in shapes]
+    cps = [pipeline.Params(**{**params.__dict__, "nclusters": k, "kmeans_iters": it}).c()
+           for _, _, k, it in shapes]
+    cents = [v[1].clone() for v in views]
+
+    def plain_once():
+        st = stream_handle()
+        for i, (w, h, k, it) in enumerate(shapes):
+            cents[i].copy_(views[i][1])
+            N.check(lib.split_pipeline_run(ptr(views[i][0]), w, h, C.byref(cps[i]), ptr(cents[i]),
+                                           ptr(outs[i][0]), ptr(outs[i][1]), ptr(outs[i][2]),
+                                           pipe.ws.ptr, pipe.ws.nbytes, None, st), "plain")
+    plain_once()
+    t_plain = []
+    for s in range(max(2, steps // 2) + 1):
+        flush.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        plain_once()
+        e1.record()
+        torch.cuda.synchronize()
+        if s:
+            t_plain.append(e0.elapsed_time(e1))
+    # identical labels: the batch equals the per-image runs
+    same = all(torch.equal(b.segment_labels_of(i).view(-1), outs[i][1])
+               for i in range(nimages))
+    tb, tp = statistics.median(t_batch), statistics.median(t_plain)
+    return {"workload": f"{nimages} images, sides U[128,2048] per axis, K in {{4,8,16,32}}, "
+                        f"10-20 k-means iterations, 5-D features, 8-CCL, merge<256, erosion, "
+                        f"normals ({total_px / 1e6:.1f} Mpix)",
+            "batched_mpix_s": round(total_px / (tb * 1e-3) / 1e6, 1),
+            "plain_mpix_s": round(total_px / (tp * 1e-3) / 1e6, 1),
+            "batched_ms": round(tb, 3), "plain_ms": round(tp, 3),
+            "speedup": round(tp / tb, 2), "identical_labels": bool(same),
+            "batched_launches_per_run": None}
+
+
 # ------------------------------------------------------------------------ GPU
 def main():
     ap = argparse.ArgumentParser()
@@ -243,6 +339,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--ref-side", type=int, default=512)
     ap.add_argument("--cpu-side", type=int, default=512)
+    ap.add_argument("--batch-images", type=int, default=256)
+    ap.add_argument("--no-batch", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -354,6 +452,10 @@ def main():
                 "kernel": "kmeans_kernel (cooperative, 20 iterations)",
                 "algorithmic_bytes_per_launch": km_bytes, "peak_source": peak_kind}
 
+    batched = None
+    if not args.no_batch and args.batch_images > 0:
+        batched = run_batched(dev, args.batch_images, steps=5)
+
     if rank == 0:
         cpu = None
         if not args.no_cpu_baseline:
@@ -377,6 +479,7 @@ def main():
             "cpu_baseline": cpu,
             "clocks": clocks,
             "stages_ms": {k: round(v, 4) for k, v in stage_ms.items()},
+            "batched": batched,
             "wall_s_timed_region": round(t_wall, 3),
         }
         print(json.dumps(line), flush=True)
