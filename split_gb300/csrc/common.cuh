@@ -60,7 +60,10 @@ struct WsHeader {
   unsigned barrier_count;
   unsigned barrier_gen;
   unsigned work_counter[2];
-  int pad[59];
+  int pad0;
+  // layout the workspace's persistent state was last cleared for (0: never)
+  unsigned long long stamp;
+  int pad[56];
 };
 static_assert(sizeof(WsHeader) == 256, "header is one 256-byte line");
 

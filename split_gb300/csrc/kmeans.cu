@@ -940,9 +940,13 @@ static int run(int mode, const void* points, int layout, int dim, int64_t n,
   p.image_cnt = l.image_cnt;
   p.state = l.state;
   p.hdr = l.hdr;
-  // header words used by the barrier and the work counters start at zero
+  // header words used by the barrier and the work counters start at zero,
+  // and so do the arrival counters (a workspace last used for another image
+  // size holds other data where they now sit)
   SG_CUDA_TRY(cudaMemsetAsync(reinterpret_cast<char*>(l.hdr) + sizeof(int), 0,
                               sizeof(unsigned) * 4, st));
+  SG_CUDA_TRY(cudaMemsetAsync(l.group_cnt, 0, sizeof(unsigned) * (size_t)groups, st));
+  SG_CUDA_TRY(cudaMemsetAsync(l.image_cnt, 0, sizeof(unsigned), st));
   (void)centroids_in;
   init_kernel<<<1, 256, 0, st>>>(p);
   SG_TRY(launch_status());
@@ -1237,6 +1241,8 @@ int kmeans_batch_run(const KmBatchPlan& plan, void* ws, cudaStream_t st) {
   p.hdr = l.hdr;
   SG_CUDA_TRY(cudaMemsetAsync(reinterpret_cast<char*>(l.hdr) + sizeof(int), 0,
                               sizeof(unsigned) * 4, st));
+  SG_CUDA_TRY(cudaMemsetAsync(l.group_cnt, 0, sizeof(unsigned) * (size_t)plan.groups, st));
+  SG_CUDA_TRY(cudaMemsetAsync(l.image_cnt, 0, sizeof(unsigned) * (size_t)plan.nimages, st));
   init_kernel<<<1, 256, 0, st>>>(p);
   SG_TRY(launch_status());
   if (plan.dim == 3) load_user_centroids<3><<<1, 256, 0, st>>>(p);

@@ -203,7 +203,14 @@ __global__ void decide_kernel(Layout L, int policy) {
 __device__ __forceinline__ int next_of(const Layout& L, const int32_t* sizes, int P, int r) {
   if (__ldg(sizes + r) >= P) return r;
   if (*(volatile unsigned long long*)(L.best + r) == 0ull) return r;
-  return *(volatile int*)(L.map + r);
+  const int nx = *(volatile int*)(L.map + r);
+  // map entries come from winning pairs, so they are segment ids; anything
+  // else is a corrupted workspace: stop the chain here
+  if (nx < 0 || nx >= L.state->n) {
+    set_status(&L.hdr->status, SPLIT_ERR_INVALID);
+    return r;
+  }
+  return nx;
 }
 
 // mutual pairs: the larger id keeps itself (fix_map_cycles.cuh:28-43)
@@ -256,6 +263,23 @@ __global__ void relabel_kernel(int32_t* lab, int64_t n, const State* stp, const 
        i += (int64_t)gridDim.x * blockDim.x)
     lab[i] = relabel(st, fin, lab[i]);
 }
+
+// Clears the state that every call leaves at zero (hash table, bids) when the
+// workspace was last used with another layout (or never): reusing one
+// workspace for images of different sizes moves these regions.
+__global__ void guard_kernel(const WsHeader* h, unsigned long long stamp, Layout L, long long n) {
+  if (*(volatile const unsigned long long*)&h->stamp == stamp) return;
+  const long long cap = 1ll << L.cap_log2;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < cap; i += stride) {
+    L.keys[i] = 0ull;
+    L.counts[i] = 0u;
+  }
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += stride)
+    L.best[i] = 0ull;
+}
+
+__global__ void stamp_kernel(WsHeader* h, unsigned long long stamp) { h->stamp = stamp; }
 
 __global__ void set_state_kernel(State* st, const int32_t* sizes, int P, int policy, int cap_log2,
                                  int n) {
@@ -317,6 +341,11 @@ static int merge_run(int32_t* labels, const Geoms& gs, int P, int policy, const 
   const int grid = (int)blocks;
   const int32_t* sizes = d_sizes ? d_sizes : l.size;
   const bool ref = policy == SPLIT_MERGE_REF_CHROMA;
+  const unsigned long long stamp = ((unsigned long long)l.cap_log2 << 40) | (unsigned long long)n;
+  mrg::guard_kernel<<<grid, mrg::kThreads, 0, st>>>(l.hdr, stamp, l, n);
+  SG_TRY(launch_status());
+  mrg::stamp_kernel<<<1, 1, 0, st>>>(l.hdr, stamp);
+  SG_TRY(launch_status());
   mrg::set_state_kernel<<<1, 1, 0, st>>>(l.state, sizes, P, policy, l.cap_log2, (int)n);
   SG_TRY(launch_status());
   if (!d_sizes) SG_CUDA_TRY(cudaMemsetAsync(l.size, 0, sizeof(int32_t) * (size_t)n, st));

@@ -195,3 +195,44 @@ def test_kmeans_unit_range_flag(cuda):
         out.append((lab.cpu().numpy(), cent.cpu().numpy()))
     for lab, cent in out[1:]:
         assert np.array_equal(lab, out[0][0]) and np.array_equal(cent, out[0][1])
+
+
+def test_workspace_reuse_across_sizes(cuda):
+    """One workspace serving images of different sizes in turn (its internal
+    layout moves with the size): merge and whole-pipeline results stay exact."""
+    import torch
+    from split_gb300 import ccl, pipeline
+    from split_gb300._util import Workspace
+    rng = np.random.default_rng(77)
+    ws = Workspace(ccl.merge_small_segments_workspace(700, 500), cuda)
+    for (w, h) in [(700, 500), (123, 77), (640, 480), (31, 900), (700, 500)]:
+        lab = rng.integers(0, 4, size=(h // 3 + 1, w // 3 + 1)).repeat(3, 0).repeat(3, 1)
+        lab = np.ascontiguousarray(lab[:h, :w]).astype(np.int32)
+        lab[rng.random(lab.shape) < 0.03] = 9
+        seg = oracle.ccl(lab, 8, 0)
+        g = _t(seg, cuda)
+        ccl.merge_small_segments(None, g, ws, 20, policy=ccl.MOST_BOUNDARY)
+        assert np.array_equal(g.cpu().numpy(), oracle.merge_small(seg, 20, 0)), (w, h)
+        ws.check("merge")
+    params = pipeline.Params(merge_P=64)
+    big = pipeline.Pipeline(512, 384, params, cuda)
+    import ctypes as C
+    from split_gb300 import _native as N
+    from split_gb300._util import ptr, stream_handle
+    for i, (w, h) in enumerate([(512, 384), (200, 100), (333, 250), (512, 384)]):
+        rgb = synth.voronoi_rgb8(300 + i, w, h, 24, sigma=4.0)
+        c0 = synth.pick_centroids(300 + i, rgb, 16, 5)
+        alone = pipeline.Pipeline(w, h, params, cuda)
+        alone.run(_t(rgb, cuda), _t(c0, cuda))
+        cent = _t(c0, cuda)
+        out = [torch.empty(w * h, dtype=torch.int32, device=cuda) for _ in range(2)]
+        nrm = torch.empty(3 * w * h, dtype=torch.float32, device=cuda)
+        cp = params.c()
+        st = N.load().split_pipeline_run(ptr(_t(rgb, cuda)), w, h, C.byref(cp), ptr(cent),
+                                         ptr(out[0]), ptr(out[1]), ptr(nrm), big.ws.ptr,
+                                         big.ws.nbytes, None, stream_handle())
+        assert st == 0
+        torch.cuda.synchronize()
+        assert torch.equal(out[1].view(h, w), alone.segment_labels), (w, h)
+        assert torch.equal(cent, alone.centroids), (w, h)
+        big.ws.check("pipeline")
