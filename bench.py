@@ -264,9 +264,12 @@ def run_batched(dev, nimages, steps, seed=SEED + 1000):
     b.load(imgs, cents)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
     c0_all = b.centroids.clone()
+    l0 = pipeline.launch_count()
+    b.run()
+    torch.cuda.synchronize()
+    batch_launches = pipeline.launch_count() - l0
     b.capture()
     torch.cuda.synchronize()
-    launches0 = pipeline.launch_count()
     t_batch = []
     for s in range(steps + 1):
         b.centroids.copy_(c0_all)
@@ -287,7 +290,11 @@ def run_batched(dev, nimages, steps, seed=SEED + 1000):
     from split_gb300 import _native as N
     from split_gb300._util import ptr, stream_handle
     lib = N.load()
+    # initial centroids (the batch runs update the arena in place)
+    b.centroids.copy_(c0_all)
     views = [(b.rgb_of(i), b.centroids_of(i).clone()) for i in range(nimages)]
+    b.replay()  # leaves the arenas holding one run's results for the comparison below
+    torch.cuda.synchronize()
     outs = [(torch.empty(w * h, dtype=torch.int32, device=dev),
              torch.empty(w * h, dtype=torch.int32, device=dev),
              torch.empty(3 * w * h, dtype=torch.float32, device=dev)) for w, h, _, _ in shapes]
@@ -302,7 +309,10 @@ def run_batched(dev, nimages, steps, seed=SEED + 1000):
             N.check(lib.split_pipeline_run(ptr(views[i][0]), w, h, C.byref(cps[i]), ptr(cents[i]),
                                            ptr(outs[i][0]), ptr(outs[i][1]), ptr(outs[i][2]),
                                            pipe.ws.ptr, pipe.ws.nbytes, None, st), "plain")
+    l0 = pipeline.launch_count()
     plain_once()
+    torch.cuda.synchronize()
+    plain_launches = pipeline.launch_count() - l0
     t_plain = []
     for s in range(max(2, steps // 2) + 1):
         flush.zero_()
@@ -324,7 +334,7 @@ def run_batched(dev, nimages, steps, seed=SEED + 1000):
             "plain_mpix_s": round(total_px / (tp * 1e-3) / 1e6, 1),
             "batched_ms": round(tb, 3), "plain_ms": round(tp, 3),
             "speedup": round(tp / tb, 2), "identical_labels": bool(same),
-            "batched_launches_per_run": None}
+            "launches_per_run": {"batched": int(batch_launches), "plain": int(plain_launches)}}
 
 
 # ------------------------------------------------------------------------ GPU
