@@ -338,6 +338,55 @@ def run_batched(dev, nimages, steps, seed=SEED + 1000):
 
 
 # ------------------------------------------------------------------------ GPU
+def run_serving(dev, nimages, nrequests, seed=SEED + 2000):
+    """Continuous batching under open-loop Poisson arrivals (40 GB admission
+    budget, batches of at most 64 Mpix, two batches in flight).  A closed
+    run of every request at once gives the saturation throughput; open-loop
+    runs at 50% and 80% of it give p50/p99 latency.  Request images sit in
+    pinned host memory, as a receive path would leave them."""
+    import torch
+    from split_gb300 import pipeline
+    from split_gb300.serve import Request, Server, poisson_arrivals
+    shapes = batch_shapes(nimages, seed)
+    imgs, cents = batch_images(shapes, seed)
+    h_rgb = [torch.from_numpy(im).pin_memory() for im in imgs]
+    h_c0 = [torch.from_numpy(c).pin_memory() for c in cents]
+    params = pipeline.Params()
+
+    def requests(arrivals):
+        out = []
+        for j, t in enumerate(arrivals):
+            i = j % nimages
+            w, h, k, iters = shapes[i]
+            out.append(Request(j, h_rgb[i], k, iters, h_c0[i], float(t)))
+        return out
+
+    srv = Server(params, device=dev, keep_results=False)
+    srv.serve(requests([0.0] * min(64, nrequests)), realtime=False)   # warm-up
+    srv.completed.clear()
+    nb0 = len(srv.batch_sizes)
+    t = time.perf_counter()
+    done = srv.serve(requests([0.0] * nrequests), realtime=False)
+    wall = time.perf_counter() - t
+    sat = Server.report(done, wall)
+    sat["mean_batch"] = round(nrequests / max(1, len(srv.batch_sizes) - nb0), 2)
+    sat_rps = len(done) / wall
+    out = {"requests": nrequests, "distinct_images": nimages,
+           "mean_mpix_per_request": round(sum(s[0] * s[1] for s in shapes) / nimages / 1e6, 3),
+           "saturation": sat}
+    for load in (0.5, 0.8):
+        srv = Server(params, device=dev, keep_results=False)
+        arr = poisson_arrivals(seed + int(load * 100), nrequests, load * sat_rps)
+        t = time.perf_counter()
+        done = srv.serve(requests(arr))
+        wall = time.perf_counter() - t
+        rep = Server.report(done, wall)
+        rep["offered_rps"] = round(load * sat_rps, 1)
+        rep["mean_batch"] = round(sum(srv.batch_sizes) / max(1, len(srv.batch_sizes)), 2)
+        out[f"load_{int(load * 100)}"] = rep
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -351,6 +400,8 @@ def main():
     ap.add_argument("--cpu-side", type=int, default=512)
     ap.add_argument("--batch-images", type=int, default=256)
     ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--serve-requests", type=int, default=1024)
+    ap.add_argument("--no-serve", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -465,6 +516,9 @@ def main():
     batched = None
     if not args.no_batch and args.batch_images > 0:
         batched = run_batched(dev, args.batch_images, steps=5)
+    serving = None
+    if not args.no_serve and args.serve_requests > 0:
+        serving = run_serving(dev, min(args.batch_images, 256) or 64, args.serve_requests)
 
     if rank == 0:
         cpu = None
@@ -490,6 +544,7 @@ def main():
             "clocks": clocks,
             "stages_ms": {k: round(v, 4) for k, v in stage_ms.items()},
             "batched": batched,
+            "serving": serving,
             "wall_s_timed_region": round(t_wall, 3),
         }
         print(json.dumps(line), flush=True)
