@@ -338,6 +338,53 @@ def run_batched(dev, nimages, steps, seed=SEED + 1000):
 
 
 # ------------------------------------------------------------------------ GPU
+def run_stress(dev, side=8192, steps=10, seed=2024):
+    """Labelling stress case: side x side maze + blob labels (one serpentine
+    corridor over half the pixels), 4- and 8-connected min-index CCL with
+    component sizes, device-resident (268 MB in, 268 MB out: larger than L2).
+    The oracle's union-find on one host thread is timed once beside it."""
+    import numpy as np
+    import torch
+    from split_gb300 import ccl, synth
+    lab = synth.maze_labels(seed, side, side)
+    d_lab = torch.from_numpy(lab).to(dev)
+    out = torch.empty_like(d_lab)
+    sizes = torch.zeros(side * side, dtype=torch.int32, device=dev)
+    ws = None
+    res = {"workload": f"{side}x{side} maze+blob labels, min-index CCL with sizes"}
+    npx = side * side
+    peak, _ = peaks()
+    for conn in (4, 8):
+        for _ in range(3):
+            ws = ccl.connected_components(d_lab, ws, out, connectivity=conn, convention=0,
+                                          sizes=sizes)
+        e = [torch.cuda.Event(enable_timing=True) for _ in range(2 * steps)]
+        for x in e:
+            x.record()
+        torch.cuda.synchronize()
+        for s in range(steps):
+            e[2 * s].record()
+            ws = ccl.connected_components(d_lab, ws, out, connectivity=conn, convention=0,
+                                          sizes=sizes)
+            e[2 * s + 1].record()
+        torch.cuda.synchronize()
+        ms = statistics.median(e[2 * s].elapsed_time(e[2 * s + 1]) for s in range(steps))
+        gbs = npx * 8 / (ms * 1e-3) / 1e9
+        res[f"ccl{conn}"] = {"ms": round(ms, 4), "mpix_s": round(npx / (ms * 1e-3) / 1e6, 1),
+                             "gb_s": round(gbs, 1), "frac": round(gbs / peak, 4)}
+    ws.check("stress ccl")
+    try:
+        import oracle
+        t = time.perf_counter()
+        ref = oracle.ccl(lab, 8, 0)
+        dt = time.perf_counter() - t
+        res["oracle_ccl8_s"] = round(dt, 3)
+        res["identical"] = bool(np.array_equal(out.cpu().numpy(), ref))
+    except Exception as exc:  # the oracle is a checker here; report why it is absent
+        res["oracle"] = f"unavailable: {exc}"
+    return res
+
+
 def run_serving(dev, nimages, nrequests, seed=SEED + 2000):
     """Continuous batching under open-loop Poisson arrivals (40 GB admission
     budget, batches of at most 64 Mpix, two batches in flight).  A closed
@@ -402,6 +449,7 @@ def main():
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--serve-requests", type=int, default=1024)
     ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--no-stress", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -516,6 +564,7 @@ def main():
     batched = None
     if not args.no_batch and args.batch_images > 0:
         batched = run_batched(dev, args.batch_images, steps=5)
+    stress = None if args.no_stress else run_stress(dev)
     serving = None
     if not args.no_serve and args.serve_requests > 0:
         serving = run_serving(dev, min(args.batch_images, 256) or 64, args.serve_requests)
@@ -545,6 +594,7 @@ def main():
             "stages_ms": {k: round(v, 4) for k, v in stage_ms.items()},
             "batched": batched,
             "serving": serving,
+            "stress": stress,
             "wall_s_timed_region": round(t_wall, 3),
         }
         print(json.dumps(line), flush=True)

@@ -236,3 +236,106 @@ def test_workspace_reuse_across_sizes(cuda):
         assert torch.equal(out[1].view(h, w), alone.segment_labels), (w, h)
         assert torch.equal(cent, alone.centroids), (w, h)
         big.ws.check("pipeline")
+
+
+# ---------------------------------------------------------------- edge cases
+@pytest.mark.parametrize("radius", [5, 8, 16])
+def test_erode_large_radius(cuda, radius):
+    import torch
+    from split_gb300 import morph
+    rng = np.random.default_rng(radius)
+    lab = rng.integers(0, 3, size=(12, 15)).repeat(23, 0).repeat(19, 1)[:270, :277]
+    lab = np.ascontiguousarray(lab).astype(np.int32)
+    out = morph.erode(_t(lab, cuda), radius, out=torch.empty(lab.shape, dtype=torch.int32,
+                                                            device=cuda))
+    assert np.array_equal(out.cpu().numpy(), oracle.erode(lab, radius))
+
+
+@pytest.mark.parametrize("fill", ["uniform", "checker"])
+def test_ccl_degenerate_images(cuda, fill):
+    """One component covering the image, and every pixel its own component
+    under 4-connectivity (a checkerboard joins diagonally under 8)."""
+    import torch
+    from split_gb300 import ccl
+    h, w = 333, 517
+    if fill == "uniform":
+        lab = np.full((h, w), 5, np.int32)
+    else:
+        lab = ((np.arange(h)[:, None] + np.arange(w)[None, :]) % 2).astype(np.int32)
+    for conn in (4, 8):
+        for conv in (0, 1):
+            out = torch.empty((h, w), dtype=torch.int32, device=cuda)
+            ccl.connected_components(_t(lab, cuda), None, out, connectivity=conn,
+                                     convention=conv)
+            assert np.array_equal(out.cpu().numpy(), oracle.ccl(lab, conn, conv))
+
+
+@pytest.mark.parametrize("policy", [0, 1])
+def test_merge_all_small_and_none_small(cuda, policy):
+    import torch
+    from split_gb300 import ccl
+    rng = np.random.default_rng(9)
+    h, w = 96, 160
+    lab = rng.integers(0, 6, size=(h // 2, w // 2)).repeat(2, 0).repeat(2, 1).astype(np.int32)
+    seg = oracle.ccl(lab, 8, 0)
+    chroma = (rng.integers(0, 256, size=(2, h * w)) / 256.0).astype(np.float32)
+    for P in (1, h * w + 1):          # nothing small / everything small
+        ref = oracle.merge_small(seg, P, policy, chroma)
+        g = _t(seg, cuda)
+        ccl.merge_small_segments(_t(chroma, cuda), g, None, P, policy=policy)
+        assert np.array_equal(g.cpu().numpy(), ref), P
+
+
+def test_kmeans_k64_many_iterations(cuda):
+    """K at its maximum (64) over 5-D features, 32 iterations, in lockstep:
+    labels equal the FP32-exact assignment, centroids the FP64 update of the
+    device's labels (empty clusters keep their centroid on both sides)."""
+    import torch
+    from split_gb300 import kmeans
+    w, h, k = 300, 211, 64
+    rgb = synth.voronoi_rgb8(77, w, h, 150, npalette=40, illum_gradient=True, sigma=5.0)
+    feats = synth.features(rgb, 5)
+    c = synth.pick_centroids(77, rgb, k, 5)
+    pts = _t(feats, cuda)
+    cent = _t(c, cuda)
+    labels = torch.empty(w * h, dtype=torch.int32, device=cuda)
+    ws = None
+    for it in range(32):
+        ws = kmeans.cluster(pts, cent, labels, ws, max_iter=1, threshold=-1.0, layout=0,
+                            dim=5, width=w)
+        gl = labels.cpu().numpy()
+        gc = cent.cpu().numpy()
+        assert np.array_equal(gl, oracle.kmeans_assign_f32(feats, c)), f"iteration {it}"
+        ref, _ = oracle.kmeans_update_f64(gl, feats, c)
+        rel = np.abs(gc - ref) / np.maximum(np.abs(ref), 1e-30)
+        assert rel.max() <= 1e-5, f"iteration {it}: centroid rel err {rel.max():.3g}"
+        c = gc
+    ws.check("kmeans")
+
+
+def test_ccl_stress_8192_maze(cuda):
+    """Labelling stress case: 8192 x 8192 maze (one serpentine corridor over
+    half the image, path > 10^7 px) plus random wall blobs; 4- and
+    8-connected, both conventions, bit-exact, with component sizes."""
+    import torch
+    from split_gb300 import ccl
+    n = 8192
+    lab = synth.maze_labels(2024, n, n)
+    d_lab = _t(lab, cuda)
+    out = torch.empty((n, n), dtype=torch.int32, device=cuda)
+    sizes = torch.zeros(n * n, dtype=torch.int32, device=cuda)
+    ws = None
+    for conn in (4, 8):
+        for conv in (0, 1):
+            sizes.zero_()
+            ws = ccl.connected_components(d_lab, ws, out, connectivity=conn, convention=conv,
+                                          sizes=sizes)
+            ref = oracle.ccl(lab, conn, conv)
+            got = out.cpu().numpy()
+            assert np.array_equal(got, ref), (conn, conv)
+            roots, counts = np.unique(ref, return_counts=True)
+            assert np.array_equal(sizes.cpu().numpy()[roots], counts)
+            if conn == 4 and conv == 0:
+                assert counts.max() > n * n // 3       # the serpentine corridor
+                assert len(roots) > 10 ** 4
+    ws.check("ccl")
