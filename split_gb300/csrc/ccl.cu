@@ -28,11 +28,30 @@ namespace sg {
 namespace ccl {
 
 constexpr int TH = kTileH, TW = kTileW, kThreads = 256;
-constexpr unsigned kUnionCap = 1u << 22;
+constexpr int kWarpsPerTile = kThreads / 32;
+constexpr int kRowsPerWarp = TH / kWarpsPerTile;   // 4 rows per warp, 2 pixels per lane
+// Bounds on union retries and on find chains (a tile forest has fewer than
+// TH * TW nodes; global chains are short after halving).  Running out sets
+// SPLIT_ERR_NOT_CONVERGED in the workspace status and returns.
+constexpr unsigned kUnionCap = 1u << 16;
+constexpr unsigned kFindCap = 1u << 20;
+constexpr unsigned kFull = 0xffffffffu;
+static_assert(TW == 64 && TH % kWarpsPerTile == 0, "a warp covers whole 64-pixel rows");
 
 template <bool MAXC>
 __device__ __forceinline__ bool better(int a, int b) {
   return MAXC ? a > b : a < b;
+}
+
+__device__ __forceinline__ unsigned lanemask_le() {
+  unsigned m;
+  asm("mov.u32 %0, %%lanemask_le;" : "=r"(m));
+  return m;
+}
+__device__ __forceinline__ unsigned lanemask_ge() {
+  unsigned m;
+  asm("mov.u32 %0, %%lanemask_ge;" : "=r"(m));
+  return m;
 }
 
 // ---- shared-memory union-find --------------------------------------------
@@ -41,9 +60,19 @@ __device__ __forceinline__ bool better(int a, int b) {
 // a race is retried by sunite with the node's new parent.
 __device__ __forceinline__ int sfind(volatile int* par, int x) {
   int p = par[x];
-  while (p != x) {
+  for (int hop = 0; p != x && hop < TH * TW; ++hop) {
     const int gp = par[p];
     if (gp != p) par[x] = gp;
+    x = p;
+    p = par[x];
+  }
+  return x;
+}
+
+// Root of x without writes (for phases where nothing hooks any more).
+__device__ __forceinline__ int sroot(const int* par, int x) {
+  int p = par[x];
+  for (int hop = 0; p != x && hop < TH * TW; ++hop) {
     x = p;
     p = par[x];
   }
@@ -68,20 +97,27 @@ __device__ __forceinline__ void sunite(int* par, int a, int b, int* status) {
   set_status(status, SPLIT_ERR_NOT_CONVERGED);
 }
 
-// ---- global union-find (parents in labels_out) -----------------------------
-__device__ __forceinline__ int gfind(const int* P, int x, unsigned& budget) {
+// ---- global union-find over local roots (parents in labels_out) ----------
+// Parents only move towards the better end (atomicMin / atomicMax hooks, and
+// halving stores of a grandparent), so every store points a node at one of
+// its ancestors and concurrent finds stay correct.
+__device__ __forceinline__ int gfind(int* P, int x, unsigned& budget) {
   int p = __ldcg(P + x);
-  while (p != x && budget) {
-    x = p;
-    p = __ldcg(P + x);
+  while (p != x) {
+    if (!budget) return x;
     --budget;
+    const int gp = __ldcg(P + p);
+    if (gp == p) return p;
+    __stcg(P + x, gp);   // path halving
+    x = gp;
+    p = __ldcg(P + x);
   }
   return x;
 }
 
 template <bool MAXC>
 __device__ void gunite(int* P, int a, int b, int* status) {
-  unsigned budget = kUnionCap;
+  unsigned budget = kFindCap;
   for (unsigned it = 0; it < kUnionCap && budget; ++it) {
     a = gfind(P, a, budget);
     b = gfind(P, b, budget);
@@ -96,147 +132,344 @@ __device__ void gunite(int* P, int a, int b, int* status) {
   set_status(status, SPLIT_ERR_NOT_CONVERGED);
 }
 
-// Tile pass.  Thread t owns 8 consecutive pixels of row t / 8; runs of equal
-// label inside those 8 pixels are linked without atomics, and a union is only
-// issued where run adjacency does not already imply it:
-//   W  : only at the first pixel of a thread's 8 (other W links are runs);
-//   N  : unless W and NW both carry the label (the NW/N run already joins);
-//   NW : only if neither W nor N carries the label;
-//   NE : only if N does not carry the label and E (in the tile) does not
-//        either (E's own N link covers NE).
+// Links that must be unioned between a pixel p (label v) and the row above,
+// given equality flags with its neighbours.  Skipped links are implied by
+// earlier ones (runs in a row are joined; W + NW cover N; W or N cover NW;
+// N or E cover NE), which keeps the number of atomics near the number of
+// run overlaps.
+struct Links {
+  bool n, nw, ne;
+};
+template <int CONN>
+__device__ __forceinline__ Links needed(bool N, bool W, bool NW, bool NE, bool E) {
+  Links l;
+  l.n = N && !(W && NW);
+  l.nw = CONN == 8 && NW && !W && !N;
+  l.ne = CONN == 8 && NE && !N && !E;
+  return l;
+}
+
+// Tile pass.  Warp w owns rows [4w, 4w + 4) of a 32 x 64 tile; lane l holds
+// columns l and l + 32 of each row.  Row runs come from warp ballots: the
+// node of a run is its first pixel (minimum convention) or its last
+// (maximum), and every pixel records its node.  Unions run on nodes only, in
+// a shared-memory union-find; after one find per node every pixel reads its
+// root in one step and stores the global index of that local root.  Local
+// roots clear their size counter.
 template <bool MAXC, int CONN>
 __global__ void __launch_bounds__(kThreads)
 tile_kernel(const int32_t* __restrict__ in, Geoms gs, int* __restrict__ P,
             int32_t* __restrict__ sizes, int* status) {
-  static_assert(TW == 64 && TH * TW == kThreads * 8, "8 pixels per thread");
   __shared__ int lab[TH * TW];
   __shared__ int par[TH * TW];
   const TileRef t = tile_ref(gs, blockIdx.x);
-  const int W = t.W, H = t.H, tx0 = t.tx0, ty0 = t.ty0;
+  const int W = t.W, tx0 = t.tx0, ty0 = t.ty0;
   const long long off = t.off;
-  const int tw = min(TW, W - tx0), th = min(TH, H - ty0);
-  for (int i = threadIdx.x; i < TH * TW; i += kThreads) {
-    const int r = i / TW, c = i % TW;
-    lab[i] = (r < th && c < tw) ? __ldg(in + off + (long long)(ty0 + r) * W + tx0 + c) : 0;
-  }
-  __syncthreads();
-  const int r = threadIdx.x >> 3, c0 = (threadIdx.x & 7) * 8;
-  const int base = r * TW + c0;
-  {
-    // runs point at their best pixel: the first (minimum index convention)
-    // or the last (maximum index convention)
-    const bool ok_row = r < th;
+  const int tw = min(TW, W - tx0), th = min(TH, t.H - ty0);
+  const int lane = threadIdx.x & 31, r0 = (threadIdx.x >> 5) * kRowsPerWarp;
+  const bool ca = lane < tw, cb = lane + 32 < tw;
+  int va[kRowsPerWarp], vb[kRowsPerWarp], na[kRowsPerWarp], nb[kRowsPerWarp];
+#pragma unroll
+  for (int k = 0; k < kRowsPerWarp; ++k) {
+    const int r = r0 + k;
+    const bool rok = r < th;
+    const int32_t* row = in + off + (long long)(ty0 + (rok ? r : 0)) * W + tx0;
+    va[k] = (rok && ca) ? __ldg(row + lane) : 0;
+    vb[k] = (rok && cb) ? __ldg(row + lane + 32) : 0;
+    lab[r * TW + lane] = va[k];
+    lab[r * TW + lane + 32] = vb[k];
+    // run nodes of this row
+    const bool oa = rok && ca, ob = rok && cb;
+    int nda, ndb;
     if (!MAXC) {
-      int run = base;
-      par[base] = base;
-#pragma unroll
-      for (int j = 1; j < 8; ++j) {
-        const int i = base + j;
-        if (!(ok_row && c0 + j < tw) || lab[i] != lab[i - 1]) run = i;
-        par[i] = run;
-      }
+      const int la = __shfl_up_sync(kFull, va[k], 1);
+      const int a31 = __shfl_sync(kFull, va[k], 31);
+      const int lb0 = __shfl_up_sync(kFull, vb[k], 1);
+      const int lb = lane == 0 ? a31 : lb0;
+      const unsigned ma = __ballot_sync(kFull, oa && (lane == 0 || la != va[k]));
+      const unsigned mb = __ballot_sync(kFull, ob && lb != vb[k]);
+      const unsigned le = lanemask_le();
+      nda = 31 - __clz(ma & le | 1u);
+      const unsigned mbl = mb & le;
+      ndb = mbl ? 63 - __clz(mbl) : 31 - __clz(ma | 1u);
     } else {
-      int run = base + 7;
-      par[base + 7] = base + 7;
-#pragma unroll
-      for (int j = 6; j >= 0; --j) {
-        const int i = base + j;
-        if (!(ok_row && c0 + j + 1 < tw) || lab[i] != lab[i + 1]) run = i;
-        par[i] = run;
-      }
+      const int ra0 = __shfl_down_sync(kFull, va[k], 1);
+      const int b0 = __shfl_sync(kFull, vb[k], 0);
+      const int ra = lane == 31 ? b0 : ra0;
+      const int rb = __shfl_down_sync(kFull, vb[k], 1);
+      const unsigned ma = __ballot_sync(kFull, oa && (lane + 1 >= tw || ra != va[k]));
+      const unsigned mb = __ballot_sync(kFull, ob && (lane + 33 >= tw || rb != vb[k]));
+      const unsigned ge = lanemask_ge();
+      const unsigned mag = ma & ge, mbg = mb & ge;
+      nda = mag ? __ffs(mag) - 1 : 31 + __ffs(mb | 0x80000000u);
+      ndb = 31 + __ffs(mbg | 0x80000000u);
     }
+    na[k] = oa ? r * TW + nda : r * TW + lane;
+    nb[k] = ob ? r * TW + ndb : r * TW + lane + 32;
+    par[r * TW + lane] = na[k];
+    par[r * TW + lane + 32] = nb[k];
   }
   __syncthreads();
-  if (r < th) {
+  // links with the row above (rows 1 .. th - 1 of the tile).  All warp
+  // shuffles happen first, with every lane converged, and the needed links
+  // are kept as bits; the unions (divergent, retried) come afterwards with
+  // no warp-synchronous instruction behind them.
+  unsigned links = 0;   // bit 6k + 3h + j: row k, half h, link j (N, NW, NE)
 #pragma unroll
-    for (int j = 0; j < 8; ++j) {
-      const int c = c0 + j;
-      if (c >= tw) break;
-      const int i = base + j;
-      const int v = lab[i];
-      const bool hasW = c > 0 && lab[i - 1] == v;
-      if (j == 0 && hasW) sunite<MAXC>(par, i, i - 1, status);
-      if (r > 0) {
-        const bool n = lab[i - TW] == v;
-        const bool nw = c > 0 && lab[i - TW - 1] == v;
-        if (n && !(hasW && nw)) sunite<MAXC>(par, i, i - TW, status);
-        if (CONN == 8) {
-          if (nw && !hasW && !n) sunite<MAXC>(par, i, i - TW - 1, status);
-          const bool ne = c + 1 < tw && lab[i - TW + 1] == v;
-          const bool e = c + 1 < tw && lab[i + 1] == v;
-          if (ne && !n && !e) sunite<MAXC>(par, i, i - TW + 1, status);
-        }
-      }
+  for (int k = 0; k < kRowsPerWarp; ++k) {
+    const int r = r0 + k;
+    const bool rok = r > 0 && r < th;              // warp-uniform
+    const int ua = r > 0 ? lab[(r - 1) * TW + lane] : 0;
+    const int ub = r > 0 ? lab[(r - 1) * TW + lane + 32] : 0;
+    const int a = va[k], b = vb[k];
+    // row neighbours of the pixel and of the pixel above
+    const int la = __shfl_up_sync(kFull, a, 1), a31 = __shfl_sync(kFull, a, 31);
+    const int lb0 = __shfl_up_sync(kFull, b, 1);
+    const int ra0 = __shfl_down_sync(kFull, a, 1), b0 = __shfl_sync(kFull, b, 0);
+    const int rb = __shfl_down_sync(kFull, b, 1);
+    const int ula = __shfl_up_sync(kFull, ua, 1), ua31 = __shfl_sync(kFull, ua, 31);
+    const int ulb0 = __shfl_up_sync(kFull, ub, 1);
+    const int ura0 = __shfl_down_sync(kFull, ua, 1), ub0 = __shfl_sync(kFull, ub, 0);
+    const int urb = __shfl_down_sync(kFull, ub, 1);
+    const int lb = lane == 0 ? a31 : lb0, ulb = lane == 0 ? ua31 : ulb0;
+    const int ra = lane == 31 ? b0 : ra0, ura = lane == 31 ? ub0 : ura0;
+    if (rok && ca) {
+      const bool hasW = lane > 0, hasE = lane + 1 < tw;
+      const Links l = needed<CONN>(ua == a, hasW && la == a, hasW && ula == a,
+                                   hasE && ura == a, hasE && ra == a);
+      links |= (unsigned)(l.n | (l.nw << 1) | (l.ne << 2)) << (6 * k);
+    }
+    if (rok && cb) {
+      const bool hasE = lane + 33 < tw;
+      const Links l = needed<CONN>(ub == b, lb == b, ulb == b, hasE && urb == b,
+                                   hasE && rb == b);
+      links |= (unsigned)(l.n | (l.nw << 1) | (l.ne << 2)) << (6 * k + 3);
     }
   }
-  __syncthreads();
-  if (r < th) {
+  while (links) {
+    const int bit = __ffs(links) - 1;
+    links &= links - 1;
+    const int k = bit / 6, h = (bit % 6) / 3, j = bit % 3;
+    const int up = (r0 + k - 1) * TW + lane + 32 * h + (j == 1 ? -1 : j == 2 ? 1 : 0);
+    int nd = na[0];
 #pragma unroll
-    for (int j = 0; j < 8; ++j) {
-      const int c = c0 + j;
-      if (c >= tw) break;
-      const int i = base + j;
-      const int root = sfind(par, i);
-      const long long g = off + (long long)(ty0 + r) * W + tx0 + c;
-      P[g] = (int)(off + (long long)(ty0 + root / TW) * W + tx0 + root % TW);
-      if (sizes && root == i) sizes[g] = 0;
+    for (int q = 0; q < kRowsPerWarp; ++q)
+      if (q == k) nd = h ? nb[q] : na[q];
+    sunite<MAXC>(par, nd, par[up], status);
+  }
+  __syncwarp();
+  __syncthreads();
+  // one find per node (read-only, so concurrent finds see a fixed forest),
+  // then every node points straight at its root
+  int roota[kRowsPerWarp], rootb[kRowsPerWarp];
+#pragma unroll
+  for (int k = 0; k < kRowsPerWarp; ++k) {
+    const int r = r0 + k;
+    const int ia = r * TW + lane, ib = ia + 32;
+    roota[k] = (r < th && ca && na[k] == ia) ? sroot(par, ia) : -1;
+    rootb[k] = (r < th && cb && nb[k] == ib) ? sroot(par, ib) : -1;
+  }
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < kRowsPerWarp; ++k) {
+    const int ia = (r0 + k) * TW + lane;
+    if (roota[k] >= 0) par[ia] = roota[k];
+    if (rootb[k] >= 0) par[ia + 32] = rootb[k];
+  }
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < kRowsPerWarp; ++k) {
+    const int r = r0 + k;
+    if (r >= th) continue;
+    const long long rowg = off + (long long)(ty0 + r) * W + tx0;
+    if (ca) {
+      const int root = par[na[k]];
+      const long long g = rowg + lane;
+      __stcg(P + g, (int)(off + (long long)(ty0 + root / TW) * W + tx0 + root % TW));
+      if (sizes && root == r * TW + lane) sizes[g] = 0;
+    }
+    if (cb) {
+      const int root = par[nb[k]];
+      const long long g = rowg + lane + 32;
+      __stcg(P + g, (int)(off + (long long)(ty0 + root / TW) * W + tx0 + root % TW));
+      if (sizes && root == r * TW + lane + 32) sizes[g] = 0;
     }
   }
 }
 
+// Border pass, one 128-thread block per tile: warps 0-1 join the top row
+// with the row above (N, NW, NE links into the tiles above), warp 2 joins
+// the left column with the column to its left (W, NW), warp 3 the right
+// column with the tile to its right (NE, 8-connectivity only).  Unions start
+// at the local roots the tile pass stored and skip links implied by others
+// (the same rules as inside a tile, with neighbours read across the edge).
+constexpr int kBorderThreads = 128;
+
 template <bool MAXC, int CONN>
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kBorderThreads)
 border_kernel(const int32_t* __restrict__ in, Geoms gs, int* P, int* status) {
   const TileRef t = tile_ref(gs, blockIdx.x);
   const int W = t.W, tx0 = t.tx0, ty0 = t.ty0;
   const long long off = t.off;
   const int tw = min(TW, W - tx0), th = min(TH, t.H - ty0);
-  // top row (tw pixels), left column (th - 1 pixels), right column (th - 1)
-  const int nb = tw + 2 * (th - 1);
-  for (int j = threadIdx.x; j < nb; j += kThreads) {
-    int r, c;
-    if (j < tw) { r = 0; c = j; }
-    else if (j < tw + th - 1) { r = j - tw + 1; c = 0; }
-    else { r = j - tw - th + 2; c = tw - 1; }
-    const int x = tx0 + c, y = ty0 + r;
-    const int g = (int)(off + (long long)y * W + x);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (warp < 2) {
+    if (ty0 == 0) return;
+    const int c = warp * 32 + lane;
+    if (c >= tw) return;
+    const int x = tx0 + c;
+    const long long g = off + (long long)ty0 * W + x;
     const int v = __ldg(in + g);
-    // backward neighbours that lie in another tile
-    if (c == 0 && x > 0 && __ldg(in + g - 1) == v) gunite<MAXC>(P, g, g - 1, status);
-    if (y > 0) {
-      if (r == 0 && __ldg(in + g - W) == v) gunite<MAXC>(P, g, g - W, status);
-      if (CONN == 8) {
-        if ((r == 0 || c == 0) && x > 0 && __ldg(in + g - W - 1) == v)
-          gunite<MAXC>(P, g, g - W - 1, status);
-        if ((r == 0 || c == tw - 1) && x + 1 < W && __ldg(in + g - W + 1) == v)
-          gunite<MAXC>(P, g, g - W + 1, status);
-      }
+    const bool hasW = x > 0, hasE = x + 1 < W;
+    const bool N = __ldg(in + g - W) == v;
+    const bool Wq = hasW && __ldg(in + g - 1) == v;
+    const bool NW = hasW && __ldg(in + g - W - 1) == v;
+    const bool NE = hasE && __ldg(in + g - W + 1) == v;
+    const bool E = hasE && __ldg(in + g + 1) == v;
+    // at the tile's first column the W link crosses into the left tile and
+    // is made by that edge's warp; the rule still holds across tiles
+    const Links l = needed<CONN>(N, Wq, NW, NE, E);
+    if (l.n || l.nw || l.ne) {
+      const int a = __ldcg(P + g);
+      if (l.n) gunite<MAXC>(P, a, __ldcg(P + g - W), status);
+      if (l.nw) gunite<MAXC>(P, a, __ldcg(P + g - W - 1), status);
+      if (l.ne) gunite<MAXC>(P, a, __ldcg(P + g - W + 1), status);
     }
+  } else if (warp == 2) {
+    if (tx0 == 0 || lane >= th) return;
+    const int y = ty0 + lane;
+    const long long g = off + (long long)y * W + tx0;
+    const int v = __ldg(in + g);
+    const bool Wq = __ldg(in + g - 1) == v;
+    if (lane == 0) {
+      // the corner pixel: its N / NW links belong to the top-edge warps
+      if (Wq) gunite<MAXC>(P, __ldcg(P + g), __ldcg(P + g - 1), status);
+      return;
+    }
+    const bool N = __ldg(in + g - W) == v;
+    const bool NW = __ldg(in + g - W - 1) == v;
+    // W is implied when N and NW carry the label (both columns are joined
+    // one row up, and N joins inside this tile)
+    const bool lw = Wq && !(N && NW);
+    const bool lnw = CONN == 8 && NW && !Wq && !N;
+    if (lw || lnw) {
+      const int a = __ldcg(P + g);
+      if (lw) gunite<MAXC>(P, a, __ldcg(P + g - 1), status);
+      if (lnw) gunite<MAXC>(P, a, __ldcg(P + g - W - 1), status);
+    }
+  } else if (CONN == 8) {
+    // right column, rows 1 .. th - 1: the NE link into the tile to the right
+    const int x = tx0 + tw - 1;
+    if (x + 1 >= W || lane == 0 || lane >= th) return;
+    const long long g = off + (long long)(ty0 + lane) * W + x;
+    const int v = __ldg(in + g);
+    const bool NE = __ldg(in + g - W + 1) == v;
+    if (NE && __ldg(in + g - W) != v && __ldg(in + g + 1) != v)
+      gunite<MAXC>(P, __ldcg(P + g), __ldcg(P + g - W + 1), status);
   }
 }
 
-// Flatten pass, one block per tile (only image pixels are touched, so batch
-// arenas may carry padding between images).
+// Flatten pass, one block per tile, same pixel mapping as the tile pass.
+// After the border pass every pixel's entry points at a local root of its
+// own tile (or, for a local root joined across tiles, at another tile's
+// local root).  Each local component is resolved once: pixels whose entry
+// leaves the tile chase the global forest (read-only: entries of other
+// tiles are being finalised concurrently, always to their root), the rest
+// follow entries inside the tile through shared memory.  Component sizes
+// are counted per tile and added with one atomic per local component.
+__device__ __forceinline__ int local_of(long long v, long long off, int W, int tx0, int ty0,
+                                        int tw, int th) {
+  const long long rel = v - off;
+  if (rel < 0) return -1;
+  const int y = (int)(rel / W), x = (int)(rel - (long long)y * W);
+  const int r = y - ty0, c = x - tx0;
+  return (r >= 0 && r < th && c >= 0 && c < tw) ? r * TW + c : -1;
+}
+
+__device__ __forceinline__ int groot(const int* P, int x, unsigned& budget) {
+  int p = __ldcg(P + x);
+  while (p != x && budget) {
+    --budget;
+    x = p;
+    p = __ldcg(P + x);
+  }
+  return x;
+}
+
 __global__ void __launch_bounds__(kThreads)
 flatten_kernel(int* P, Geoms gs, int32_t* __restrict__ sizes, int* status) {
-  const unsigned full = 0xffffffffu;
+  __shared__ int ent[TH * TW];   // the pixel's entry (global index)
+  __shared__ int res[TH * TW];   // resolved root of a terminal pixel, else -1
+  __shared__ int cnt[TH * TW];   // pixels that resolved through this terminal
   const TileRef t = tile_ref(gs, blockIdx.x);
-  for (int q = threadIdx.x; q < TH * TW; q += kThreads) {
-    const int x = t.tx0 + q % TW, y = t.ty0 + q / TW;
-    int root = -1;
-    if (x < t.W && y < t.H) {
-      const long long g = t.off + (long long)y * t.W + x;
-      unsigned budget = kUnionCap;
-      const int lr = __ldcg(P + g);
-      root = gfind(P, lr, budget);
+  const int W = t.W, tx0 = t.tx0, ty0 = t.ty0;
+  const long long off = t.off;
+  const int tw = min(TW, W - tx0), th = min(TH, t.H - ty0);
+  const int lane = threadIdx.x & 31, r0 = (threadIdx.x >> 5) * kRowsPerWarp;
+  int e[2 * kRowsPerWarp];
+#pragma unroll
+  for (int k = 0; k < 2 * kRowsPerWarp; ++k) {
+    const int r = r0 + (k >> 1), c = lane + 32 * (k & 1);
+    const int i = r * TW + c;
+    const bool ok = r < th && c < tw;
+    const long long g = off + (long long)(ty0 + r) * W + tx0 + c;
+    e[k] = ok ? __ldcg(P + g) : -1;
+    ent[i] = e[k];
+    cnt[i] = 0;
+    int rv = -1;
+    if (ok && e[k] == (int)g) rv = (int)g;
+    res[i] = rv;
+  }
+  __syncthreads();
+  // pixels whose entry leaves the tile: local roots joined elsewhere
+#pragma unroll
+  for (int k = 0; k < 2 * kRowsPerWarp; ++k) {
+    const int r = r0 + (k >> 1), c = lane + 32 * (k & 1);
+    if (r < th && c < tw && res[r * TW + c] < 0 &&
+        local_of(e[k], off, W, tx0, ty0, tw, th) < 0) {
+      unsigned budget = kFindCap;
+      res[r * TW + c] = groot(P, e[k], budget);
       if (!budget) set_status(status, SPLIT_ERR_NOT_CONVERGED);
-      P[g] = root;
-      if (lr != root) P[lr] = root;  // later pixels of this local tree: one hop
     }
-    if (sizes) {
-      const unsigned peers = __match_any_sync(full, root);
-      const int leader = __ffs(peers) - 1;
-      if (root >= 0 && (threadIdx.x & 31) == leader) atomicAdd(sizes + root, __popc(peers));
+  }
+  __syncthreads();
+  // chase (divergent) first; warp-wide matching only once the warp has
+  // reconverged
+  int fin[2 * kRowsPerWarp], term[2 * kRowsPerWarp];
+#pragma unroll
+  for (int k = 0; k < 2 * kRowsPerWarp; ++k) {
+    const int r = r0 + (k >> 1), c = lane + 32 * (k & 1);
+    int x = -1;
+    if (r < th && c < tw) {
+      x = r * TW + c;
+      for (unsigned hop = 0; res[x] < 0; ++hop) {
+        const int nx = local_of(ent[x], off, W, tx0, ty0, tw, th);
+        if (nx < 0 || hop >= TH * TW) {   // cannot happen for a consistent forest
+          set_status(status, SPLIT_ERR_NOT_CONVERGED);
+          break;
+        }
+        x = nx;
+      }
+    }
+    term[k] = x;
+    fin[k] = (x >= 0 && res[x] >= 0) ? res[x] : -1;
+  }
+  __syncwarp();
+  if (sizes) {
+#pragma unroll
+    for (int k = 0; k < 2 * kRowsPerWarp; ++k) {
+      const unsigned peers = __match_any_sync(kFull, term[k]);
+      if (term[k] >= 0 && lane == __ffs(peers) - 1) atomicAdd(&cnt[term[k]], __popc(peers));
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < 2 * kRowsPerWarp; ++k) {
+    const int r = r0 + (k >> 1), c = lane + 32 * (k & 1);
+    if (r < th && c < tw) {
+      const int i = r * TW + c;
+      __stcg(P + off + (long long)(ty0 + r) * W + tx0 + c, fin[k]);
+      if (sizes && cnt[i] > 0) atomicAdd(sizes + res[i], cnt[i]);
     }
   }
 }
@@ -259,7 +492,8 @@ static int run(const int32_t* in, const Geoms& gs, int32_t* out, int32_t* sizes,
                cudaStream_t st) {
   tile_kernel<MAXC, CONN><<<gs.total_tiles, kThreads, 0, st>>>(in, gs, out, sizes, &hdr->status);
   SG_TRY(launch_status());
-  border_kernel<MAXC, CONN><<<gs.total_tiles, kThreads, 0, st>>>(in, gs, out, &hdr->status);
+  border_kernel<MAXC, CONN><<<gs.total_tiles, kBorderThreads, 0, st>>>(in, gs, out,
+                                                                      &hdr->status);
   SG_TRY(launch_status());
   flatten_kernel<<<gs.total_tiles, kThreads, 0, st>>>(out, gs, sizes, &hdr->status);
   return launch_status();

@@ -82,5 +82,8 @@ def test_cpp_sample_pipeline_matches_oracle(tmp_path, cuda):
     assert np.array_equal(eroded, oracle.erode(merged, 1))
     nrm = _read(out, "normals.f32", np.float32, (3, n))
     ref_n = oracle.sobel_normals_f64(feats[0].reshape(h, w), 1.0)
-    cosang = np.clip(np.sum(nrm.astype(np.float64) * ref_n.reshape(3, n), axis=0), -1.0, 1.0)
-    assert np.arccos(cosang).max() <= 1e-4
+    got = nrm.astype(np.float64)
+    ref_n = ref_n.reshape(3, n)
+    # angle from atan2(|a x b|, a . b): well conditioned near zero
+    ang = np.arctan2(np.linalg.norm(np.cross(got.T, ref_n.T), axis=1), (got * ref_n).sum(0))
+    assert ang.max() <= 1e-4
