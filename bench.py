@@ -19,6 +19,7 @@ path has no cross-image exchange), reports the whole-job rate.
 from __future__ import annotations
 
 import argparse
+import dataclasses
 import json
 import os
 import statistics
@@ -470,8 +471,17 @@ def main():
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=dev)
 
-    from split_gb300 import _native, pipeline
+    from split_gb300 import _native, pipeline, tune
     _native.load()
+    # launch choices of this GPU: the cached table, else measured now
+    t_tune = time.perf_counter()
+    if tune.ensure(dev) is not None:
+        tuning = {"source": "cache"}
+    else:
+        _, detail = tune.autotune(dev)
+        tuning = {"source": "measured", "seconds": round(time.perf_counter() - t_tune, 2),
+                  "timings_ms": detail}
+    tuning["table"] = [dataclasses.asdict(e) for e in tune.current()]
     W, H = args.width, args.height
     npx = W * H
     rgb_np, c0_np = make_image(W, H, SEED + rank)
@@ -595,6 +605,7 @@ def main():
             "batched": batched,
             "serving": serving,
             "stress": stress,
+            "tuning": tuning,
             "wall_s_timed_region": round(t_wall, 3),
         }
         print(json.dumps(line), flush=True)

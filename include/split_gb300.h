@@ -345,6 +345,33 @@ int split_batch_run(split_batch* batch, void* stream);
 /* Kernels launched by this library since it was loaded (all entry points). */
 unsigned long long split_launch_count(void);
 
+/* ======================================================================== */
+/* tuning table (no counterpart in the reference)                           */
+/* ======================================================================== */
+
+/* Launch choices per image size class, filled by an autotuner
+ * (split_gb300/tune.py measures the candidates on the current GPU and caches
+ * the winners).  An image uses the first entry whose max_pixels is at least
+ * its pixel count; with no such entry (or an empty table) the defaults
+ * apply: 64-row k-means units, as many resident blocks per SM as fit.
+ * The unit height is chosen from each image's own size, so an image gets the
+ * same reduction tree (and bit-identical results) alone, in a pipeline and
+ * in a batch.  Results differ between unit heights only by FP32 rounding of
+ * the centroid sums.  Changing the table between sizing a batch and binding
+ * it is allowed (workspaces are sized for the smallest unit height). */
+#define SPLIT_TUNE_MAX_ENTRIES 64
+typedef struct {
+  int64_t max_pixels;        /* upper bound of the class (entries ascending) */
+  int kmeans_unit_rows;      /* 64 or 128: rows of a k-means work unit       */
+  int kmeans_blocks_per_sm;  /* 0 = as many as fit, else 1..8 (capped)       */
+} split_tune_entry;
+
+/* Replaces the table (n = 0 restores the defaults).  Rejects unsorted
+ * classes and values outside the ranges above. */
+int split_tune_set(const split_tune_entry* entries, int n);
+/* Copies up to `capacity` entries; returns the table's length. */
+int split_tune_get(split_tune_entry* out, int capacity);
+
 #ifdef __cplusplus
 }
 #endif

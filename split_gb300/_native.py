@@ -54,6 +54,8 @@ _SIGS = {
     "split_pipeline_workspace_size": (_sz, [_i32, _i32, _vp]),
     "split_pipeline_run": (_i32, [_vp, _i32, _i32, _vp, _vp, _vp, _vp, _vp, _vp, _sz, _vp, _vp]),
     "split_launch_count": (C.c_ulonglong, []),
+    "split_tune_set": (C.c_int, [C.c_void_p, C.c_int]),
+    "split_tune_get": (C.c_int, [C.c_void_p, C.c_int]),
     "split_batch_create": (_i32, [_vp, _i32, _vp, _vp]),
     "split_batch_destroy": (None, [_vp]),
     "split_batch_workspace_size": (_sz, [_vp]),
@@ -86,6 +88,15 @@ class BatchImage(C.Structure):
     """split_batch_image (include/split_gb300.h)."""
     _fields_ = [("width", C.c_int), ("height", C.c_int), ("nclusters", C.c_int),
                 ("kmeans_iters", C.c_int)]
+
+
+class TuneEntry(C.Structure):
+    """split_tune_entry (include/split_gb300.h)."""
+    _fields_ = [("max_pixels", C.c_int64), ("kmeans_unit_rows", C.c_int),
+                ("kmeans_blocks_per_sm", C.c_int)]
+
+
+TUNE_MAX_ENTRIES = 64
 
 
 class SplitError(RuntimeError):

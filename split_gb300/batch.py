@@ -21,6 +21,8 @@ class Batch:
         self.shapes = [tuple(int(v) for v in s) for s in shapes]
         self.device = torch.device("cuda", torch.cuda.current_device()) if device is None \
             else torch.device(device)
+        from . import tune
+        tune.ensure_once(self.device)   # this GPU's cached launch choices, if any
         arr = (N.BatchImage * len(self.shapes))(*[N.BatchImage(*s) for s in self.shapes])
         h = C.c_void_p()
         cp = self.params.c()

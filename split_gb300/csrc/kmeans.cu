@@ -20,6 +20,9 @@
 #include <math.h>
 #include <string.h>
 
+#include <mutex>
+#include <vector>
+
 #include "common.cuh"
 
 namespace sg {
@@ -33,10 +36,10 @@ namespace km {
 #endif
 constexpr int kThreads = 256;
 constexpr int kWarps = kThreads / 32;
-// A unit is a kTile x kTile pixel tile; warp w owns rows [8w, 8w + 8) of it.
+// A unit is a tile of unit_rows x kTile pixels (unit_rows = 64 or 128, per
+// image from the tuning table); warp w owns rows [w * r, (w + 1) * r) of it,
+// r = unit_rows / 8.
 constexpr int kTile = 64;
-constexpr int kUnit = kTile * kTile;   // pixels per unit
-constexpr int kWarpRows = kTile / kWarps;
 constexpr int kGroup = SG_KM_GROUP;    // units per group
 constexpr int kMaxK = 64;
 constexpr int kMaxDim = 5;
@@ -64,6 +67,7 @@ struct Image {
   int ngroups;
   int height;               // rows (ceil(npoints / width))
   int ntx;                  // tiles per row of tiles
+  int unit_rows;            // rows of a unit (kTile or 2 * kTile, from the tuning table)
 };
 
 struct ImageState {
@@ -86,6 +90,7 @@ struct Params {
   unsigned* image_cnt;   // [nimages]
   ImageState* state;     // [nimages]
   WsHeader* hdr;
+  int blocks_per_sm;     // 0: as many as fit (host side only)
 };
 
 constexpr int cstride(int dim) { return dim == 3 ? 4 : 8; }
@@ -283,7 +288,7 @@ __device__ __forceinline__ float2 ffma2(float2 a, float2 b, float2 c) {
 constexpr int kPx = 4;                 // consecutive pixels per lane
 constexpr int kLanesPerRow = kTile / kPx;  // 16 lanes cover a tile row
 constexpr int kBatchRows = 32 / kLanesPerRow;
-static_assert(kWarpRows % kBatchRows == 0, "whole batches per warp span");
+static_assert((kTile / kWarps) % kBatchRows == 0, "whole batches per warp span");
 
 // The lane's kPx consecutive pixels of image row `row` starting at column
 // `col`; ok[j] marks pixels inside the image.
@@ -402,12 +407,13 @@ __device__ void process_unit(const Image& im, int unit, Smem& sm, bool write_lab
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   constexpr int CS = cstride(DIM);
   constexpr bool kXY = DIM == 5 && LAYOUT != SPLIT_LAYOUT_PLANAR;
+  const int wrows = im.unit_rows / kWarps;
   const int ty = unit / im.ntx, tx = unit - ty * im.ntx;
-  const int row0 = ty * kTile + warp * kWarpRows;
+  const int row0 = ty * im.unit_rows + warp * wrows;
   const int col0 = tx * kTile;
   if (row0 >= im.height) return;
   const int lrow = lane / kLanesPerRow, lcol = (lane % kLanesPerRow) * kPx;
-  const int rows_in = min(kWarpRows, im.height - row0);
+  const int rows_in = min(wrows, im.height - row0);
   const int cols_in = min(kTile, im.width - col0);
   const bool unit_box = kXY && (LAYOUT == SPLIT_LAYOUT_RGB8 || im.unit_range);
   const bool vec_labels =
@@ -434,7 +440,7 @@ __device__ void process_unit(const Image& im, int unit, Smem& sm, bool write_lab
 #pragma unroll
   for (int d = 0; d < DIM; ++d) acc[d] = 0.0f;
 
-  for (int b = 0; b < kWarpRows / kBatchRows; ++b) {
+  for (int b = 0; b < wrows / kBatchRows; ++b) {
     if (b * kBatchRows >= rows_in) break;
     const int row = row0 + b * kBatchRows + lrow;
     const int col = col0 + lcol;
@@ -803,8 +809,8 @@ struct Layout {
 
 inline int height_of(int64_t n, int width) { return (int)((n + width - 1) / width); }
 inline int tiles_x(int width) { return (width + kTile - 1) / kTile; }
-inline int units_of(int64_t n, int width) {
-  return tiles_x(width) * ((height_of(n, width) + kTile - 1) / kTile);
+inline int units_of(int64_t n, int width, int rows = kTile) {
+  return tiles_x(width) * ((height_of(n, width) + rows - 1) / rows);
 }
 inline int groups_of(int units) { return (units + kGroup - 1) / kGroup; }
 
@@ -851,6 +857,26 @@ __global__ void load_user_centroids(Params p) {
   }
 }
 
+// ---- tuning table (host side) ----------------------------------------------
+// Per image size class: the unit height and the resident blocks per SM of
+// the cooperative launch.  A unit height is chosen from the image's own pixel
+// count, so an image gets the same reduction tree alone and in a batch.
+struct TuneTable {
+  std::mutex m;
+  std::vector<split_tune_entry> e;
+};
+static TuneTable& tune_table() {
+  static TuneTable t;
+  return t;
+}
+split_tune_entry tuned(int64_t npix) {
+  TuneTable& t = tune_table();
+  std::lock_guard<std::mutex> g(t.m);
+  for (const split_tune_entry& x : t.e)
+    if (npix <= x.max_pixels) return x;
+  return split_tune_entry{INT64_MAX, kTile, 0};
+}
+
 template <int LAYOUT, int DIM, int MODE>
 static int launch(Params& p, cudaStream_t st) {
   DeviceInfo di;
@@ -859,6 +885,7 @@ static int launch(Params& p, cudaStream_t st) {
   int per_sm = 0;
   SG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kThreads, 0));
   if (per_sm < 1) return SPLIT_ERR_UNSUPPORTED;
+  if (p.blocks_per_sm > 0 && p.blocks_per_sm < per_sm) per_sm = p.blocks_per_sm;
   int grid = di.sm_count * per_sm;
   if (grid > p.total_units) grid = p.total_units > 0 ? p.total_units : 1;
   if (MODE == kAssignOnly) {
@@ -904,7 +931,8 @@ static int run(int mode, const void* points, int layout, int dim, int64_t n,
   if (!valid_features(points, layout, dim, n, width, K)) return SPLIT_ERR_INVALID;
   const int unit_range = (layout & SPLIT_FEATURES_UNIT_RANGE) ? 1 : 0;
   layout &= ~SPLIT_FEATURES_UNIT_RANGE;
-  const int units = units_of(n, width), groups = groups_of(units);
+  const split_tune_entry te = tuned(n);
+  const int units = units_of(n, width, te.kmeans_unit_rows), groups = groups_of(units);
   Layout l = carve(nullptr, units, groups, 1);
   if (!ws || ws_bytes < l.bytes || (reinterpret_cast<uintptr_t>(ws) & 255))
     return SPLIT_ERR_WORKSPACE;
@@ -927,8 +955,10 @@ static int run(int mode, const void* points, int layout, int dim, int64_t n,
   im.nunits = units;
   im.height = height_of(n, width);
   im.ntx = tiles_x(width);
+  im.unit_rows = te.kmeans_unit_rows;
   im.group_begin = 0;
   im.ngroups = groups;
+  p.blocks_per_sm = te.kmeans_blocks_per_sm;
   p.nimages = 1;
   p.images = nullptr;
   p.total_units = units;
@@ -1113,7 +1143,9 @@ extern "C" int split_kmeans_cluster_noalloc(const void* points, int layout, int 
                                             void* stream) {
   using namespace sg::km;
   if (!centroids || !labels || npoints <= 0 || width < 1) return SPLIT_ERR_INVALID;
-  const int units = units_of(npoints, width), groups = groups_of(units);
+  // the units run() will use (tuned height, never below 64 rows)
+  const int units = units_of(npoints, width, tuned(npoints).kmeans_unit_rows);
+  const int groups = groups_of(units);
   if (units > kStaticTiles) return SPLIT_ERR_WORKSPACE;
   const size_t need = carve(nullptr, units, groups, 1).bytes;
   if (need > kStaticBytes) return SPLIT_ERR_WORKSPACE;
@@ -1150,10 +1182,13 @@ namespace kmb {
 struct BatchCounts {
   int units, groups;
 };
-BatchCounts batch_counts(const KmBatchImage* imgs, int n) {
+// Unit and group totals; sized (for the workspace) at the smallest unit
+// height, which needs the most records, or at each image's tuned height.
+BatchCounts batch_counts(const KmBatchImage* imgs, int n, bool tuned_rows) {
   BatchCounts c{0, 0};
   for (int i = 0; i < n; ++i) {
-    const int u = km::units_of(imgs[i].npoints, imgs[i].width);
+    const int rows = tuned_rows ? km::tuned(imgs[i].npoints).kmeans_unit_rows : km::kTile;
+    const int u = km::units_of(imgs[i].npoints, imgs[i].width, rows);
     c.units += u;
     c.groups += km::groups_of(u);
   }
@@ -1164,7 +1199,7 @@ using kmb::BatchCounts;
 using kmb::batch_counts;
 
 size_t kmeans_batch_workspace(const KmBatchImage* imgs, int nimages) {
-  const BatchCounts c = batch_counts(imgs, nimages);
+  const BatchCounts c = batch_counts(imgs, nimages, false);
   return km::carve(nullptr, c.units, c.groups, nimages > 1 ? nimages : 2).bytes;
 }
 
@@ -1175,7 +1210,7 @@ int kmeans_batch_prepare(const KmBatchImage* imgs, int nimages, int layout, int 
   if (!imgs || nimages < 1 || (dim != 3 && dim != 5)) return SPLIT_ERR_INVALID;
   const int unit_range = (layout & SPLIT_FEATURES_UNIT_RANGE) ? 1 : 0;
   layout &= ~SPLIT_FEATURES_UNIT_RANGE;
-  const BatchCounts c = batch_counts(imgs, nimages);
+  const BatchCounts c = batch_counts(imgs, nimages, true);
   const int slots = nimages > 1 ? nimages : 2;
   Layout l = carve(nullptr, c.units, c.groups, slots);
   if (!ws || ws_bytes < l.bytes || (reinterpret_cast<uintptr_t>(ws) & 255))
@@ -1183,6 +1218,7 @@ int kmeans_batch_prepare(const KmBatchImage* imgs, int nimages, int layout, int 
   l = carve(ws, c.units, c.groups, slots);
   std::vector<Image> host(nimages);
   int ub = 0, gb = 0, max_iter = 0;
+  int64_t total_px = 0;
   for (int i = 0; i < nimages; ++i) {
     const KmBatchImage& b = imgs[i];
     if (!valid_features(b.points, layout, dim, b.npoints, b.width, b.nclusters) || !b.centroids ||
@@ -1201,7 +1237,9 @@ int kmeans_batch_prepare(const KmBatchImage* imgs, int nimages, int layout, int 
     im.max_iter = b.iters;
     im.threshold = b.threshold;
     im.unit_begin = ub;
-    im.nunits = units_of(b.npoints, b.width);
+    im.unit_rows = tuned(b.npoints).kmeans_unit_rows;
+    im.nunits = units_of(b.npoints, b.width, im.unit_rows);
+    total_px += b.npoints;
     im.group_begin = gb;
     im.ngroups = groups_of(im.nunits);
     im.height = height_of(b.npoints, b.width);
@@ -1220,6 +1258,7 @@ int kmeans_batch_prepare(const KmBatchImage* imgs, int nimages, int layout, int 
   plan->max_iter = max_iter;
   plan->layout = layout;
   plan->dim = dim;
+  plan->blocks_per_sm = tuned(total_px).kmeans_blocks_per_sm;
   return SPLIT_OK;
 }
 
@@ -1239,6 +1278,7 @@ int kmeans_batch_run(const KmBatchPlan& plan, void* ws, cudaStream_t st) {
   p.image_cnt = l.image_cnt;
   p.state = l.state;
   p.hdr = l.hdr;
+  p.blocks_per_sm = plan.blocks_per_sm;
   SG_CUDA_TRY(cudaMemsetAsync(reinterpret_cast<char*>(l.hdr) + sizeof(int), 0,
                               sizeof(unsigned) * 4, st));
   SG_CUDA_TRY(cudaMemsetAsync(l.group_cnt, 0, sizeof(unsigned) * (size_t)plan.groups, st));
@@ -1253,3 +1293,29 @@ int kmeans_batch_run(const KmBatchPlan& plan, void* ws, cudaStream_t st) {
 }
 
 }  // namespace sg
+
+// ---------------------------------------------------------------------------
+// Tuning table C API
+// ---------------------------------------------------------------------------
+extern "C" int split_tune_set(const split_tune_entry* entries, int n) {
+  if (n < 0 || n > SPLIT_TUNE_MAX_ENTRIES || (n > 0 && !entries)) return SPLIT_ERR_INVALID;
+  for (int i = 0; i < n; ++i) {
+    const split_tune_entry& e = entries[i];
+    if (e.max_pixels <= 0 || (i > 0 && e.max_pixels <= entries[i - 1].max_pixels))
+      return SPLIT_ERR_INVALID;
+    if (e.kmeans_unit_rows != 64 && e.kmeans_unit_rows != 128) return SPLIT_ERR_INVALID;
+    if (e.kmeans_blocks_per_sm < 0 || e.kmeans_blocks_per_sm > 8) return SPLIT_ERR_INVALID;
+  }
+  sg::km::TuneTable& t = sg::km::tune_table();
+  std::lock_guard<std::mutex> g(t.m);
+  t.e.assign(entries, entries + n);
+  return SPLIT_OK;
+}
+
+extern "C" int split_tune_get(split_tune_entry* out, int capacity) {
+  sg::km::TuneTable& t = sg::km::tune_table();
+  std::lock_guard<std::mutex> g(t.m);
+  const int n = (int)t.e.size();
+  for (int i = 0; i < n && i < capacity && out; ++i) out[i] = t.e[i];
+  return n;
+}

@@ -23,6 +23,7 @@ struct KmBatchImage {
 
 struct KmBatchPlan {
   int nimages, units, groups, max_iter, layout, dim;
+  int blocks_per_sm;   // from the tuning table (0: as many as fit)
 };
 
 size_t kmeans_batch_workspace(const KmBatchImage* imgs, int nimages);

@@ -42,6 +42,8 @@ class Pipeline:
         self.width, self.height, self.params = width, height, params
         self.device = torch.device("cuda", torch.cuda.current_device()) if device is None \
             else torch.device(device)
+        from . import tune
+        tune.ensure_once(self.device)   # this GPU's cached launch choices, if any
         self._cp = params.c()
         nbytes = N.load().split_pipeline_workspace_size(width, height, C.byref(self._cp))
         if nbytes == 0:
