@@ -7,15 +7,17 @@
 // matrix, the radix sort per iteration or the host round trip per iteration.
 //
 // Work decomposition (fixed per image, so a result never depends on what else
-// shares the launch): an image is cut into units of kUnit pixels; units are
-// grouped kGroup at a time.  Blocks take units from a device work counter.
-// Per unit, every warp accumulates (x - c_label) over its 32-pixel batches in
+// shares the launch): an image is cut into units (tiles of 64 or 128 rows by
+// 64 columns); blocks take units from a device work counter.  Per unit, every
+// warp accumulates (x - c_label) over its pixel batches in FP32 registers and
 // a warp-private shared-memory slot (warp butterfly sums per distinct label),
-// the block sums the 8 warp slots in warp order and writes the unit partial.
-// The last block to finish a unit of a group sums the group's unit partials in
-// unit order; the last block to finish a group of an image sums the group
-// partials in group order and forms c_new = c + S / n.  All sums therefore
-// have one fixed shape: the update is bit-reproducible.
+// and the block sums the 8 warp slots in warp order: the unit partial, a
+// fixed-shape FP32 sum.  Unit partials are added into per-image accumulators
+// exactly: each is rounded to a multiple of 2^-24 and added as a 96-bit
+// fixed-point integer (64-bit atomics on a low and a high word).  Integer
+// addition does not depend on order, so the image total is the same whatever
+// order units finish in and whatever else shares the launch.  The last unit
+// of an image forms c_new = c + S / n in FP64, rounded to FP32.
 #include <limits.h>
 #include <math.h>
 #include <string.h>
@@ -28,9 +30,6 @@
 namespace sg {
 namespace km {
 
-#ifndef SG_KM_GROUP
-#define SG_KM_GROUP 32
-#endif
 #ifndef SG_KM_MINBLOCKS
 #define SG_KM_MINBLOCKS 3
 #endif
@@ -40,11 +39,14 @@ constexpr int kWarps = kThreads / 32;
 // image from the tuning table); warp w owns rows [w * r, (w + 1) * r) of it,
 // r = unit_rows / 8.
 constexpr int kTile = 64;
-constexpr int kGroup = SG_KM_GROUP;    // units per group
 constexpr int kMaxK = 64;
 constexpr int kMaxDim = 5;
-// partial record: kMaxK * kMaxDim float sums then kMaxK int counts
-constexpr int kRec = kMaxK * kMaxDim + kMaxK;
+// Unit partials are added into the image accumulators as multiples of
+// 2^-24; a partial must stay below 2^38 in magnitude (a unit holds at most
+// 8192 pixels, so |x - c| below 3e7 everywhere).  Beyond it the call reports
+// SPLIT_ERR_OVERFLOW.
+constexpr float kFixScale = 16777216.0f;   // 2^24
+constexpr float kFixLimit = 274877906944.0f;   // 2^38
 
 enum Mode { kCluster = 0, kUpdateOnly = 1, kAssignOnly = 2 };
 
@@ -63,8 +65,6 @@ struct Image {
   int32_t* d_iterations;
   int unit_begin;
   int nunits;
-  int group_begin;
-  int ngroups;
   int height;               // rows (ceil(npoints / width))
   int ntx;                  // tiles per row of tiles
   int unit_rows;            // rows of a unit (kTile or 2 * kTile, from the tuning table)
@@ -83,11 +83,11 @@ struct Params {
   int nimages;
   int total_units;
   int max_iter;
-  float* unit_part;      // [total_units][kRec]
-  float* group_part;     // [total_groups][kRec]
-  float* cur;            // [2][nimages][kMaxK * 8]
-  unsigned* group_cnt;   // [total_groups]
-  unsigned* image_cnt;   // [nimages]
+  unsigned long long* acc_lo;  // [nimages][kMaxK * kMaxDim] low 32-bit words of the sums
+  unsigned long long* acc_hi;  // [nimages][kMaxK * kMaxDim] high words (signed)
+  unsigned* acc_cnt;           // [nimages][kMaxK] member counts
+  float* cur;                  // [2][nimages][kMaxK * 8]
+  unsigned* image_cnt;         // [nimages] units finished this iteration
   ImageState* state;     // [nimages]
   WsHeader* hdr;
   int blocks_per_sm;     // 0: as many as fit (host side only)
@@ -231,13 +231,8 @@ __device__ __forceinline__ float warp_sum(float v) {
   return v;
 }
 
-constexpr int kChunk = 8;     // records summed per thread in one pass
-constexpr int kChunks = 8;    // chunks per pass (64 records per pass)
-constexpr int kVals = kMaxK * kMaxDim + kMaxK;
-
 struct Smem {
   alignas(16) float cent[kMaxK * 8];
-  float scratch[kChunks][kVals];
   float acc[kWarps][kMaxK * kMaxDim];
   int cnt[kWarps][kMaxK];
   float lut[256];
@@ -566,8 +561,13 @@ __device__ void process_unit(const Image& im, int unit, Smem& sm, bool write_lab
 }
 
 // Sum the warp slots in warp order into a unit record; clear the slots.
-__device__ void block_to_record(Smem& sm, float* rec, int K, int dim) {
+// Sums the block's 8 warp slots in warp order (the unit partial), clears
+// them, and adds the partial into the image accumulators (96-bit fixed point:
+// low 32 bits and the signed rest in two 64-bit words).
+__device__ void block_to_accum(Smem& sm, const Params& p, int img, int K, int dim) {
   __syncthreads();
+  unsigned long long* lo = p.acc_lo + (size_t)img * (kMaxK * kMaxDim);
+  unsigned long long* hi = p.acc_hi + (size_t)img * (kMaxK * kMaxDim);
   for (int idx = threadIdx.x; idx < K * kMaxDim; idx += blockDim.x) {
     float s = 0.0f;
 #pragma unroll
@@ -575,7 +575,12 @@ __device__ void block_to_record(Smem& sm, float* rec, int K, int dim) {
       s = __fadd_rn(s, sm.acc[w][idx]);
       sm.acc[w][idx] = 0.0f;
     }
-    if ((idx % kMaxDim) < dim) __stcg(rec + idx, s);
+    if ((idx % kMaxDim) < dim && s != 0.0f) {
+      if (!(fabsf(s) < kFixLimit)) set_status(&p.hdr->status, SPLIT_ERR_OVERFLOW);
+      const long long q = __float2ll_rn(__fmul_rn(s, kFixScale));
+      atomicAdd(lo + idx, (unsigned long long)q & 0xffffffffull);
+      atomicAdd(hi + idx, (unsigned long long)(q >> 32));
+    }
   }
   for (int k = threadIdx.x; k < K; k += blockDim.x) {
     int c = 0;
@@ -584,62 +589,8 @@ __device__ void block_to_record(Smem& sm, float* rec, int K, int dim) {
       c += sm.cnt[w][k];
       sm.cnt[w][k] = 0;
     }
-    __stcg(reinterpret_cast<int*>(rec + kMaxK * kMaxDim) + k, c);
+    if (c) atomicAdd(p.acc_cnt + (size_t)img * kMaxK + k, (unsigned)c);
   }
-}
-
-// Sum `count` records (stride kRec) into `out` with one fixed shape: records
-// are summed 8 at a time in order (all 8 loads in flight), the chunk sums of a
-// pass are then summed in chunk order, and the passes in pass order.  Value v
-// enumerates the K*dim float sums followed by the K counts.
-__device__ void sum_records(Smem& sm, const float* src, int count, float* out,
-                            int K, int dim) {
-  const int nv = K * dim + K;
-  for (int pass0 = 0; pass0 < count; pass0 += kChunk * kChunks) {
-    const int in_pass = min(count - pass0, kChunk * kChunks);
-    const int nch = (in_pass + kChunk - 1) / kChunk;
-    __syncthreads();
-    for (int w = threadIdx.x; w < nv * nch; w += blockDim.x) {
-      const int v = w % nv, c = w / nv;
-      const int r0 = pass0 + c * kChunk;
-      const int rn = min(kChunk, count - r0);
-      const bool is_cnt = v >= K * dim;
-      const int off = is_cnt ? kMaxK * kMaxDim + (v - K * dim)
-                             : (v / dim) * kMaxDim + (v % dim);
-      const float* s = src + (size_t)r0 * kRec + off;
-      float x[kChunk];
-#pragma unroll
-      for (int r = 0; r < kChunk; ++r) x[r] = r < rn ? __ldcg(s + (size_t)r * kRec) : 0.0f;
-      if (is_cnt) {
-        int a = 0;
-#pragma unroll
-        for (int r = 0; r < kChunk; ++r) a += __float_as_int(x[r]);
-        sm.scratch[c][v] = __int_as_float(a);
-      } else {
-        float a = x[0];
-#pragma unroll
-        for (int r = 1; r < kChunk; ++r) a = __fadd_rn(a, x[r]);
-        sm.scratch[c][v] = a;
-      }
-    }
-    __syncthreads();
-    for (int v = threadIdx.x; v < nv; v += blockDim.x) {
-      const bool is_cnt = v >= K * dim;
-      const int off = is_cnt ? kMaxK * kMaxDim + (v - K * dim)
-                             : (v / dim) * kMaxDim + (v % dim);
-      if (is_cnt) {
-        int a = pass0 ? __float_as_int(__ldcg(out + off)) : 0;
-        for (int c = 0; c < nch; ++c) a += __float_as_int(sm.scratch[c][v]);
-        __stcg(reinterpret_cast<int*>(out + off), a);
-      } else {
-        float a = sm.scratch[0][v];
-        for (int c = 1; c < nch; ++c) a = __fadd_rn(a, sm.scratch[c][v]);
-        if (pass0) a = __fadd_rn(__ldcg(out + off), a);
-        __stcg(out + off, a);
-      }
-    }
-  }
-  __syncthreads();
 }
 
 template <int DIM>
@@ -655,24 +606,38 @@ __device__ __forceinline__ void load_centroids(const float* src, int K,
 // Image-level finish: new centroids c + S / n (empty cluster: unchanged),
 // convergence test of cluster.cu:71-88, outputs on the last iteration.
 template <int DIM, int MODE>
-__device__ void finish_image(const Params& p, int img, const Image& im, int it,
-                             const float* total) {
+__device__ void finish_image(const Params& p, int img, const Image& im, int it) {
   __shared__ float sdelta;
   const float* c_old = p.cur + ((size_t)(it & 1) * p.nimages + img) * (kMaxK * 8);
   float* c_new = p.cur + ((size_t)((it + 1) & 1) * p.nimages + img) * (kMaxK * 8);
-  const int* cnt = reinterpret_cast<const int*>(total + kMaxK * kMaxDim);
+  unsigned long long* lo = p.acc_lo + (size_t)img * (kMaxK * kMaxDim);
+  unsigned long long* hi = p.acc_hi + (size_t)img * (kMaxK * kMaxDim);
+  unsigned* cnt = p.acc_cnt + (size_t)img * kMaxK;
   __shared__ float sdiff[kMaxK * kMaxDim];
   for (int idx = threadIdx.x; idx < im.K * DIM; idx += blockDim.x) {
-    const int k = idx / DIM, d = idx % DIM;
+    const int k = idx / DIM, d = idx % DIM, a = k * kMaxDim + d;
     const float c = __ldcg(c_old + k * 8 + d);
-    const int n = __ldcg(cnt + k);
+    const unsigned n = __ldcg(cnt + k);
     float cn = c;
-    if (n > 0) cn = __fadd_rn(c, __fdiv_rn(__ldcg(total + k * kMaxDim + d), (float)n));
+    if (n > 0) {
+      // S = (hi * 2^32 + lo) * 2^-24, exact up to the final FP64 rounding
+      const double h = (double)(long long)__ldcg(hi + a);
+      const double l = (double)__ldcg(lo + a);
+      const double S = __dmul_rn(__dadd_rn(__dmul_rn(h, 4294967296.0), l), 1.0 / 16777216.0);
+      cn = __double2float_rn(__dadd_rn((double)c, __ddiv_rn(S, (double)n)));
+    }
     __stcg(c_new + k * 8 + d, cn);
     const float df = __fsub_rn(cn, c);
     sdiff[idx] = __fmul_rn(df, df);
   }
   __syncthreads();
+  // the accumulators start the next iteration at zero (every unit of this
+  // image has been added, and nothing adds to it before the grid barrier)
+  for (int idx = threadIdx.x; idx < im.K * kMaxDim; idx += blockDim.x) {
+    __stcg(lo + idx, 0ull);
+    __stcg(hi + idx, 0ull);
+  }
+  for (int k = threadIdx.x; k < im.K; k += blockDim.x) __stcg(cnt + k, 0u);
   if (threadIdx.x < 32) {
     // squared centroid shift, summed in a fixed order
     float acc = 0.0f;
@@ -747,43 +712,19 @@ __global__ void __launch_bounds__(kThreads, SG_KM_MINBLOCKS) kmeans_kernel(Param
                       (MODE == kCluster && (im.threshold >= 0.0f || it == im.max_iter - 1));
       process_unit<LAYOUT, DIM, MODE>(im, lu, sm, wl);
       if (MODE == kAssignOnly) continue;
-      float* rec = p.unit_part + (size_t)u * kRec;
-      block_to_record(sm, rec, im.K, DIM);
-      // publish the unit partial; the last unit of a group sums the group
-      __threadfence();
-      __syncthreads();
-      const int g = lu / kGroup;
-      const int gbeg = g * kGroup;
-      const int gcount = min(kGroup, im.nunits - gbeg);
-      if (threadIdx.x == 0) {
-        const unsigned prev = atomicAdd(&p.group_cnt[im.group_begin + g], 1u);
-        sm.flag = (prev == (unsigned)gcount - 1);
-        if (sm.flag) p.group_cnt[im.group_begin + g] = 0;
-      }
-      __syncthreads();
-      if (!sm.flag) continue;
-      __threadfence();
-      float* grec = p.group_part + (size_t)(im.group_begin + g) * kRec;
-      sum_records(sm, p.unit_part + (size_t)(im.unit_begin + gbeg) * kRec, gcount, grec,
-                  im.K, DIM);
+      block_to_accum(sm, p, img, im.K, DIM);
+      // the last unit of the image forms its new centroids
       __threadfence();
       __syncthreads();
       if (threadIdx.x == 0) {
         const unsigned prev = atomicAdd(&p.image_cnt[img], 1u);
-        sm.flag = (prev == (unsigned)im.ngroups - 1);
+        sm.flag = (prev == (unsigned)im.nunits - 1);
         if (sm.flag) p.image_cnt[img] = 0;
       }
       __syncthreads();
       if (!sm.flag) continue;
       __threadfence();
-      // image total into the unit record slot of the image's first unit
-      // (its partial was consumed by the group sum above)
-      float* tot = p.unit_part + (size_t)im.unit_begin * kRec;
-      __syncthreads();
-      sum_records(sm, p.group_part + (size_t)im.group_begin * kRec, im.ngroups, tot, im.K, DIM);
-      __threadfence();
-      __syncthreads();
-      finish_image<DIM, MODE>(p, img, im, it, tot);
+      finish_image<DIM, MODE>(p, img, im, it);
       __syncthreads();
     }
     if (MODE == kAssignOnly) break;
@@ -796,10 +737,10 @@ __global__ void __launch_bounds__(kThreads, SG_KM_MINBLOCKS) kmeans_kernel(Param
 // ---------------------------------------------------------------------------
 
 struct Layout {
-  float* unit_part;
-  float* group_part;
+  unsigned long long* acc_lo;
+  unsigned long long* acc_hi;
+  unsigned* acc_cnt;
   float* cur;
-  unsigned* group_cnt;
   unsigned* image_cnt;
   ImageState* state;
   Image* images;
@@ -812,21 +753,33 @@ inline int tiles_x(int width) { return (width + kTile - 1) / kTile; }
 inline int units_of(int64_t n, int width, int rows = kTile) {
   return tiles_x(width) * ((height_of(n, width) + rows - 1) / rows);
 }
-inline int groups_of(int units) { return (units + kGroup - 1) / kGroup; }
-
-static Layout carve(void* ws, int total_units, int total_groups, int nimages) {
+// The workspace holds per-image state only (accumulators, centroids, counters):
+// its size does not depend on the image sizes.
+static Layout carve(void* ws, int nimages) {
   Carver c(ws);
   Layout l;
   l.hdr = c.take<WsHeader>(1);
-  l.unit_part = c.take<float>((size_t)total_units * kRec);
-  l.group_part = c.take<float>((size_t)total_groups * kRec);
+  l.acc_lo = c.take<unsigned long long>((size_t)nimages * kMaxK * kMaxDim);
+  l.acc_hi = c.take<unsigned long long>((size_t)nimages * kMaxK * kMaxDim);
+  l.acc_cnt = c.take<unsigned>((size_t)nimages * kMaxK);
   l.cur = c.take<float>((size_t)2 * nimages * kMaxK * 8);
-  l.group_cnt = c.take<unsigned>((size_t)total_groups);
   l.image_cnt = c.take<unsigned>((size_t)nimages);
   l.state = c.take<ImageState>((size_t)nimages);
   l.images = nimages > 1 ? c.take<Image>((size_t)nimages) : nullptr;
   l.bytes = c.size();
   return l;
+}
+
+// Header words used by the barrier and the work counters, the accumulators
+// and the arrival counters start every call at zero (a call that stopped
+// early, or a workspace used by another call, may have left data there).
+static int reset_counters(const Layout& l, int nimages, cudaStream_t st) {
+  SG_CUDA_TRY(cudaMemsetAsync(reinterpret_cast<char*>(l.hdr) + sizeof(int), 0,
+                              sizeof(unsigned) * 4, st));
+  SG_CUDA_TRY(cudaMemsetAsync(l.acc_lo, 0, reinterpret_cast<char*>(l.cur) -
+                                               reinterpret_cast<char*>(l.acc_lo), st));
+  SG_CUDA_TRY(cudaMemsetAsync(l.image_cnt, 0, sizeof(unsigned) * (size_t)nimages, st));
+  return SPLIT_OK;
 }
 
 // Per-image iteration state (cluster.cu:65-68: delta = 0, old_delta =
@@ -932,11 +885,11 @@ static int run(int mode, const void* points, int layout, int dim, int64_t n,
   const int unit_range = (layout & SPLIT_FEATURES_UNIT_RANGE) ? 1 : 0;
   layout &= ~SPLIT_FEATURES_UNIT_RANGE;
   const split_tune_entry te = tuned(n);
-  const int units = units_of(n, width, te.kmeans_unit_rows), groups = groups_of(units);
-  Layout l = carve(nullptr, units, groups, 1);
+  const int units = units_of(n, width, te.kmeans_unit_rows);
+  Layout l = carve(nullptr, 1);
   if (!ws || ws_bytes < l.bytes || (reinterpret_cast<uintptr_t>(ws) & 255))
     return SPLIT_ERR_WORKSPACE;
-  l = carve(ws, units, groups, 1);
+  l = carve(ws, 1);
   Params p{};
   Image& im = p.img0;
   im.points = points;
@@ -956,27 +909,19 @@ static int run(int mode, const void* points, int layout, int dim, int64_t n,
   im.height = height_of(n, width);
   im.ntx = tiles_x(width);
   im.unit_rows = te.kmeans_unit_rows;
-  im.group_begin = 0;
-  im.ngroups = groups;
   p.blocks_per_sm = te.kmeans_blocks_per_sm;
   p.nimages = 1;
   p.images = nullptr;
   p.total_units = units;
   p.max_iter = max_iter;
-  p.unit_part = l.unit_part;
-  p.group_part = l.group_part;
+  p.acc_lo = l.acc_lo;
+  p.acc_hi = l.acc_hi;
+  p.acc_cnt = l.acc_cnt;
   p.cur = l.cur;
-  p.group_cnt = l.group_cnt;
   p.image_cnt = l.image_cnt;
   p.state = l.state;
   p.hdr = l.hdr;
-  // header words used by the barrier and the work counters start at zero,
-  // and so do the arrival counters (a workspace last used for another image
-  // size holds other data where they now sit)
-  SG_CUDA_TRY(cudaMemsetAsync(reinterpret_cast<char*>(l.hdr) + sizeof(int), 0,
-                              sizeof(unsigned) * 4, st));
-  SG_CUDA_TRY(cudaMemsetAsync(l.group_cnt, 0, sizeof(unsigned) * (size_t)groups, st));
-  SG_CUDA_TRY(cudaMemsetAsync(l.image_cnt, 0, sizeof(unsigned), st));
+  SG_TRY(reset_counters(l, 1, st));
   (void)centroids_in;
   init_kernel<<<1, 256, 0, st>>>(p);
   SG_TRY(launch_status());
@@ -999,8 +944,7 @@ extern "C" size_t split_kmeans_cluster_workspace_size_2d(int64_t npoints, int wi
   (void)nclusters;
   (void)dim;
   if (npoints <= 0 || width < 1) return 0;
-  const int u = km::units_of(npoints, width);
-  return km::carve(nullptr, u, km::groups_of(u), 1).bytes;
+  return km::carve(nullptr, 1).bytes;
 }
 
 extern "C" size_t split_kmeans_cluster_workspace_size(int64_t npoints, int nclusters, int dim) {
@@ -1084,9 +1028,10 @@ extern "C" int split_kmeans_propagate(const int32_t* labels, int64_t npoints,
 // file-scope device array of fixed size, so a call needs no workspace.
 //
 // Limits and sharing rules:
-//   - the image may span at most kStaticTiles 64 x 64 tiles (2048: a
-//     3840 x 2160 frame fits); larger images are rejected with
-//     SPLIT_ERR_WORKSPACE before anything is launched;
+//   - the array holds the state of one image (accumulators, centroids,
+//     counters: about 10 KB); the entry point supports images of at most
+//     kStaticTiles 64 x 64 tiles (2048: a 3840 x 2160 frame fits) and rejects
+//     larger ones with SPLIT_ERR_WORKSPACE before anything is launched;
 //   - every GPU that loads the library holds the array until the process
 //     exits; its device address is looked up once per device, on the first
 //     call made with that device current;
@@ -1100,16 +1045,16 @@ namespace sg {
 namespace km {
 
 constexpr int kStaticTiles = 2048;
-constexpr int kStaticGroups = (kStaticTiles + kGroup - 1) / kGroup;
 
-// Size of carve(ws, kStaticTiles, kStaticGroups, 1), evaluated at compile time.
+// Size of carve(ws, 1), evaluated at compile time (every piece starts on a
+// 256-byte boundary).
 constexpr size_t round256(size_t v) { return (v + 255) & ~size_t(255); }
 constexpr size_t kStaticBytes =
     round256(round256(round256(round256(round256(round256(round256(sizeof(WsHeader)) +
-                                                          (size_t)kStaticTiles * kRec * 4) +
-                                                 (size_t)kStaticGroups * kRec * 4) +
-                                        (size_t)2 * kMaxK * 8 * 4) +
-                               (size_t)kStaticGroups * 4) +
+                                                          (size_t)kMaxK * kMaxDim * 8) +
+                                                 (size_t)kMaxK * kMaxDim * 8) +
+                                        (size_t)kMaxK * 4) +
+                               (size_t)2 * kMaxK * 8 * 4) +
                       4) +
              sizeof(ImageState));
 
@@ -1144,21 +1089,15 @@ extern "C" int split_kmeans_cluster_noalloc(const void* points, int layout, int 
   using namespace sg::km;
   if (!centroids || !labels || npoints <= 0 || width < 1) return SPLIT_ERR_INVALID;
   // the units run() will use (tuned height, never below 64 rows)
-  const int units = units_of(npoints, width, tuned(npoints).kmeans_unit_rows);
-  const int groups = groups_of(units);
-  if (units > kStaticTiles) return SPLIT_ERR_WORKSPACE;
-  const size_t need = carve(nullptr, units, groups, 1).bytes;
-  if (need > kStaticBytes) return SPLIT_ERR_WORKSPACE;
+  if (units_of(npoints, width) > kStaticTiles) return SPLIT_ERR_WORKSPACE;
+  if (carve(nullptr, 1).bytes > kStaticBytes) return SPLIT_ERR_WORKSPACE;
   void* ws = nullptr;
   SG_TRY(static_scratch(&ws));
   cudaStream_t st = as_stream(stream);
-  // The array keeps the previous call's contents: the header (status word,
-  // barrier words, work counters) and the group / image arrival counters
-  // must start at zero.
-  Layout l = carve(ws, units, groups, 1);
+  // The array keeps the previous call's contents: the status word starts at
+  // zero here (run() clears the barrier words, counters and accumulators).
+  Layout l = carve(ws, 1);
   SG_CUDA_TRY(cudaMemsetAsync(l.hdr, 0, sizeof(WsHeader), st));
-  SG_CUDA_TRY(cudaMemsetAsync(l.group_cnt, 0, sizeof(unsigned) * (size_t)groups, st));
-  SG_CUDA_TRY(cudaMemsetAsync(l.image_cnt, 0, sizeof(unsigned), st));
   SG_TRY(run(kCluster, points, layout, dim, npoints, width, xy_scale, centroids, centroids,
              nclusters, labels, nullptr, ws, kStaticBytes, max_iter, threshold, d_iterations,
              st));
@@ -1180,17 +1119,16 @@ namespace sg {
 
 namespace kmb {
 struct BatchCounts {
-  int units, groups;
+  int units;
 };
 // Unit and group totals; sized (for the workspace) at the smallest unit
 // height, which needs the most records, or at each image's tuned height.
 BatchCounts batch_counts(const KmBatchImage* imgs, int n, bool tuned_rows) {
-  BatchCounts c{0, 0};
+  BatchCounts c{0};
   for (int i = 0; i < n; ++i) {
     const int rows = tuned_rows ? km::tuned(imgs[i].npoints).kmeans_unit_rows : km::kTile;
     const int u = km::units_of(imgs[i].npoints, imgs[i].width, rows);
     c.units += u;
-    c.groups += km::groups_of(u);
   }
   return c;
 }
@@ -1199,8 +1137,8 @@ using kmb::BatchCounts;
 using kmb::batch_counts;
 
 size_t kmeans_batch_workspace(const KmBatchImage* imgs, int nimages) {
-  const BatchCounts c = batch_counts(imgs, nimages, false);
-  return km::carve(nullptr, c.units, c.groups, nimages > 1 ? nimages : 2).bytes;
+  (void)batch_counts;
+  return km::carve(nullptr, nimages > 1 ? nimages : 2).bytes;
 }
 
 int kmeans_batch_prepare(const KmBatchImage* imgs, int nimages, int layout, int dim,
@@ -1212,12 +1150,12 @@ int kmeans_batch_prepare(const KmBatchImage* imgs, int nimages, int layout, int 
   layout &= ~SPLIT_FEATURES_UNIT_RANGE;
   const BatchCounts c = batch_counts(imgs, nimages, true);
   const int slots = nimages > 1 ? nimages : 2;
-  Layout l = carve(nullptr, c.units, c.groups, slots);
+  Layout l = carve(nullptr, slots);
   if (!ws || ws_bytes < l.bytes || (reinterpret_cast<uintptr_t>(ws) & 255))
     return SPLIT_ERR_WORKSPACE;
-  l = carve(ws, c.units, c.groups, slots);
+  l = carve(ws, slots);
   std::vector<Image> host(nimages);
-  int ub = 0, gb = 0, max_iter = 0;
+  int ub = 0, max_iter = 0;
   int64_t total_px = 0;
   for (int i = 0; i < nimages; ++i) {
     const KmBatchImage& b = imgs[i];
@@ -1240,12 +1178,9 @@ int kmeans_batch_prepare(const KmBatchImage* imgs, int nimages, int layout, int 
     im.unit_rows = tuned(b.npoints).kmeans_unit_rows;
     im.nunits = units_of(b.npoints, b.width, im.unit_rows);
     total_px += b.npoints;
-    im.group_begin = gb;
-    im.ngroups = groups_of(im.nunits);
     im.height = height_of(b.npoints, b.width);
     im.ntx = tiles_x(b.width);
     ub += im.nunits;
-    gb += im.ngroups;
     max_iter = max_iter > b.iters ? max_iter : b.iters;
   }
   SG_CUDA_TRY(cudaMemcpyAsync(l.images, host.data(), sizeof(Image) * nimages,
@@ -1254,7 +1189,6 @@ int kmeans_batch_prepare(const KmBatchImage* imgs, int nimages, int layout, int 
   SG_CUDA_TRY(cudaStreamSynchronize(st));
   plan->nimages = nimages;
   plan->units = c.units;
-  plan->groups = c.groups;
   plan->max_iter = max_iter;
   plan->layout = layout;
   plan->dim = dim;
@@ -1265,24 +1199,21 @@ int kmeans_batch_prepare(const KmBatchImage* imgs, int nimages, int layout, int 
 int kmeans_batch_run(const KmBatchPlan& plan, void* ws, cudaStream_t st) {
   using namespace km;
   const int slots = plan.nimages > 1 ? plan.nimages : 2;
-  Layout l = carve(ws, plan.units, plan.groups, slots);
+  Layout l = carve(ws, slots);
   Params p{};
   p.nimages = plan.nimages;
   p.images = l.images;  // a one-image batch reads its descriptor from the table too
   p.total_units = plan.units;
   p.max_iter = plan.max_iter;
-  p.unit_part = l.unit_part;
-  p.group_part = l.group_part;
+  p.acc_lo = l.acc_lo;
+  p.acc_hi = l.acc_hi;
+  p.acc_cnt = l.acc_cnt;
   p.cur = l.cur;
-  p.group_cnt = l.group_cnt;
   p.image_cnt = l.image_cnt;
   p.state = l.state;
   p.hdr = l.hdr;
   p.blocks_per_sm = plan.blocks_per_sm;
-  SG_CUDA_TRY(cudaMemsetAsync(reinterpret_cast<char*>(l.hdr) + sizeof(int), 0,
-                              sizeof(unsigned) * 4, st));
-  SG_CUDA_TRY(cudaMemsetAsync(l.group_cnt, 0, sizeof(unsigned) * (size_t)plan.groups, st));
-  SG_CUDA_TRY(cudaMemsetAsync(l.image_cnt, 0, sizeof(unsigned) * (size_t)plan.nimages, st));
+  SG_TRY(reset_counters(l, plan.nimages, st));
   init_kernel<<<1, 256, 0, st>>>(p);
   SG_TRY(launch_status());
   if (plan.dim == 3) load_user_centroids<3><<<1, 256, 0, st>>>(p);

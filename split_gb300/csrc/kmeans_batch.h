@@ -22,7 +22,7 @@ struct KmBatchImage {
 };
 
 struct KmBatchPlan {
-  int nimages, units, groups, max_iter, layout, dim;
+  int nimages, units, max_iter, layout, dim;
   int blocks_per_sm;   // from the tuning table (0: as many as fit)
 };
 
