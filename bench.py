@@ -451,6 +451,9 @@ def main():
     ap.add_argument("--serve-requests", type=int, default=1024)
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--no-stress", action="store_true")
+    ap.add_argument("--tune", default="auto", choices=["auto", "off"],
+                    help="auto: this GPU's cached launch table, else measure it now; "
+                         "off: the library defaults")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -475,7 +478,11 @@ def main():
     _native.load()
     # launch choices of this GPU: the cached table, else measured now
     t_tune = time.perf_counter()
-    if tune.ensure(dev) is not None:
+    if args.tune == "off":
+        tune.apply([])
+        tune._ensured.add(tune.device_key(dev))   # keep the defaults for this run
+        tuning = {"source": "defaults"}
+    elif tune.ensure(dev) is not None:
         tuning = {"source": "cache"}
     else:
         _, detail = tune.autotune(dev)
