@@ -977,7 +977,21 @@ extern "C" int split_kmeans_assign(const void* points, int layout, int dim, int6
                  workspace, workspace_bytes, 1, -1.0f, nullptr, as_stream(stream));
 }
 
+namespace sg {
+namespace segm {
+int run(const int32_t* labels, const void* points, int layout, int dim, int64_t n, int width,
+        float xy_scale, float* centroids, int K, void* ws, size_t ws_bytes, cudaStream_t st);
+size_t workspace_bytes(int K, int dim);
+}  // namespace segm
+}  // namespace sg
+
 extern "C" size_t split_kmeans_update_workspace_size(int64_t npoints, int nclusters, int dim) {
+  // more clusters than the k-means kernel holds in shared memory: per-cluster
+  // accumulators (16 B per feature value + a count)
+  if (nclusters > km::kMaxK) {
+    if (npoints <= 0 || dim < 1) return 0;
+    return segm::workspace_bytes(nclusters, dim);
+  }
   return split_kmeans_cluster_workspace_size(npoints, nclusters, dim);
 }
 
@@ -986,6 +1000,9 @@ extern "C" int split_kmeans_update(const int32_t* labels, const void* points, in
                                    float* centroids, int nclusters, void* workspace,
                                    size_t workspace_bytes, void* stream) {
   if (!centroids || !labels) return SPLIT_ERR_INVALID;
+  if (nclusters > km::kMaxK)
+    return segm::run(labels, points, layout, dim, npoints, width, xy_scale, centroids,
+                     nclusters, workspace, workspace_bytes, as_stream(stream));
   return km::run(km::kUpdateOnly, points, layout, dim, npoints, width, xy_scale, centroids,
                  centroids, nclusters, nullptr, labels, workspace, workspace_bytes, 1, -1.0f,
                  nullptr, as_stream(stream));
@@ -1250,3 +1267,178 @@ extern "C" int split_tune_get(split_tune_entry* out, int capacity) {
   for (int i = 0; i < n && i < capacity && out; ++i) out[i] = t.e[i];
   return n;
 }
+
+// ---------------------------------------------------------------------------
+// Centroids of many clusters (K > kMaxK): calculate_centroids on segment
+// labels (samples/src/main.cu:293-294, :306-307 call it with K = the number
+// of segments).  Per-cluster sums of the member features in the same 96-bit
+// fixed point as the k-means update (each feature rounded to a multiple of
+// 2^-24, low and high words added with 64-bit atomics), so the result is the
+// same whatever order pixels are added in.  A warp whose 32 pixels share one
+// label adds one warp sum; mixed warps add per pixel.  Means in FP64,
+// rounded to FP32; a cluster without members keeps its input centroid.
+// ---------------------------------------------------------------------------
+namespace sg {
+namespace segm {
+
+constexpr int kThreads = 256;
+
+struct Layout {
+  WsHeader* hdr;
+  unsigned long long* lo;   // [K][dim]
+  unsigned long long* hi;   // [K][dim]
+  unsigned* cnt;            // [K]
+  size_t bytes;
+};
+
+inline Layout carve(void* ws, int K, int dim) {
+  Carver c(ws);
+  Layout l;
+  l.hdr = c.take<WsHeader>(1);
+  l.lo = c.take<unsigned long long>((size_t)K * dim);
+  l.hi = c.take<unsigned long long>((size_t)K * dim);
+  l.cnt = c.take<unsigned>((size_t)K);
+  l.bytes = c.size();
+  return l;
+}
+
+__device__ __forceinline__ unsigned long long shfl_xor_u64(unsigned long long v, int o) {
+  const unsigned a = __shfl_xor_sync(0xffffffffu, (unsigned)v, o);
+  const unsigned b = __shfl_xor_sync(0xffffffffu, (unsigned)(v >> 32), o);
+  return ((unsigned long long)b << 32) | a;
+}
+
+template <int LAYOUT, int DIM>
+__global__ void __launch_bounds__(kThreads)
+accumulate_kernel(const int32_t* __restrict__ labels, const void* __restrict__ points,
+                  int64_t n, int width, float xy_scale, int K, Layout L) {
+  const int lane = threadIdx.x & 31;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  // every lane runs the same number of rounds (warp-wide shuffles below)
+  const int64_t rounds = (n + stride - 1) / stride;
+  for (int64_t r = 0; r < rounds; ++r) {
+    const int64_t i = r * stride + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    int l = -1;
+    float f[DIM];
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) f[d] = 0.0f;
+    if (i < n) {
+      l = __ldg(labels + i);
+      if (l < 0 || l >= K) l = -1;
+    }
+    if (l >= 0) {
+      if (LAYOUT == SPLIT_LAYOUT_FLOAT4) {
+        const float4 v = __ldg(static_cast<const float4*>(points) + i);
+        f[0] = v.x;
+        f[1] = v.y;
+        f[2] = v.z;
+      } else if (LAYOUT == SPLIT_LAYOUT_RGB8) {
+        const uint8_t* p = static_cast<const uint8_t*>(points) + 3 * i;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) f[c] = __fdiv_rn((float)__ldg(p + c), 255.0f);
+      } else {
+        const float* p = static_cast<const float*>(points);
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) f[d] = __ldg(p + (int64_t)d * n + i);
+      }
+      if (DIM == 5 && LAYOUT != SPLIT_LAYOUT_PLANAR) {
+        const int64_t row = i / width;
+        f[3] = __fmul_rn(xy_scale, (float)(i - row * width));
+        f[4] = __fmul_rn(xy_scale, (float)row);
+      }
+    }
+    unsigned long long qlo[DIM], qhi[DIM];
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) {
+      if (!(fabsf(f[d]) < 274877906944.0f)) set_status(&L.hdr->status, SPLIT_ERR_OVERFLOW);
+      const long long q = l >= 0 ? __float2ll_rn(__fmul_rn(f[d], 16777216.0f)) : 0ll;
+      qlo[d] = (unsigned long long)q & 0xffffffffull;
+      qhi[d] = (unsigned long long)(q >> 32);
+    }
+    const int l0 = __shfl_sync(0xffffffffu, l, 0);
+    if (__all_sync(0xffffffffu, l == l0) && l0 >= 0) {
+      // one label across the warp: butterfly sums, one set of atomics
+#pragma unroll
+      for (int d = 0; d < DIM; ++d) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+          qlo[d] += shfl_xor_u64(qlo[d], o);
+          qhi[d] += shfl_xor_u64(qhi[d], o);
+        }
+      }
+      if (lane == 0) {
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) {
+          atomicAdd(L.lo + (size_t)l0 * DIM + d, qlo[d]);
+          atomicAdd(L.hi + (size_t)l0 * DIM + d, qhi[d]);
+        }
+        atomicAdd(L.cnt + l0, 32u);
+      }
+    } else if (l >= 0) {
+#pragma unroll
+      for (int d = 0; d < DIM; ++d) {
+        atomicAdd(L.lo + (size_t)l * DIM + d, qlo[d]);
+        atomicAdd(L.hi + (size_t)l * DIM + d, qhi[d]);
+      }
+      atomicAdd(L.cnt + l, 1u);
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kThreads)
+finish_kernel(Layout L, int K, int dim, float* __restrict__ centroids) {
+  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < (int64_t)K * dim;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    const int k = (int)(idx / dim), d = (int)(idx - (int64_t)k * dim);
+    const unsigned nk = L.cnt[k];
+    if (nk == 0) continue;
+    const double h = (double)(long long)L.hi[idx];
+    const double l = (double)L.lo[idx];
+    const double S = __dmul_rn(__dadd_rn(__dmul_rn(h, 4294967296.0), l), 1.0 / 16777216.0);
+    centroids[(int64_t)d * K + k] = __double2float_rn(__ddiv_rn(S, (double)nk));
+  }
+}
+
+size_t workspace_bytes(int K, int dim) { return carve(nullptr, K, dim).bytes; }
+
+int run(const int32_t* labels, const void* points, int layout, int dim, int64_t n, int width,
+        float xy_scale, float* centroids, int K, void* ws, size_t ws_bytes, cudaStream_t st) {
+  layout &= ~SPLIT_FEATURES_UNIT_RANGE;
+  if (!labels || !points || !centroids || n <= 0 || n > 0x7fffffffLL || K < 1 || width < 1)
+    return SPLIT_ERR_INVALID;
+  if ((dim != 3 && dim != 5) || layout < SPLIT_LAYOUT_PLANAR || layout > SPLIT_LAYOUT_RGB8)
+    return SPLIT_ERR_INVALID;
+  if (layout == SPLIT_LAYOUT_FLOAT4 && (reinterpret_cast<uintptr_t>(points) & 15))
+    return SPLIT_ERR_INVALID;
+  Layout l = carve(nullptr, K, dim);
+  if (!ws || ws_bytes < l.bytes || (reinterpret_cast<uintptr_t>(ws) & 255))
+    return SPLIT_ERR_WORKSPACE;
+  l = carve(ws, K, dim);
+  SG_CUDA_TRY(cudaMemsetAsync(reinterpret_cast<char*>(l.hdr) + sizeof(int), 0,
+                              l.bytes - sizeof(int), st));
+  DeviceInfo di;
+  SG_TRY(device_info(&di));
+  int64_t blocks = (n + kThreads - 1) / kThreads;
+  const int64_t cap = (int64_t)di.sm_count * 8;
+  if (blocks > cap) blocks = cap;
+#define SG_SEG_CASE(LY, D)                                                                 \
+  if (layout == LY && dim == D) {                                                          \
+    accumulate_kernel<LY, D><<<(int)blocks, kThreads, 0, st>>>(labels, points, n, width,  \
+                                                               xy_scale, K, l);            \
+  }
+  SG_SEG_CASE(SPLIT_LAYOUT_PLANAR, 3)
+  SG_SEG_CASE(SPLIT_LAYOUT_PLANAR, 5)
+  SG_SEG_CASE(SPLIT_LAYOUT_FLOAT4, 3)
+  SG_SEG_CASE(SPLIT_LAYOUT_FLOAT4, 5)
+  SG_SEG_CASE(SPLIT_LAYOUT_RGB8, 3)
+  SG_SEG_CASE(SPLIT_LAYOUT_RGB8, 5)
+#undef SG_SEG_CASE
+  SG_TRY(launch_status());
+  int64_t fb = ((int64_t)K * dim + kThreads - 1) / kThreads;
+  if (fb > cap) fb = cap;
+  finish_kernel<<<(int)fb, kThreads, 0, st>>>(l, K, dim, centroids);
+  return launch_status();
+}
+
+}  // namespace segm
+}  // namespace sg

@@ -102,12 +102,17 @@ def calculate_centroids(labels: torch.Tensor, points: torch.Tensor, centroids: t
                         stream=None) -> Workspace:
     """split::device::kmeans::calculate_centroids (centroids.cuh:26-30).
 
-    Empty clusters keep their previous centroid (documented divergence)."""
+    Any number of clusters: up to 64 through the k-means kernel's update, more
+    (segment labels, K = number of segments) through per-cluster fixed-point
+    accumulators.  Empty clusters keep their previous centroid (documented
+    divergence); labels outside [0, K) are ignored."""
     n, d = _features(points, layout, dim)
     require_cuda(centroids, "centroids", torch.float32)
     require_cuda(labels, "labels", torch.int32)
     k = centroids.shape[1]
-    ws = ensure_workspace(temp, cluster_workspace_2d(n, width, k, d), points.device)
+    need = cluster_workspace_2d(n, width, k, d) if k <= 64 else \
+        calculate_centroids_workspace(n, k, d)
+    ws = ensure_workspace(temp, need, points.device)
     st = N.load().split_kmeans_update(ptr(labels), ptr(points), layout, d, n, width, xy_scale,
                                       ptr(centroids), k, ws.ptr, ws.nbytes,
                                       stream_handle(stream))

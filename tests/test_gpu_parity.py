@@ -339,3 +339,46 @@ def test_ccl_stress_8192_maze(cuda):
                 assert counts.max() > n * n // 3       # the serpentine corridor
                 assert len(roots) > 10 ** 4
     ws.check("ccl")
+
+
+@pytest.mark.parametrize("layout,dim", [(0, 3), (1, 3), (2, 3), (2, 5), (0, 5)])
+def test_segment_means_many_clusters(cuda, layout, dim):
+    """calculate_centroids with K = number of segments (thousands): per-segment
+    FP64 means of the member features within 1e-5 relative; empty segments
+    keep their input centroid; eroded (-1) pixels are ignored; the result
+    does not depend on the run (fixed-point sums)."""
+    import torch
+    from split_gb300 import kmeans
+    w, h = 517, 333
+    rgb = synth.voronoi_rgb8(88, w, h, 600, sigma=4.0)
+    feats = synth.features(rgb, dim)
+    seg = oracle.ccl(oracle.kmeans_assign_f32(
+        synth.features(rgb, 3), synth.pick_centroids(88, rgb, 8, 3)).reshape(h, w), 8, 0)
+    lab, nseg = oracle.compress_labels(seg)
+    lab = lab.reshape(-1).astype(np.int32)
+    lab[::97] = -1                          # eroded pixels
+    k = nseg + 5                            # a few empty clusters at the end
+    assert k > 64
+    c_in = np.random.default_rng(1).random((dim, k)).astype(np.float32)
+    if layout == 0:
+        pts = _t(feats, cuda)
+    elif layout == 1:
+        f4 = np.zeros((w * h, 4), np.float32)
+        f4[:, :3] = feats[:3].T
+        pts = _t(f4, cuda)
+    else:
+        pts = _t(rgb.reshape(-1, 3), cuda)
+    outs = []
+    for _ in range(2):
+        cent = _t(c_in, cuda)
+        kmeans.calculate_centroids(_t(lab, cuda), pts, cent, layout=layout, dim=dim, width=w)
+        outs.append(cent.cpu().numpy())
+    assert np.array_equal(outs[0], outs[1])
+    got = outs[0]
+    ref, cnt = oracle.kmeans_update_f64(lab, feats, c_in)
+    assert (cnt[nseg:] == 0).all() and (cnt > 0).sum() > 64
+    # clusters without members (the trailing ones, and segments whose pixels
+    # were all marked eroded) keep their input centroid exactly
+    np.testing.assert_array_equal(got[:, cnt == 0], c_in[:, cnt == 0])
+    rel = np.abs(got - ref) / np.maximum(np.abs(ref), 1e-30)
+    assert rel.max() <= 1e-5
