@@ -222,6 +222,25 @@ int split_merge_small(int32_t* labels, int width, int height, int P,
                       int policy, const float* chroma, const int32_t* d_sizes,
                       void* workspace, size_t workspace_bytes, void* stream);
 
+/* Replaces split::device::ccl::merge_smooth_boundaries_workspace
+ * (merge_smooth_boundaries.cuh:29-31). */
+size_t split_merge_smooth_workspace_size(int width, int height);
+
+/* Replaces split::device::ccl::merge_smooth_boundaries
+ * (merge_smooth_boundaries.cuh:20-25, merge_smooth_boundaries.cu:134-243).
+ * labels (in/out): segment ids in [0, w*h).  points: planar float features,
+ * at least 3 rows of w*h (rows 0..2 are read).  Every segment joins the
+ * 8-adjacent segment with the smallest mean |x_p - x_q| over their directed
+ * boundary edges (ties to the lowest id), among pairs with more than 15
+ * edges and mean below threshold * max_i |x_i|.  Mutual pairs keep the
+ * larger id; chains resolve to their end.  The reference file does not
+ * compile as written (its reduce_by_key takes a predicate as the
+ * reduction); this follows its documented intent.  The segment count the
+ * reference takes is not needed. */
+int split_merge_smooth(int32_t* labels, int width, int height, const float* points,
+                       float threshold, void* workspace, size_t workspace_bytes,
+                       void* stream);
+
 /* ======================================================================== */
 /* erosion / normals / feature preparation                                  */
 /* ======================================================================== */

@@ -259,6 +259,26 @@ inline void merge_small_segments(const_view2d<float> chrominance, view2d<int> la
         "ccl::merge_small_segments");
 }
 
+/* ccl/merge_smooth_boundaries.cuh:29-31 (segment and edge counts not needed). */
+inline std::size_t merge_smooth_boundaries_workspace(int npoints, int nsegments, int nedges,
+                                                     int width) {
+  (void)nsegments;
+  (void)nedges;
+  return split_merge_smooth_workspace_size(width, (npoints + width - 1) / width);
+}
+
+/* ccl/merge_smooth_boundaries.cuh:20-25.  points: planar (>= 3) x N. */
+inline void merge_smooth_boundaries(const_view2d<float> points, int nsegments,
+                                    view2d<int> labels, Temp& temp, float threshold = 0.01f,
+                                    cudaStream_t stream = nullptr) {
+  (void)nsegments;
+  const int w = (int)labels.num_cols(), h = (int)labels.num_rows();
+  temp.reserve(split_merge_smooth_workspace_size(w, h));
+  check(split_merge_smooth(labels.data(), w, h, points.data(), threshold, temp.get(),
+                           temp.size(), stream),
+        "ccl::merge_smooth_boundaries");
+}
+
 }  // namespace ccl
 
 /* ------------------------------------------------------------------- morph */

@@ -147,3 +147,18 @@ def canonical(labels: np.ndarray) -> np.ndarray:
     flat = np.asarray(labels).reshape(-1)
     _, first, inv = np.unique(flat, return_index=True, return_inverse=True)
     return first[inv].reshape(np.asarray(labels).shape).astype(np.int64)
+
+
+def merge_smooth(labels: np.ndarray, points: np.ndarray, threshold: float = 0.01) -> np.ndarray:
+    """(H, W) int32 segment ids in [0, H*W), planar (>= 3, H*W) float32
+    features -> merged labels (smooth-boundary rule)."""
+    a = _c(labels, np.int32).copy()
+    p = _c(points, np.float32)
+    h, w = a.shape
+    lib = _load()
+    lib.orc_merge_smooth.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_float]
+    lib.orc_merge_smooth.restype = C.c_int
+    rc = lib.orc_merge_smooth(_p(a), w, h, _p(p), float(threshold))
+    if rc:
+        raise RuntimeError(f"orc_merge_smooth failed ({rc})")
+    return a

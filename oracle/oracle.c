@@ -434,3 +434,121 @@ ORC_API void orc_luminance_f64(const uint8_t* rgb, int64_t n, double* lum) {
     lum[i] = (116.0 * fy - 16.0) / 100.0;
   }
 }
+
+/* ------------------------------------------------------------------------ */
+/* smooth-boundary merge                                                     */
+/* ------------------------------------------------------------------------ */
+/* Restates the documented behaviour of split/src/split/device/ccl/
+ * merge_smooth_boundaries.cu:134-243 (the file itself does not compile: its
+ * reduce_by_key is given thrust::less as the reduction):
+ *   directed 8-neighbour edges between different labels, image border
+ *   excluded (segment_adjacency.cu:112-142, :170-254); per pair (s, t) the
+ *   edge count and the mean of |x_p - x_q| over feature rows 0..2 (FP32
+ *   norm, VecNorm :25-35); pairs with mean >= D = threshold * max_i |x_i|
+ *   (:193-195) or with at most 15 edges (:197-205) dropped; each segment maps
+ *   to its candidate with the smallest (mean, id) (:207-226); mutual pairs
+ *   keep the larger id (fix_map_cycles.cuh:14-44); labels follow their chains
+ *   (map_until_converged.cuh:14-31).
+ * The pair sums are formed like the CUDA path's: every edge norm rounded to
+ * a multiple of 2^-32 and summed as an integer, the mean in double, rounded
+ * to float.  Sequential, sort-based.  Labels must lie in [0, w * h). */
+typedef struct {
+  int32_t s, t;
+  long long q;
+} SmEdge;
+
+static int sm_cmp(const void* a, const void* b) {
+  const SmEdge* x = (const SmEdge*)a;
+  const SmEdge* y = (const SmEdge*)b;
+  if (x->s != y->s) return x->s < y->s ? -1 : 1;
+  if (x->t != y->t) return x->t < y->t ? -1 : 1;
+  return 0;
+}
+
+static float sm_norm(const float* pts, int64_t n, int64_t p, int64_t q) {
+  float s = 0.0f;
+  for (int d = 0; d < 3; ++d) {
+    const float v = pts[d * n + p] - pts[d * n + q];
+    s = s + v * v;
+  }
+  return sqrtf(s);
+}
+
+ORC_API int orc_merge_smooth(int32_t* labels, int width, int height, const float* pts,
+                             float threshold) {
+  const int64_t n = (int64_t)width * height;
+  SmEdge* e = (SmEdge*)malloc(sizeof(SmEdge) * (size_t)(8 * n + 1));
+  int32_t* map = (int32_t*)malloc(sizeof(int32_t) * (size_t)n);
+  float* bestd = (float*)malloc(sizeof(float) * (size_t)n);
+  int32_t* bestt = (int32_t*)malloc(sizeof(int32_t) * (size_t)n);
+  if (!e || !map || !bestd || !bestt) {
+    free(e); free(map); free(bestd); free(bestt);
+    return 2;
+  }
+  for (int64_t i = 0; i < n; ++i)
+    if (labels[i] < 0 || labels[i] >= n) {
+      free(e); free(map); free(bestd); free(bestt);
+      return 1;
+    }
+  /* threshold */
+  float maxsq = 0.0f;
+  for (int64_t i = 0; i < n; ++i) {
+    float s = 0.0f;
+    for (int d = 0; d < 3; ++d) s = s + pts[d * n + i] * pts[d * n + i];
+    if (s > maxsq) maxsq = s;
+  }
+  const float D = threshold * sqrtf(maxsq);
+  /* edges */
+  int64_t ne = 0;
+  for (int y = 0; y < height; ++y)
+    for (int x = 0; x < width; ++x) {
+      const int64_t p = (int64_t)y * width + x;
+      for (int dy = -1; dy <= 1; ++dy)
+        for (int dx = -1; dx <= 1; ++dx) {
+          if (!dx && !dy) continue;
+          const int nx = x + dx, ny = y + dy;
+          if (nx < 0 || ny < 0 || nx >= width || ny >= height) continue;
+          const int64_t q = (int64_t)ny * width + nx;
+          if (labels[q] == labels[p]) continue;
+          e[ne].s = labels[p];
+          e[ne].t = labels[q];
+          e[ne].q = llrintf(sm_norm(pts, n, p, q) * 4294967296.0f);
+          ++ne;
+        }
+    }
+  qsort(e, (size_t)ne, sizeof(SmEdge), sm_cmp);
+  for (int64_t i = 0; i < n; ++i) {
+    map[i] = (int32_t)i;
+    bestt[i] = -1;
+  }
+  for (int64_t a = 0; a < ne;) {
+    int64_t b = a;
+    long long sum = 0;
+    while (b < ne && e[b].s == e[a].s && e[b].t == e[a].t) sum += e[b++].q;
+    const int64_t cnt = b - a;
+    const float mean = (float)(((double)sum * (1.0 / 4294967296.0)) / (double)cnt);
+    const int s = e[a].s, t = e[a].t;
+    if (mean < D && cnt > 15) {
+      if (bestt[s] < 0 || mean < bestd[s] || (mean == bestd[s] && t < bestt[s])) {
+        bestd[s] = mean;
+        bestt[s] = t;
+      }
+    }
+    a = b;
+  }
+  for (int64_t s = 0; s < n; ++s)
+    if (bestt[s] >= 0) map[s] = bestt[s];
+  /* mutual pairs: the larger id keeps itself */
+  for (int64_t s = 0; s < n; ++s) {
+    const int32_t t = map[s];
+    if (t != s && map[t] == s && s > t) map[s] = (int32_t)s;
+  }
+  /* chains */
+  for (int64_t i = 0; i < n; ++i) {
+    int32_t r = labels[i];
+    for (int64_t steps = 0; map[r] != r && steps <= n; ++steps) r = map[r];
+    labels[i] = r;
+  }
+  free(e); free(map); free(bestd); free(bestt);
+  return 0;
+}

@@ -55,6 +55,9 @@ _SIGS = {
     "split_pipeline_run": (_i32, [_vp, _i32, _i32, _vp, _vp, _vp, _vp, _vp, _vp, _sz, _vp, _vp]),
     "split_launch_count": (C.c_ulonglong, []),
     "split_tune_set": (C.c_int, [C.c_void_p, C.c_int]),
+    "split_merge_smooth_workspace_size": (C.c_size_t, [C.c_int, C.c_int]),
+    "split_merge_smooth": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_float,
+                                     C.c_void_p, C.c_size_t, C.c_void_p]),
     "split_tune_get": (C.c_int, [C.c_void_p, C.c_int]),
     "split_batch_create": (_i32, [_vp, _i32, _vp, _vp]),
     "split_batch_destroy": (None, [_vp]),

@@ -86,3 +86,35 @@ def merge_small_segments(chrominance: torch.Tensor | None, labels: torch.Tensor,
                                     ws.ptr, ws.nbytes, stream_handle(stream))
     N.check(st, "ccl.merge_small_segments")
     return ws
+
+
+def merge_smooth_boundaries_workspace(width: int, height: int) -> int:
+    """merge_smooth_boundaries.cuh:29-31 (sized by the image; the segment and
+    edge counts are not needed)."""
+    return N.load().split_merge_smooth_workspace_size(width, height)
+
+
+def merge_smooth_boundaries(points: torch.Tensor, nsegments: int, labels: torch.Tensor,
+                            temp: Workspace | None = None, threshold: float = 0.01, *,
+                            stream=None) -> Workspace:
+    """split::device::ccl::merge_smooth_boundaries (merge_smooth_boundaries.cuh:20-25).
+
+    points: planar float32 (>= 3, H*W) features (rows 0..2 are read);
+    labels: (H, W) int32 segment ids in [0, H*W), merged in place.  Segments
+    join the neighbour with the smallest mean feature difference across
+    their boundary, among neighbours sharing more than 15 boundary edges with
+    a mean below threshold * max |x|.  ``nsegments`` is accepted for
+    signature compatibility; ids need not be compressed."""
+    del nsegments
+    require_cuda(points, "points", torch.float32)
+    require_cuda(labels, "labels", torch.int32)
+    if labels.dim() != 2:
+        raise ValueError("labels must be (height, width)")
+    h, w = labels.shape
+    if points.dim() != 2 or points.shape[0] < 3 or points.shape[1] != h * w:
+        raise ValueError("points must be a planar (>= 3, height * width) tensor")
+    ws = ensure_workspace(temp, merge_smooth_boundaries_workspace(w, h), labels.device)
+    st = N.load().split_merge_smooth(ptr(labels), w, h, ptr(points), float(threshold), ws.ptr,
+                                     ws.nbytes, stream_handle(stream))
+    N.check(st, "ccl.merge_smooth_boundaries")
+    return ws

@@ -382,3 +382,31 @@ def test_segment_means_many_clusters(cuda, layout, dim):
     np.testing.assert_array_equal(got[:, cnt == 0], c_in[:, cnt == 0])
     rel = np.abs(got - ref) / np.maximum(np.abs(ref), 1e-30)
     assert rel.max() <= 1e-5
+
+
+@pytest.mark.parametrize("threshold", [0.01, 0.02, 0.1])
+def test_merge_smooth_boundaries(cuda, threshold):
+    """Smooth-boundary merge, bit-exact against the oracle on seeded blobs
+    with Lab-like features (L in [0, 100], a, b in [-60, 60]) plus noise."""
+    import torch
+    from split_gb300 import ccl
+    w, h = 300, 211
+    rng = np.random.default_rng(int(threshold * 1000))
+    blocks = rng.integers(0, 6, size=(h // 6 + 1, w // 6 + 1)).repeat(6, 0).repeat(6, 1)[:h, :w]
+    seg = oracle.ccl(blocks.astype(np.int32), 8, 0)
+    # block classes c and c + 3 share a colour: adjacent segments of those
+    # classes have smooth boundaries, the others sharp ones
+    base = np.stack([rng.uniform(0, 100, 3), rng.uniform(-60, 60, 3), rng.uniform(-60, 60, 3)])
+    pts = base[:, (blocks % 3).ravel()] + rng.normal(0, 0.5, size=(3, w * h))
+    pts = np.ascontiguousarray(pts, dtype=np.float32)
+    ref = oracle.merge_smooth(seg, pts, threshold)
+    g = _t(seg, cuda)
+    ws = ccl.merge_smooth_boundaries(_t(pts, cuda), 0, g, None, threshold)
+    got = g.cpu().numpy()
+    ws.check("merge_smooth")
+    assert np.array_equal(got, ref)
+    assert len(np.unique(ref)) < len(np.unique(seg))      # something merged
+    # the workspace is left clean: a second call on the merged labels agrees too
+    ref2 = oracle.merge_smooth(ref, pts, threshold)
+    ccl.merge_smooth_boundaries(_t(pts, cuda), 0, g, ws, threshold)
+    assert np.array_equal(g.cpu().numpy(), ref2)

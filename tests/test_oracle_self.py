@@ -94,3 +94,22 @@ def test_merge_sorted_labels_quirk():
     seg = oracle.compress_labels(oracle.ccl(lab, 4, 0))[0].reshape(lab.shape)
     assert np.array_equal(oracle.merge_small(seg, 100, 1, np.ones((2, seg.size), np.float32)), seg)
     assert not np.array_equal(oracle.merge_small(seg, 100, 0), seg)
+
+
+def test_merge_smooth_rules():
+    """Two halves with a long, smooth boundary merge into the larger id; a
+    sharp boundary or a boundary of at most 15 edges keeps them apart."""
+    h, w = 20, 16
+    lab = np.zeros((h, w), np.int32)
+    lab[:, w // 2:] = w // 2                   # ids: the first pixel of each half
+    pts = np.zeros((3, h * w), np.float32)
+    pts[0] = 0.5
+    pts[0, lab.ravel() == w // 2] = 0.5005     # smooth: difference 5e-4
+    pts[1] = 1.0
+    out = oracle.merge_smooth(lab, pts, 0.01)
+    assert (out == w // 2).all()
+    sharp = pts.copy()
+    sharp[0, lab.ravel() == w // 2] = 0.9      # difference 0.4 >= 0.01 * max
+    assert np.array_equal(oracle.merge_smooth(lab, sharp, 0.01), lab)
+    short = lab[:2].copy()                     # 2 rows: 4 edges each way, <= 15
+    assert np.array_equal(oracle.merge_smooth(short, pts[:, : 2 * w], 0.01), short)
