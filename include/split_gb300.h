@@ -277,6 +277,20 @@ int split_sobel_normals_rgb8(const uint8_t* rgb, int width, int height,
 int split_pack_rgb8(const uint8_t* rgb, int64_t npixels, float* features4,
                     float* luminance, void* stream);
 
+/* The sample's k-means features (samples/src/main.cu:169-173, :215-225;
+ * replaces color::convert_color_space(rgb_to_lab) followed by
+ * color::beta_feature, beta_feature.cuh:12-15): RGB8 -> channels clamped to
+ * >= 1/255 -> L*a*b* (conversion.inl:8-64) -> (beta, a*, b*) with beta = -mu
+ * for achromatic pixels (|a*|, |b*| < 0.2 max |a*|) darker than 0.2 L*max,
+ * +mu for achromatic pixels brighter than 0.95 L*max, 0 otherwise
+ * (beta_feature.cu:26-78).  layout: SPLIT_LAYOUT_FLOAT4 ((beta, a*, b*, 0)
+ * per pixel, 16-byte aligned) or SPLIT_LAYOUT_PLANAR (3 x n).  luminance:
+ * optional n floats of L*.  Two passes over the RGB8 input. */
+size_t split_pack_lab_beta_workspace_size(int64_t npixels);
+int split_pack_lab_beta(const uint8_t* rgb, int64_t npixels, float mu, int layout,
+                        float* features, float* luminance, void* workspace,
+                        size_t workspace_bytes, void* stream);
+
 /* ======================================================================== */
 /* pipeline                                                                  */
 /* ======================================================================== */
@@ -291,7 +305,10 @@ typedef struct split_pipeline_params {
   int kmeans_iters;
   float kmeans_threshold; /* < 0: exactly kmeans_iters iterations            */
   int features;           /* SPLIT_LAYOUT_FLOAT4: pack float4 features first;
-                             SPLIT_LAYOUT_RGB8: read the bytes directly      */
+                             SPLIT_LAYOUT_RGB8: read the bytes directly;
+                             SPLIT_PIPELINE_FEATURES_LAB_BETA: the sample's
+                             (beta, a*, b*) features (split_pack_lab_beta;
+                             single images only, not batches)              */
   int connectivity;       /* 4 or 8                                          */
   int convention;         /* SPLIT_LABEL_MIN_INDEX / SPLIT_LABEL_MAX_INDEX   */
   int merge_P;            /* merge segments smaller than P; 0 = no merge     */
@@ -299,7 +316,11 @@ typedef struct split_pipeline_params {
   int erode_radius;       /* 0 = no erosion                                  */
   int compute_normals;    /* nonzero: normals of L* / 100                    */
   float depth;
+  float beta_mu;          /* mu of the beta feature (the reference: 1e5)     */
 } split_pipeline_params;
+
+/* split_pipeline_params.features value for the sample's Lab + beta features. */
+#define SPLIT_PIPELINE_FEATURES_LAB_BETA 3
 
 enum { SPLIT_PIPELINE_STAGES = 6 }; /* pack, kmeans, ccl, merge, erode, normals */
 

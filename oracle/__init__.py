@@ -162,3 +162,27 @@ def merge_smooth(labels: np.ndarray, points: np.ndarray, threshold: float = 0.01
     if rc:
         raise RuntimeError(f"orc_merge_smooth failed ({rc})")
     return a
+
+
+def lab_beta_f64(rgb: np.ndarray, mu: float = 1e5):
+    """The sample's features in FP64 (samples/src/main.cu:169-173, :215-225):
+    RGB8 (..., 3) -> channels / 255 clamped to >= 1/255 -> sRGB linearised
+    (conversion.inl:15-20) -> XYZ (:22-24) -> L*a*b* (:46-64) -> beta in
+    place of L* (beta_feature.cu:26-78: lambda = 0.2 max |a*|, bounds 0.2
+    and 0.95 of the largest L*).  Returns ((3, N) beta, a*, b*; (N,) L*)."""
+    v = np.maximum(np.asarray(rgb, np.float64).reshape(-1, 3) / 255.0, 1.0 / 255.0)
+    lin = np.where(v > 0.04045, ((v + 0.055) / 1.055) ** 2.4, v / 12.92) * 100.0
+    m = np.array([[0.4124564, 0.3575761, 0.1804375],
+                  [0.2126729, 0.7151522, 0.0721750],
+                  [0.0193339, 0.1191920, 0.9503041]])
+    xyz = lin @ m.T
+    t = xyz / np.array([95.047, 100.0, 108.883])
+    f = np.where(t > 0.008856, np.cbrt(t), 7.787 * t + 16.0 / 116.0)
+    L = 116.0 * f[:, 1] - 16.0
+    a = 500.0 * (f[:, 0] - f[:, 1])
+    b = 200.0 * (f[:, 1] - f[:, 2])
+    lam = 0.2 * np.abs(a).max()
+    lo, hi = 0.2 * L.max(), 0.95 * L.max()
+    achrom = (np.abs(a) < lam) & (np.abs(b) < lam)
+    beta = np.where(achrom & (L < lo), -mu, np.where(achrom & (L > hi), mu, 0.0))
+    return np.stack([beta, a, b]), L

@@ -126,6 +126,20 @@ def rgb_to_lab(rgb_planar):
     return out
 
 
+def lab_beta(rgb_planar, mu=1e5):
+    """The sample's features: (3, N) RGB in [0, 1] -> ((3, N) beta, a*, b*;
+    (N,) L*)  (main.cu:169-173, :215-225; beta_feature.cu:47-78)."""
+    a = np.ascontiguousarray(rgb_planar, np.float32)
+    n = a.shape[1]
+    feats = np.empty_like(a)
+    lum = np.empty(n, np.float32)
+    lib = load()
+    lib.ref_lab_beta.argtypes = [C.c_void_p, C.c_int, C.c_float, C.c_void_p, C.c_void_p]
+    lib.ref_lab_beta.restype = C.c_int
+    lib.ref_lab_beta(_p(a), n, float(mu), _p(feats), _p(lum))
+    return feats, lum
+
+
 class quiet:
     """Silences the reference's progress prints (std::cout / printf) on the
     process's stdout for the duration of a block."""

@@ -13,7 +13,9 @@
 #include <thrust/device_free.h>
 
 #include "split/device/ccl/compress_labels.cuh"
+#include "split/device/color/beta_feature.cuh"
 #include "split/device/color/conversion.cuh"
+#include "split/device/detail/unary_functional.cuh"
 #include "split/device/ccl/connected_components.cuh"
 #include "split/device/ccl/merge_small_segments.cuh"
 #include "split/device/kmeans/centroids.cuh"
@@ -148,6 +150,22 @@ int ref_rgb_to_lab(const float* rgb, int n, float* lab) {
   to_dev(A, rgb, 3 * (std::size_t)n);
   split::device::color::convert_color_space(A, B, split::device::color::rgb_to_lab<>());
   to_host(B, lab, 3 * (std::size_t)n);
+  return 0;
+}
+
+// The sample's feature preparation (samples/src/main.cu:169-173, :215-225):
+// RGB in [0, 1] clamped to >= 1/255, converted to L*a*b*, L* saved, then the
+// beta feature written in place of L*.  features: planar 3 x n (beta, a, b);
+// luminance: n (L*).
+int ref_lab_beta(const float* rgb, int n, float mu, float* features, float* luminance) {
+  Mat A(3, n), B(3, n);
+  to_dev(A, rgb, 3 * (std::size_t)n);
+  thrust::transform(A.values.begin(), A.values.end(), A.values.begin(),
+                    split::device::detail::unary_max<real>(1.f / 255.f));
+  split::device::color::convert_color_space(A, B, split::device::color::rgb_to_lab<>());
+  thrust::copy(B.row(0).begin(), B.row(0).end(), luminance);
+  split::device::color::beta_feature(B, B.row(0), mu);
+  to_host(B, features, 3 * (std::size_t)n);
   return 0;
 }
 

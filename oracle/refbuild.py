@@ -46,7 +46,12 @@ SOURCES = [
     "split/src/split/device/morph/erode.cu",
     "split/src/split/device/sfs/sobel_normals.cu",
     "split/src/split/device/detail/normalize_vectors.cu",
+    "split/src/split/device/color/beta_feature.cu",
 ]
+
+# Headers a source used through includes of the Thrust / CUSP versions it was
+# written against (added to that file's staged copy only).
+EXTRA_INCLUDES = {"beta_feature.cu": ("thrust/extrema.h",)}
 
 _GET = re.compile(r"\.get<(\d+)>\(\)")
 _IDENT = re.compile(r"[A-Za-z0-9_]")
@@ -123,8 +128,9 @@ def stage_sources(verbose: bool = False) -> bool:
         dst = os.path.join(SRC, os.path.basename(rel)[:-3] + ".cpp")
         with open(os.path.join(REF_ROOT, rel)) as f:
             text = f.read()
+        extra = "".join(f"#include <{h}>\n" for h in EXTRA_INCLUDES.get(os.path.basename(rel), ()))
         with open(dst, "w") as f:
-            f.write(rewrite_get(text))
+            f.write(extra + rewrite_get(text))
     for root, _, files in os.walk(os.path.join(SRC, "include")):
         for name in files:
             p = os.path.join(root, name)

@@ -56,6 +56,9 @@ _SIGS = {
     "split_launch_count": (C.c_ulonglong, []),
     "split_tune_set": (C.c_int, [C.c_void_p, C.c_int]),
     "split_merge_smooth_workspace_size": (C.c_size_t, [C.c_int, C.c_int]),
+    "split_pack_lab_beta_workspace_size": (C.c_size_t, [C.c_int64]),
+    "split_pack_lab_beta": (C.c_int, [C.c_void_p, C.c_int64, C.c_float, C.c_int, C.c_void_p,
+                                      C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p]),
     "split_merge_smooth": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_float,
                                      C.c_void_p, C.c_size_t, C.c_void_p]),
     "split_tune_get": (C.c_int, [C.c_void_p, C.c_int]),
@@ -81,7 +84,10 @@ class PipelineParams(C.Structure):
                 ("kmeans_iters", C.c_int), ("kmeans_threshold", C.c_float),
                 ("features", C.c_int), ("connectivity", C.c_int), ("convention", C.c_int),
                 ("merge_P", C.c_int), ("merge_policy", C.c_int), ("erode_radius", C.c_int),
-                ("compute_normals", C.c_int), ("depth", C.c_float)]
+                ("compute_normals", C.c_int), ("depth", C.c_float), ("beta_mu", C.c_float)]
+
+
+FEATURES_LAB_BETA = 3   # split_pipeline_params.features: the sample's Lab + beta
 
 
 PIPELINE_STAGES = ("pack", "kmeans", "ccl", "merge", "erode", "normals")

@@ -377,14 +377,24 @@ border_kernel(const int32_t* __restrict__ in, Geoms gs, int* P, int* status) {
 // tiles are being finalised concurrently, always to their root), the rest
 // follow entries inside the tile through shared memory.  Component sizes
 // are counted per tile and added with one atomic per local component.
-__device__ __forceinline__ int local_of(long long v, long long off, int W, int tx0, int ty0,
-                                        int tw, int th) {
-  const long long rel = v - off;
-  if (rel < 0) return -1;
-  const int y = (int)(rel / W), x = (int)(rel - (long long)y * W);
-  const int r = y - ty0, c = x - tx0;
-  return (r >= 0 && r < th && c >= 0 && c < tw) ? r * TW + c : -1;
-}
+// Maps a global index to its local index in the tile, or -1 outside it,
+// without integer division: rows from a float reciprocal of the width, then
+// corrected by one (the offset is below 32 rows, so the estimate is within
+// one row).
+struct TileFrame {
+  long long base;   // global index of the tile's first pixel
+  int W, tw, th;
+  float invW;
+  __device__ __forceinline__ int local(long long v) const {
+    const long long d = v - base;
+    if (d < 0 || d >= (long long)(th - 1) * W + tw) return -1;
+    const int di = (int)d;
+    int r = __float2int_rz((float)di * invW);
+    int c = di - r * W;
+    if (c < 0) { --r; c += W; } else if (c >= W) { ++r; c -= W; }
+    return c < tw ? r * TW + c : -1;
+  }
+};
 
 __device__ __forceinline__ int groot(const int* P, int x, unsigned& budget) {
   int p = __ldcg(P + x);
@@ -406,6 +416,7 @@ flatten_kernel(int* P, Geoms gs, int32_t* __restrict__ sizes, int* status) {
   const long long off = t.off;
   const int tw = min(TW, W - tx0), th = min(TH, t.H - ty0);
   const int lane = threadIdx.x & 31, r0 = (threadIdx.x >> 5) * kRowsPerWarp;
+  const TileFrame fr{off + (long long)ty0 * W + tx0, W, tw, th, 1.0f / (float)W};
   int e[2 * kRowsPerWarp];
 #pragma unroll
   for (int k = 0; k < 2 * kRowsPerWarp; ++k) {
@@ -426,7 +437,7 @@ flatten_kernel(int* P, Geoms gs, int32_t* __restrict__ sizes, int* status) {
   for (int k = 0; k < 2 * kRowsPerWarp; ++k) {
     const int r = r0 + (k >> 1), c = lane + 32 * (k & 1);
     if (r < th && c < tw && res[r * TW + c] < 0 &&
-        local_of(e[k], off, W, tx0, ty0, tw, th) < 0) {
+        fr.local(e[k]) < 0) {
       unsigned budget = kFindCap;
       res[r * TW + c] = groot(P, e[k], budget);
       if (!budget) set_status(status, SPLIT_ERR_NOT_CONVERGED);
@@ -443,7 +454,7 @@ flatten_kernel(int* P, Geoms gs, int32_t* __restrict__ sizes, int* status) {
     if (r < th && c < tw) {
       x = r * TW + c;
       for (unsigned hop = 0; res[x] < 0; ++hop) {
-        const int nx = local_of(ent[x], off, W, tx0, ty0, tw, th);
+        const int nx = fr.local(ent[x]);
         if (nx < 0 || hop >= TH * TW) {   // cannot happen for a consistent forest
           set_status(status, SPLIT_ERR_NOT_CONVERGED);
           break;

@@ -7,8 +7,16 @@
 namespace sg {
 namespace pipe {
 
+// The sample's Lab + beta features (float4 per pixel) instead of RGB / 255.
+constexpr int kFeaturesLabBeta = SPLIT_PIPELINE_FEATURES_LAB_BETA;
+
+inline bool packs(const split_pipeline_params& p) {
+  return p.features == SPLIT_LAYOUT_FLOAT4 || p.features == kFeaturesLabBeta;
+}
+
 struct Layout {
   WsHeader* hdr;
+  void* pack_ws;   // maxima of the Lab + beta pass
   float* features4;
   int32_t* seg;
   int32_t* sizes;
@@ -26,7 +34,8 @@ static Layout carve(void* ws, int W, int H, const split_pipeline_params& p) {
   Carver c(ws);
   Layout l;
   l.hdr = c.take<WsHeader>(1);
-  l.features4 = p.features == SPLIT_LAYOUT_FLOAT4 ? c.take<float>((size_t)n * 4) : nullptr;
+  l.pack_ws = p.features == kFeaturesLabBeta ? c.take<char>(512) : nullptr;
+  l.features4 = packs(p) ? c.take<float>((size_t)n * 4) : nullptr;
   l.seg = c.take<int32_t>((size_t)n);
   l.sizes = c.take<int32_t>((size_t)n);
   l.km_bytes = split_kmeans_cluster_workspace_size_2d(n, W, p.nclusters, p.dim);
@@ -42,7 +51,8 @@ static Layout carve(void* ws, int W, int H, const split_pipeline_params& p) {
 static bool valid(const split_pipeline_params* p) {
   return p && p->nclusters >= 1 && p->nclusters <= 64 && (p->dim == 3 || p->dim == 5) &&
          p->kmeans_iters >= 0 &&
-         (p->features == SPLIT_LAYOUT_FLOAT4 || p->features == SPLIT_LAYOUT_RGB8) &&
+         (p->features == SPLIT_LAYOUT_FLOAT4 || p->features == SPLIT_LAYOUT_RGB8 ||
+          p->features == kFeaturesLabBeta) &&
          (p->connectivity == 4 || p->connectivity == 8) &&
          (p->convention == SPLIT_LABEL_MIN_INDEX || p->convention == SPLIT_LABEL_MAX_INDEX) &&
          p->merge_P >= 0 && p->merge_policy == SPLIT_MERGE_MOST_BOUNDARY && p->erode_radius >= 0 &&
@@ -86,14 +96,18 @@ extern "C" int split_pipeline_run(const uint8_t* rgb, int width, int height,
   SG_TRY(mark(0));
   if (p.features == SPLIT_LAYOUT_FLOAT4)
     SG_TRY(split_pack_rgb8(rgb, n, l.features4, nullptr, stream));
+  else if (p.features == pipe::kFeaturesLabBeta)
+    SG_TRY(split_pack_lab_beta(rgb, n, p.beta_mu, SPLIT_LAYOUT_FLOAT4, l.features4, nullptr,
+                               l.pack_ws, 512, stream));
   SG_TRY(mark(1));
   // 1: k-means
   SG_TRY(mark(2));
-  const void* pts = p.features == SPLIT_LAYOUT_FLOAT4 ? static_cast<const void*>(l.features4)
-                                                       : static_cast<const void*>(rgb);
-  // packed features are byte / 255: inside the unit cube
-  const int layout = p.features == SPLIT_LAYOUT_FLOAT4 ? (SPLIT_LAYOUT_FLOAT4 | SPLIT_FEATURES_UNIT_RANGE)
-                                                        : p.features;
+  const void* pts = pipe::packs(p) ? static_cast<const void*>(l.features4)
+                             : static_cast<const void*>(rgb);
+  // byte / 255 features lie in the unit cube; Lab + beta ones do not
+  const int layout = p.features == SPLIT_LAYOUT_FLOAT4
+                         ? (SPLIT_LAYOUT_FLOAT4 | SPLIT_FEATURES_UNIT_RANGE)
+                         : pipe::packs(p) ? SPLIT_LAYOUT_FLOAT4 : p.features;
   SG_TRY(split_kmeans_cluster(pts, layout, p.dim, n, width, p.xy_scale, centroids,
                               p.nclusters, cluster_labels, l.km_ws, l.km_bytes, p.kmeans_iters,
                               p.kmeans_threshold, nullptr, stream));

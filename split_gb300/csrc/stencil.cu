@@ -309,6 +309,92 @@ __global__ void pack_kernel(const uint8_t* __restrict__ rgb, int64_t n, float4* 
   }
 }
 
+// ---- L*a*b* and the beta feature ------------------------------------------------
+// L*a*b* of an sRGB byte triple after the sample's clamp (conversion.inl:8-25
+// rgb_to_xyz, :46-64 xyz_to_lab; operations in the reference's order, FP32).
+struct Lab {
+  float L, a, b;
+};
+__device__ __forceinline__ float lab_f(float t) {
+  return t > 0.008856f ? cbrtf(t) : __fadd_rn(__fmul_rn(7.787f, t), 16.0f / 116.0f);
+}
+__device__ __forceinline__ Lab lab_from_lin(float r, float g, float b) {
+  const float X = __fadd_rn(__fadd_rn(__fmul_rn(r, 0.4124564f), __fmul_rn(g, 0.3575761f)),
+                            __fmul_rn(b, 0.1804375f));
+  const float Y = __fadd_rn(__fadd_rn(__fmul_rn(r, 0.2126729f), __fmul_rn(g, 0.7151522f)),
+                            __fmul_rn(b, 0.0721750f));
+  const float Z = __fadd_rn(__fadd_rn(__fmul_rn(r, 0.0193339f), __fmul_rn(g, 0.1191920f)),
+                            __fmul_rn(b, 0.9503041f));
+  const float fx = lab_f(__fmul_rn(X, 1.0f / 95.047f));
+  const float fy = lab_f(__fmul_rn(Y, 0.01f));
+  const float fz = lab_f(__fmul_rn(Z, 1.0f / 108.883f));
+  Lab o;
+  o.L = __fsub_rn(__fmul_rn(116.0f, fy), 16.0f);
+  o.a = __fmul_rn(500.0f, __fsub_rn(fx, fy));
+  o.b = __fmul_rn(200.0f, __fsub_rn(fy, fz));
+  return o;
+}
+
+// order-preserving integer key of a float (for atomicMax over any sign)
+__device__ __forceinline__ unsigned okey(float v) {
+  const unsigned u = __float_as_uint(v);
+  return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float okey_inv(unsigned k) {
+  return __uint_as_float((k & 0x80000000u) ? (k & 0x7fffffffu) : ~k);
+}
+
+// pass 1: the largest L* and the largest |a*| of the image (beta_feature.cu:52-64)
+__global__ void lab_max_kernel(const uint8_t* __restrict__ rgb, int64_t n, unsigned* maxima) {
+  __shared__ float lin[256];
+  for (int i = threadIdx.x; i < 256; i += blockDim.x) lin[i] = lin100(i);
+  __syncthreads();
+  unsigned kl = 0, ka = 0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const Lab c = lab_from_lin(lin[rgb[3 * i]], lin[rgb[3 * i + 1]], lin[rgb[3 * i + 2]]);
+    kl = max(kl, okey(c.L));
+    ka = max(ka, okey(fabsf(c.a)));
+  }
+  kl = __reduce_max_sync(0xffffffffu, kl);
+  ka = __reduce_max_sync(0xffffffffu, ka);
+  if ((threadIdx.x & 31) == 0) {
+    atomicMax(maxima, kl);
+    atomicMax(maxima + 1, ka);
+  }
+}
+
+// pass 2: (beta, a*, b*) features and L* (beta_feature.cu:26-45: beta = -mu
+// below 0.2 L*max, +mu above 0.95 L*max, for pixels with |a*| and |b*| below
+// 0.2 max |a*|; 0 otherwise)
+__global__ void lab_beta_kernel(const uint8_t* __restrict__ rgb, int64_t n, const unsigned* maxima,
+                                float mu, float* __restrict__ out, int float4_out,
+                                float* __restrict__ lumo) {
+  __shared__ float lin[256];
+  for (int i = threadIdx.x; i < 256; i += blockDim.x) lin[i] = lin100(i);
+  __syncthreads();
+  const float lmax = okey_inv(maxima[0]);
+  const float lambda = __fmul_rn(0.2f, okey_inv(maxima[1]));
+  const float lo = __fmul_rn(lmax, 0.20f), hi = __fmul_rn(lmax, 0.95f);
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const Lab c = lab_from_lin(lin[rgb[3 * i]], lin[rgb[3 * i + 1]], lin[rgb[3 * i + 2]]);
+    float beta = 0.0f;
+    if (fabsf(c.a) < lambda && fabsf(c.b) < lambda) {
+      if (c.L < lo) beta = -mu;
+      else if (c.L > hi) beta = mu;
+    }
+    if (float4_out) {
+      reinterpret_cast<float4*>(out)[i] = make_float4(beta, c.a, c.b, 0.0f);
+    } else {
+      out[i] = beta;
+      out[n + i] = c.a;
+      out[2 * n + i] = c.b;
+    }
+    if (lumo) lumo[i] = c.L;
+  }
+}
+
 }  // namespace stn
 }  // namespace sg
 
@@ -418,5 +504,35 @@ extern "C" int split_pack_rgb8(const uint8_t* rgb, int64_t npixels, float* featu
   if (blocks > (int64_t)di.sm_count * 8) blocks = (int64_t)di.sm_count * 8;
   stn::pack_kernel<<<(int)blocks, 256, 0, as_stream(stream)>>>(
       rgb, npixels, reinterpret_cast<float4*>(features4), luminance);
+  return launch_status();
+}
+
+// Lab + beta features of the sample (samples/src/main.cu:169-173, :215-225):
+// two passes over the RGB8 image, nothing else read or written.
+extern "C" size_t split_pack_lab_beta_workspace_size(int64_t npixels) {
+  (void)npixels;
+  return 512;
+}
+
+extern "C" int split_pack_lab_beta(const uint8_t* rgb, int64_t npixels, float mu, int layout,
+                                   float* features, float* luminance, void* workspace,
+                                   size_t workspace_bytes, void* stream) {
+  if (!rgb || !features || npixels <= 0 || !(mu >= 0.0f)) return SPLIT_ERR_INVALID;
+  if (layout != SPLIT_LAYOUT_PLANAR && layout != SPLIT_LAYOUT_FLOAT4) return SPLIT_ERR_INVALID;
+  if (layout == SPLIT_LAYOUT_FLOAT4 && (reinterpret_cast<uintptr_t>(features) & 15))
+    return SPLIT_ERR_INVALID;
+  if (!workspace || workspace_bytes < 512 || (reinterpret_cast<uintptr_t>(workspace) & 255))
+    return SPLIT_ERR_WORKSPACE;
+  cudaStream_t st = as_stream(stream);
+  unsigned* maxima = reinterpret_cast<unsigned*>(static_cast<char*>(workspace) + 256);
+  SG_CUDA_TRY(cudaMemsetAsync(maxima, 0, 2 * sizeof(unsigned), st));
+  DeviceInfo di;
+  SG_TRY(device_info(&di));
+  int64_t blocks = (npixels + 255) / 256;
+  if (blocks > (int64_t)di.sm_count * 8) blocks = (int64_t)di.sm_count * 8;
+  stn::lab_max_kernel<<<(int)blocks, 256, 0, st>>>(rgb, npixels, maxima);
+  SG_TRY(launch_status());
+  stn::lab_beta_kernel<<<(int)blocks, 256, 0, st>>>(rgb, npixels, maxima, mu, features,
+                                                     layout == SPLIT_LAYOUT_FLOAT4, luminance);
   return launch_status();
 }

@@ -27,12 +27,14 @@ class Params:
     erode_radius: int = 1
     compute_normals: bool = True
     depth: float = 1.0
+    beta_mu: float = 1e5     # features = N.FEATURES_LAB_BETA only
 
     def c(self) -> N.PipelineParams:
         return N.PipelineParams(self.nclusters, self.dim, self.xy_scale, self.kmeans_iters,
                                 self.kmeans_threshold, self.features, self.connectivity,
                                 self.convention, self.merge_P, self.merge_policy,
-                                self.erode_radius, int(self.compute_normals), self.depth)
+                                self.erode_radius, int(self.compute_normals), self.depth,
+                                self.beta_mu)
 
 
 class Pipeline:

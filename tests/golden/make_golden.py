@@ -25,6 +25,7 @@ ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 
 OUT = os.path.join(HERE, "reference_golden.npz")
+OUT_LAB = os.path.join(HERE, "lab_beta_golden.npz")
 
 
 def sha(a: np.ndarray) -> str:
@@ -51,6 +52,28 @@ def inputs():
     # heights for the normals
     d["heights"] = rng.random((48, 64), dtype=np.float32)
     return d
+
+
+def lab_beta_inputs():
+    """RGB8 image for the sample's Lab + beta features: Voronoi cells with
+    noise, plus dark, mid and bright grey patches (achromatic pixels, so that
+    beta takes -mu, 0 and +mu)."""
+    from split_gb300 import synth
+    rgb = synth.voronoi_rgb8(0x54, 128, 96, 24, sigma=2.0).copy()
+    rng = np.random.default_rng(0x55)
+    for (y0, x0, v) in ((8, 8, 18), (40, 60, 128), (60, 10, 250), (70, 90, 235)):
+        patch = v + rng.integers(-2, 3, size=(16, 24, 1))
+        rgb[y0:y0 + 16, x0:x0 + 24] = np.clip(patch, 0, 255).astype(np.uint8)
+    return rgb
+
+
+def main_lab_beta():
+    from oracle import ref
+    from split_gb300 import synth
+    rgb = lab_beta_inputs()
+    feats, lum = ref.lab_beta(synth.features(rgb, 3), 1e5)
+    np.savez_compressed(OUT_LAB, rgb_sha=sha(rgb), features=feats, luminance=lum, mu=1e5)
+    print(f"wrote {OUT_LAB}")
 
 
 def main():
@@ -88,5 +111,7 @@ def main():
     print(f"wrote {OUT} ({os.path.getsize(OUT) / 1024:.0f} KiB)")
 
 
-if __name__ == "__main__":
+if __name__ == "__main__" and sys.argv[1:] == ["lab_beta"]:
+    main_lab_beta()
+elif __name__ == "__main__":
     main()

@@ -109,3 +109,26 @@ def test_cluster_10_iterations(cuda, inp):
     assert (lab.cpu().numpy() != G["km_cluster10_labels"]).mean() <= 1e-3
     rc = G["km_cluster10_centroids"]
     assert (np.abs(cent.cpu().numpy() - rc) / np.abs(rc)).max() <= 1e-3
+
+
+@pytest.mark.parametrize("planar", [False, True])
+def test_lab_beta_features(cuda, planar):
+    """Fused Lab + beta features against the reference's own FP32 sequence
+    (clamp, rgb_to_lab, beta_feature): L*, a*, b* within 1e-3, beta identical."""
+    import torch
+    import make_golden
+    from split_gb300 import color
+    g = np.load(os.path.join(HERE, "golden", "lab_beta_golden.npz"))
+    rgb = make_golden.lab_beta_inputs()
+    n = rgb.shape[0] * rgb.shape[1]
+    d_rgb = torch.from_numpy(rgb).to(cuda)
+    feats = torch.empty((3, n) if planar else (n, 4), dtype=torch.float32, device=cuda)
+    lum = torch.empty(n, dtype=torch.float32, device=cuda)
+    color.pack_lab_beta(d_rgb, feats, lum, float(g["mu"]))
+    f = feats.cpu().numpy()
+    f = f if planar else f[:, :3].T
+    np.testing.assert_allclose(lum.cpu().numpy(), g["luminance"], atol=1e-3)
+    np.testing.assert_allclose(f[1:], g["features"][1:], atol=1e-3)
+    assert np.array_equal(f[0], g["features"][0])
+    if not planar:
+        assert (feats[:, 3] == 0).all()

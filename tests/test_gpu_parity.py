@@ -410,3 +410,42 @@ def test_merge_smooth_boundaries(cuda, threshold):
     ref2 = oracle.merge_smooth(ref, pts, threshold)
     ccl.merge_smooth_boundaries(_t(pts, cuda), 0, g, ws, threshold)
     assert np.array_equal(g.cpu().numpy(), ref2)
+
+
+def test_pipeline_lab_beta_features(cuda):
+    """The pipeline with the sample's (beta, a*, b*) features: the features
+    equal the fused pack's, the k-means labels are the FP32-exact assignment
+    of the final iteration's input over them, and the integer stages match
+    the oracle given those labels."""
+    import os
+    import sys
+    import torch
+    sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden"))
+    import make_golden
+    from split_gb300 import _native, color, kmeans, pipeline
+    rgb = make_golden.lab_beta_inputs()
+    h, w = rgb.shape[:2]
+    n = w * h
+    d_rgb = torch.from_numpy(rgb).to(cuda)
+    f4 = torch.empty((n, 4), dtype=torch.float32, device=cuda)
+    color.pack_lab_beta(d_rgb, f4)
+    feats = f4[:, :3].T.contiguous().cpu().numpy()
+    k = 6
+    c0 = feats[:, np.linspace(0, n - 1, k).astype(int)].copy()
+    p = pipeline.Params(nclusters=k, dim=3, kmeans_iters=8, features=_native.FEATURES_LAB_BETA,
+                        merge_P=32)
+    pipe = pipeline.Pipeline(w, h, p, cuda)
+    pipe.run(d_rgb, torch.from_numpy(c0).to(cuda))
+    torch.cuda.synchronize()
+    pipe.ws.check("pipeline")
+    # the same clustering through the k-means entry point on the packed features
+    cent = torch.from_numpy(c0).to(cuda)
+    lab = torch.empty(n, dtype=torch.int32, device=cuda)
+    kmeans.cluster(f4, cent, lab, None, max_iter=8, threshold=-1.0, layout=kmeans.FLOAT4,
+                   dim=3, width=w)
+    cl = pipe.cluster_labels.cpu().numpy()
+    assert np.array_equal(cl, lab.cpu().numpy())
+    assert np.array_equal(pipe.centroids.cpu().numpy(), cent.cpu().numpy())
+    seg = oracle.ccl(cl.reshape(h, w), 8, 0)
+    seg = oracle.merge_small(seg, 32, 0)
+    assert np.array_equal(pipe.segment_labels.cpu().numpy(), oracle.erode(seg, 1))

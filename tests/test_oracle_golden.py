@@ -103,3 +103,17 @@ def test_sobel_normals(inp):
     ang = np.arccos(np.clip((o * r).sum(0) / np.linalg.norm(r, axis=0), -1, 1))
     # the reference's FP32 prefix-scan formulation drifts from FP64
     assert ang.max() <= 1e-3
+
+
+def test_lab_beta_restatement_against_reference():
+    """The FP64 restatement of the sample's Lab + beta features against the
+    reference's own FP32 code: L*, a*, b* within 2e-3, beta identical."""
+    import make_golden
+    g = np.load(os.path.join(HERE, "golden", "lab_beta_golden.npz"))
+    rgb = make_golden.lab_beta_inputs()
+    assert make_golden.sha(rgb) == str(g["rgb_sha"])
+    feats, lum = oracle.lab_beta_f64(rgb, float(g["mu"]))
+    np.testing.assert_allclose(lum, g["luminance"], atol=2e-3)
+    np.testing.assert_allclose(feats[1:], g["features"][1:], atol=2e-3)
+    assert np.array_equal(feats[0], g["features"][0])
+    assert set(np.unique(feats[0])) == {-1e5, 0.0, 1e5}
