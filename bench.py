@@ -409,7 +409,7 @@ def run_serving(dev, nimages, nrequests, seed=SEED + 2000):
             out.append(Request(j, h_rgb[i], k, iters, h_c0[i], float(t)))
         return out
 
-    srv = Server(params, device=dev, keep_results=False)
+    srv = Server(params, device=dev, keep_results=False, reserve_pixels=64 << 20)
     srv.serve(requests([0.0] * min(64, nrequests)), realtime=False)   # warm-up
     srv.completed.clear()
     nb0 = len(srv.batch_sizes)
@@ -423,7 +423,10 @@ def run_serving(dev, nimages, nrequests, seed=SEED + 2000):
            "mean_mpix_per_request": round(sum(s[0] * s[1] for s in shapes) / nimages / 1e6, 3),
            "saturation": sat}
     for load in (0.5, 0.8):
-        srv = Server(params, device=dev, keep_results=False)
+        srv = Server(params, device=dev, keep_results=False, reserve_pixels=64 << 20)
+        srv.serve(requests([0.0] * min(64, nrequests)), realtime=False)   # warm-up
+        srv.completed.clear()
+        srv.batch_sizes.clear()
         arr = poisson_arrivals(seed + int(load * 100), nrequests, load * sat_rps)
         t = time.perf_counter()
         done = srv.serve(requests(arr))

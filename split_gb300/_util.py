@@ -45,6 +45,21 @@ class Workspace:
         self.view = self.buf[off:off + nbytes]
         self.nbytes = nbytes
 
+    @classmethod
+    def over(cls, buf: torch.Tensor, nbytes: int) -> "Workspace":
+        """A workspace inside an existing uint8 device buffer (kept, not
+        zeroed: the entry points leave their state ready for the next call,
+        whatever layout that call carves)."""
+        ws = cls.__new__(cls)
+        nbytes = max(int(nbytes), 256)
+        off = (-buf.data_ptr()) % 256
+        if buf.numel() < off + nbytes:
+            raise ValueError("buffer too small for the workspace")
+        ws.buf = buf
+        ws.view = buf[off:off + nbytes]
+        ws.nbytes = nbytes
+        return ws
+
     @property
     def ptr(self):
         return C.c_void_p(self.view.data_ptr())

@@ -13,10 +13,41 @@ from ._util import Workspace, ptr, stream_handle
 from .pipeline import Params
 
 
+class Arena:
+    """Device buffers that successive batches bind to instead of allocating
+    their own (a serving loop keeps one per batch in flight).  Capacities
+    grow when a batch needs more; the workspace is zero-filled once, when it
+    is (re)allocated."""
+
+    def __init__(self, device, pixels: int = 0, centroid_floats: int = 0,
+                 workspace_bytes: int = 0, normals: bool = True):
+        self.device = torch.device(device)
+        self.normals_enabled = normals
+        self.px = self.cf = self.wsb = 0
+        self.ensure(pixels, centroid_floats, workspace_bytes)
+
+    def ensure(self, pixels: int, centroid_floats: int, workspace_bytes: int) -> None:
+        d = self.device
+        if pixels > self.px:
+            self.px = pixels
+            self.rgb = torch.zeros(pixels * 3, dtype=torch.uint8, device=d)
+            self.cluster_labels = torch.zeros(pixels, dtype=torch.int32, device=d)
+            self.segment_labels = torch.zeros(pixels, dtype=torch.int32, device=d)
+            self.normals = torch.zeros(pixels * 3, dtype=torch.float32, device=d) \
+                if self.normals_enabled else None
+        if centroid_floats > self.cf:
+            self.cf = centroid_floats
+            self.centroids = torch.zeros(centroid_floats, dtype=torch.float32, device=d)
+        if workspace_bytes > self.wsb:
+            self.wsb = workspace_bytes
+            self.ws_buf = torch.zeros(workspace_bytes + 256, dtype=torch.uint8, device=d)
+
+
 class Batch:
     """Plan + resident arenas for a list of (width, height, K, iterations)."""
 
-    def __init__(self, shapes, params: Params | None = None, device=None, stream=None):
+    def __init__(self, shapes, params: Params | None = None, device=None, stream=None,
+                 arena: Arena | None = None):
         self.params = params or Params()
         self.shapes = [tuple(int(v) for v in s) for s in shapes]
         self.device = torch.device("cuda", torch.cuda.current_device()) if device is None \
@@ -35,13 +66,26 @@ class Batch:
         self.coffsets = [lib.split_batch_centroid_offset(h, i) for i in range(len(self.shapes))]
         nc = lib.split_batch_centroid_floats(h)
         d = self.device
-        self.rgb = torch.zeros(self.arena_px * 3, dtype=torch.uint8, device=d)
-        self.centroids = torch.zeros(nc, dtype=torch.float32, device=d)
-        self.cluster_labels = torch.zeros(self.arena_px, dtype=torch.int32, device=d)
-        self.segment_labels = torch.zeros(self.arena_px, dtype=torch.int32, device=d)
-        self.normals = torch.zeros(self.arena_px * 3, dtype=torch.float32, device=d) \
-            if self.params.compute_normals else None
-        self.ws = Workspace(lib.split_batch_workspace_size(h), d)
+        wsb = lib.split_batch_workspace_size(h)
+        if arena is None:
+            self.rgb = torch.zeros(self.arena_px * 3, dtype=torch.uint8, device=d)
+            self.centroids = torch.zeros(nc, dtype=torch.float32, device=d)
+            self.cluster_labels = torch.zeros(self.arena_px, dtype=torch.int32, device=d)
+            self.segment_labels = torch.zeros(self.arena_px, dtype=torch.int32, device=d)
+            self.normals = torch.zeros(self.arena_px * 3, dtype=torch.float32, device=d) \
+                if self.params.compute_normals else None
+            self.ws = Workspace(wsb, d)
+        else:
+            if self.params.compute_normals and not arena.normals_enabled:
+                raise ValueError("the arena holds no normals")
+            arena.ensure(self.arena_px, nc, wsb)
+            px = self.arena_px
+            self.rgb = arena.rgb[:3 * px]
+            self.centroids = arena.centroids[:nc]
+            self.cluster_labels = arena.cluster_labels[:px]
+            self.segment_labels = arena.segment_labels[:px]
+            self.normals = arena.normals[:3 * px] if self.params.compute_normals else None
+            self.ws = Workspace.over(arena.ws_buf, wsb)
         N.check(lib.split_batch_bind(h, ptr(self.rgb), ptr(self.centroids),
                                      ptr(self.cluster_labels), ptr(self.segment_labels),
                                      ptr(self.normals), self.ws.ptr, self.ws.nbytes,

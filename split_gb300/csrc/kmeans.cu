@@ -341,9 +341,18 @@ __device__ __forceinline__ void nearest_px(const float (&f)[kPx][DIM],
     best[j] = INFINITY;
     lab[j] = 0;
   }
-  while (mask) {
-    const int k = __ffsll((long long)mask) - 1;
-    mask &= mask - 1;
+  // ascending k over the two 32-bit halves of the mask
+  unsigned m = (unsigned)mask, hi = (unsigned)(mask >> 32);
+  int base = 0;
+  for (;;) {
+    if (!m) {
+      if (!hi) break;
+      m = hi;
+      hi = 0;
+      base = 32;
+    }
+    const int k = base + __ffs(m) - 1;
+    m &= m - 1;
     const float4 c0 = *reinterpret_cast<const float4*>(cs + k * CS);
     const float cc[5] = {c0.x, c0.y, c0.z, c0.w, DIM == 5 ? cs[k * CS + 4] : 0.0f};
 #pragma unroll
@@ -381,6 +390,113 @@ __device__ __forceinline__ void flush_acc(Smem& sm, int warp, int l, const float
   }
   const int c = __reduce_add_sync(0xffffffffu, n);
   if (lane == 0) sm.cnt[warp][l] += c;
+}
+
+// Accumulate one batch whose kPx labels are all valid: the same sums, in the
+// same order, as the general path below.
+template <int DIM>
+__device__ __forceinline__ void accumulate_valid(Smem& sm, int warp, const float (&f)[kPx][DIM],
+                                                 const int (&lab)[kPx], int& acc_l, int& acc_n,
+                                                 float (&acc)[DIM]) {
+  const unsigned full = 0xffffffffu;
+  constexpr int CS = cstride(DIM);
+  int mn = min(min(lab[0], lab[1]), min(lab[2], lab[3]));
+  int mx = max(max(lab[0], lab[1]), max(lab[2], lab[3]));
+  mn = __reduce_min_sync(full, mn);
+  mx = __reduce_max_sync(full, mx);
+  if (mn == mx) {
+    if (mn != acc_l) {
+      if (acc_l >= 0) flush_acc<DIM>(sm, warp, acc_l, acc, acc_n);
+      acc_l = mn;
+      acc_n = 0;
+#pragma unroll
+      for (int d = 0; d < DIM; ++d) acc[d] = 0.0f;
+    }
+    float c[DIM];
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) c[d] = sm.cent[mn * CS + d];
+#pragma unroll
+    for (int j = 0; j < kPx; ++j)
+#pragma unroll
+      for (int d = 0; d < DIM; ++d) acc[d] = __fadd_rn(acc[d], __fsub_rn(f[j][d], c[d]));
+    acc_n += kPx;
+    return;
+  }
+  if (acc_l >= 0) flush_acc<DIM>(sm, warp, acc_l, acc, acc_n);
+  acc_l = -1;
+  for (int l = mn; l != INT_MAX;) {
+    float sum[DIM];
+    int c = 0;
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) sum[d] = 0.0f;
+    int nxt = INT_MAX;
+#pragma unroll
+    for (int j = 0; j < kPx; ++j) {
+      if (lab[j] == l) {
+#pragma unroll
+        for (int d = 0; d < DIM; ++d)
+          sum[d] = __fadd_rn(sum[d], __fsub_rn(f[j][d], sm.cent[l * CS + d]));
+        ++c;
+      } else if (lab[j] > l) {
+        nxt = min(nxt, lab[j]);
+      }
+    }
+    flush_acc<DIM>(sm, warp, l, sum, c);
+    l = __reduce_min_sync(full, nxt);
+  }
+}
+
+// A warp span that lies wholly inside the image, with packed features (float4,
+// or RGB8 read as three 32-bit words per 4 pixels) and a candidate mask known
+// for the whole span: no per-pixel bounds checks, one pointer step per batch,
+// the column feature hoisted.  Results equal the general path's.
+template <int LAYOUT, int DIM, int MODE>
+__device__ __forceinline__ void fast_span(const Image& im, Smem& sm, int warp, int row_first,
+                                          int col, int nbatches, unsigned long long mask,
+                                          bool write_labels, int& acc_l, int& acc_n,
+                                          float (&acc)[DIM]) {
+  const int64_t step = (int64_t)kBatchRows * im.width;
+  int64_t px0 = (int64_t)row_first * im.width + col;
+  float fx[kPx];
+#pragma unroll
+  for (int j = 0; j < kPx; ++j) fx[j] = __fmul_rn(im.xy_scale, (float)(col + j));
+  for (int b = 0; b < nbatches; ++b, px0 += step) {
+    float f[kPx][DIM];
+    if (LAYOUT == SPLIT_LAYOUT_FLOAT4) {
+      const float4* p = static_cast<const float4*>(im.points) + px0;
+#pragma unroll
+      for (int j = 0; j < kPx; ++j) {
+        const float4 v = __ldg(p + j);
+        f[j][0] = v.x;
+        f[j][1] = v.y;
+        f[j][2] = v.z;
+      }
+    } else {
+      const uint32_t* p =
+          reinterpret_cast<const uint32_t*>(static_cast<const uint8_t*>(im.points) + 3 * px0);
+      const uint32_t w[3] = {__ldg(p), __ldg(p + 1), __ldg(p + 2)};
+#pragma unroll
+      for (int j = 0; j < kPx; ++j)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          const int byte = 3 * j + c;
+          f[j][c] = sm.lut[(w[byte >> 2] >> (8 * (byte & 3))) & 0xffu];
+        }
+    }
+    if (DIM == 5) {
+      const float fy = __fmul_rn(im.xy_scale, (float)(row_first + b * kBatchRows));
+#pragma unroll
+      for (int j = 0; j < kPx; ++j) {
+        f[j][3] = fx[j];
+        f[j][4] = fy;
+      }
+    }
+    int lab[kPx];
+    nearest_px<DIM>(f, sm.cent, mask, lab);
+    if (write_labels)
+      *reinterpret_cast<int4*>(im.labels + px0) = make_int4(lab[0], lab[1], lab[2], lab[3]);
+    if (MODE != kAssignOnly) accumulate_valid<DIM>(sm, warp, f, lab, acc_l, acc_n, acc);
+  }
 }
 
 // Process one unit (a 64 x 64 tile): assign (unless update-only) and
@@ -435,7 +551,15 @@ __device__ void process_unit(const Image& im, int unit, Smem& sm, bool write_lab
 #pragma unroll
   for (int d = 0; d < DIM; ++d) acc[d] = 0.0f;
 
-  for (int b = 0; b < wrows / kBatchRows; ++b) {
+  const bool fast = MODE != kUpdateOnly && unit_box && vec_labels && rows_in == wrows &&
+                    cols_in == kTile &&
+                    (LAYOUT == SPLIT_LAYOUT_FLOAT4 ||
+                     (LAYOUT == SPLIT_LAYOUT_RGB8 &&
+                      (reinterpret_cast<uintptr_t>(im.points) & 3) == 0));
+  if (fast)
+    fast_span<LAYOUT, DIM, MODE>(im, sm, warp, row0 + lrow, col0 + lcol, wrows / kBatchRows,
+                                 span_mask, write_labels, acc_l, acc_n, acc);
+  for (int b = 0; !fast && b < wrows / kBatchRows; ++b) {
     if (b * kBatchRows >= rows_in) break;
     const int row = row0 + b * kBatchRows + lrow;
     const int col = col0 + lcol;

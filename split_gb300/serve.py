@@ -4,10 +4,14 @@ Requests (an RGB8 image plus its K, iteration count and initial centroids)
 arrive open-loop.  The loop admits them in arrival order while their device
 footprint fits the HBM budget, packs every admitted request into the next
 batch (one fixed launch sequence for the batch, split_batch_*), and keeps up
-to two batches in flight on two streams: while one batch computes, the host
-admits new arrivals and stages the next batch's inputs with asynchronous
-copies from pinned memory.  A request completes when its batch's results are
-back in host memory; its latency runs from its arrival.
+to two batches in flight: while one batch computes, the host admits new
+arrivals and stages the next batch's inputs with asynchronous copies from
+pinned memory.  Each in-flight slot owns a resident arena (RGB, centroid,
+label, normal and workspace buffers, union-find and merge state included)
+that every batch of that slot binds to, so serving allocates no device
+memory once the arenas have grown to the largest batch.  A request completes
+when its batch's results are back in host memory; its latency runs from its
+arrival.
 
 Each request's result is independent of what shares its batch (per-image
 tiles, reduction trees and label spaces), so a result served in a mix equals
@@ -124,7 +128,7 @@ class Server:
 
     def __init__(self, params=None, budget_bytes: int = 40 << 30,
                  max_batch_pixels: int = 64 << 20, depth: int = 2, device=None,
-                 keep_results: bool = True):
+                 keep_results: bool = True, reserve_pixels: int = 0):
         import torch
         from .pipeline import Params
         self.torch = torch
@@ -141,8 +145,27 @@ class Server:
         self.inflight: collections.deque[_Flight] = collections.deque()
         self.completed: list[Request] = []
         self.batches = 0
+        from .batch import Arena
+        # one resident arena per slot; batch i uses slot i % depth, which the
+        # collection order (oldest first) has freed by the time it launches
+        self.arenas = [Arena(self.device, normals=bool(self.params.compute_normals))
+                       for _ in range(depth)]
         self.batch_sizes: list[int] = []
         self.t0 = time.perf_counter()
+        if reserve_pixels > 0:
+            self.reserve(reserve_pixels)
+
+    def reserve(self, pixels: int, max_requests: int = 4096) -> None:
+        """Grow every arena up front to hold a batch of `pixels` pixels (so a
+        timed serving run allocates nothing)."""
+        from .batch import Batch
+        side = 8192
+        probe = Batch([(side, max(1, (pixels + side - 1) // side), 64, 1)], self.params,
+                      self.device, arena=self.arenas[0])
+        wsb = probe.ws.nbytes
+        del probe
+        for a in self.arenas:
+            a.ensure(pixels + 64 * max_requests, self.params.dim * 64 * max_requests, wsb)
 
     def now(self) -> float:
         return time.perf_counter() - self.t0
@@ -158,7 +181,8 @@ class Server:
         from .batch import Batch
         shapes = [(r.rgb.shape[1], r.rgb.shape[0], r.nclusters, r.iters) for r in reqs]
         with torch.cuda.stream(self.h2d):
-            b = Batch(shapes, self.params, self.device, stream=self.h2d)
+            b = Batch(shapes, self.params, self.device, stream=self.h2d,
+                      arena=self.arenas[self.batches % self.depth])
             for i, r in enumerate(reqs):
                 b.rgb_of(i).copy_(self._host(r.rgb), non_blocking=True)
                 b.centroids_of(i).copy_(self._host(r.centroids), non_blocking=True)

@@ -75,3 +75,28 @@ def test_batch_graph_replay(cuda):
         torch.cuda.synchronize()
         assert torch.equal(b.segment_labels, ref_seg)
         assert torch.equal(b.centroids, ref_cen)
+
+
+def test_arena_reuse_across_compositions(cuda):
+    """Batches of different compositions bound in turn to one resident arena
+    (the serving loop's pattern, growing it twice) give the same results as
+    batches with their own fresh buffers."""
+    import torch
+    from split_gb300 import batch, pipeline
+    params = pipeline.Params(merge_P=64)
+    arena = batch.Arena(cuda)
+    comps = [SHAPES[:3], SHAPES[3:8], SHAPES[1:2], SHAPES[5:10], SHAPES[:6]]
+    for comp in comps:
+        imgs, cents = _images(comp, params.dim)
+        a = batch.Batch(comp, params, cuda, arena=arena)
+        a.load(imgs, cents)
+        a.run()
+        f = batch.Batch(comp, params, cuda)
+        f.load(imgs, cents)
+        f.run()
+        torch.cuda.synchronize()
+        a.ws.check("arena batch")
+        for i in range(len(comp)):
+            assert torch.equal(a.segment_labels_of(i), f.segment_labels_of(i))
+            assert torch.equal(a.centroids_of(i), f.centroids_of(i))
+            assert torch.equal(a.normals_of(i), f.normals_of(i))
