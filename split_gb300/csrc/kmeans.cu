@@ -236,7 +236,7 @@ struct Smem {
   float acc[kWarps][kMaxK * kMaxDim];
   int cnt[kWarps][kMaxK];
   float lut[256];
-  int unit[2];   // this unit and the next one, fetched while this one runs
+  int unit;
   int flag;
 };
 
@@ -810,26 +810,18 @@ __global__ void __launch_bounds__(kThreads, SG_KM_MINBLOCKS) kmeans_kernel(Param
   for (int it = 0; it < p.max_iter; ++it) {
     if (blockIdx.x == 0 && threadIdx.x == 0) p.hdr->work_counter[(it + 1) & 1] = 0;
     int cached = -1;
-    unsigned* counter = &p.hdr->work_counter[it & 1];
-    if (threadIdx.x == 0) sm.unit[0] = (int)atomicAdd(counter, 1u);
-    __syncthreads();
-    // sm.unit[k & 1] holds unit k of this block; thread 0 fetches unit k + 1
-    // into the other slot as unit k starts.  Every path through the body below
-    // passes a block barrier after that store and before the next read, and
-    // the store of unit k + 2 comes after every thread has read unit k.
-    for (int k = 0;; ++k) {
-      const int raw = sm.unit[k & 1];
+    for (;;) {
+      if (threadIdx.x == 0) sm.unit = (int)atomicAdd(&p.hdr->work_counter[it & 1], 1u);
+      __syncthreads();
+      const int raw = sm.unit;
+      __syncthreads();
       if (raw >= p.total_units) break;
-      if (threadIdx.x == 0) sm.unit[(k + 1) & 1] = (int)atomicAdd(counter, 1u);
       // odd iterations walk the units backwards: they start on the units the
       // previous iteration touched last, which are still resident in L2
       const int u = (it & 1) ? p.total_units - 1 - raw : raw;
       const int img = find_image(p, u);
       const Image& im = image_of(p, img);
-      if (MODE != kAssignOnly && *(volatile int*)&p.state[img].done) {
-        __syncthreads();
-        continue;
-      }
+      if (MODE != kAssignOnly && *(volatile int*)&p.state[img].done) continue;
       if (img != cached) {
         if (MODE == kAssignOnly)
           load_centroids<DIM>(p.cur + (size_t)img * (kMaxK * 8), im.K, sm.cent);
@@ -843,10 +835,7 @@ __global__ void __launch_bounds__(kThreads, SG_KM_MINBLOCKS) kmeans_kernel(Param
       const bool wl = (MODE == kAssignOnly) ||
                       (MODE == kCluster && (im.threshold >= 0.0f || it == im.max_iter - 1));
       process_unit<LAYOUT, DIM, MODE>(im, lu, sm, wl);
-      if (MODE == kAssignOnly) {
-        __syncthreads();
-        continue;
-      }
+      if (MODE == kAssignOnly) continue;
       block_to_accum(sm, p, img, im.K, DIM);
       // the last unit of the image forms its new centroids
       __threadfence();
