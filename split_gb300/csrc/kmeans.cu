@@ -810,8 +810,12 @@ __global__ void __launch_bounds__(kThreads, SG_KM_MINBLOCKS) kmeans_kernel(Param
   for (int it = 0; it < p.max_iter; ++it) {
     if (blockIdx.x == 0 && threadIdx.x == 0) p.hdr->work_counter[(it + 1) & 1] = 0;
     int cached = -1;
-    for (;;) {
-      if (threadIdx.x == 0) sm.unit = (int)atomicAdd(&p.hdr->work_counter[it & 1], 1u);
+    // the first wave is static (block b takes unit b): only later fetches go
+    // through the work counter, so blocks do not queue on it as they start
+    for (int first = 1;; first = 0) {
+      if (threadIdx.x == 0)
+        sm.unit = first ? (int)blockIdx.x
+                        : (int)gridDim.x + (int)atomicAdd(&p.hdr->work_counter[it & 1], 1u);
       __syncthreads();
       const int raw = sm.unit;
       __syncthreads();
