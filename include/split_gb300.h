@@ -265,6 +265,22 @@ int split_erode_mapped(const int32_t* labels_in, int32_t* labels_out,
 int split_sobel_normals(const float* heights, int width, int height,
                         float depth, float* normals, void* stream);
 
+/* Replaces split::device::sfs::estimate_normals (estimate_normals.cuh:14-18,
+ * estimate_normals.cu:251-308): normals (planar 3 x n) of a shading image
+ * lit from (lx, ly, lz), solving (L L^T (x) I + 2 smoothness * B (x) I3) x =
+ * intensity * L (B: the grid's 5-point Poisson matrix with the reference's
+ * border valence) from x = (0, 0, 1) by red-black block relaxation until
+ * |b - A x| <= tol |b| or max_iter sweeps (the reference: 1e-5, 1500), then
+ * normalised with z >= 0.  smoothness > 0.  *d_iterations (device int,
+ * optional) receives the sweeps performed.  The reference's cuSPARSE
+ * assembly no longer builds with CUDA 12; the system is applied matrix-free
+ * here. */
+size_t split_estimate_normals_workspace_size(int width, int height);
+int split_estimate_normals(const float* intensity, int width, int height, float lx,
+                           float ly, float lz, float smoothness, int max_iter,
+                           float tol, float* normals, int32_t* d_iterations,
+                           void* workspace, size_t workspace_bytes, void* stream);
+
 /* Normals from an RGB8 image: heights = luminance L* / 100 (fused, the
  * luminance plane is never written). */
 int split_sobel_normals_rgb8(const uint8_t* rgb, int width, int height,

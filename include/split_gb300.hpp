@@ -316,6 +316,27 @@ inline void sobel_normals(const_view2d<float> heights, view2d<float> normals, fl
         "sfs::sobel_normals");
 }
 
+/* sfs/estimate_normals.cuh:14-18: H x W shading intensity lit from L ->
+ * 3 x N planar normals; relaxation to |b - A x| <= tol |b| (the reference:
+ * 1e-5, 1500 sweeps).  Returns the sweeps performed (synchronises). */
+inline int estimate_normals(const_view2d<float> shading_intensity, float3 light_vector,
+                            view2d<float> normals, float smoothness_weight, Temp& temp,
+                            int max_iter = 1500, float tol = 1e-5f,
+                            cudaStream_t stream = nullptr) {
+  const int w = (int)shading_intensity.num_cols(), h = (int)shading_intensity.num_rows();
+  temp.reserve(split_estimate_normals_workspace_size(w, h));
+  check(split_estimate_normals(shading_intensity.data(), w, h, light_vector.x, light_vector.y,
+                               light_vector.z, smoothness_weight, max_iter, tol, normals.data(),
+                               temp.scalar(2), temp.get(), temp.size(), stream),
+        "sfs::estimate_normals");
+  int iters = 0;
+  check_cuda(cudaMemcpyAsync(&iters, temp.scalar(2), sizeof(int), cudaMemcpyDeviceToHost, stream),
+             "sfs::estimate_normals: sweeps");
+  check_cuda(cudaStreamSynchronize(stream), "sfs::estimate_normals: sync");
+  temp.check(stream);
+  return iters;
+}
+
 }  // namespace sfs
 
 }  // namespace device

@@ -186,3 +186,57 @@ def lab_beta_f64(rgb: np.ndarray, mu: float = 1e5):
     achrom = (np.abs(a) < lam) & (np.abs(b) < lam)
     beta = np.where(achrom & (L < lo), -mu, np.where(achrom & (L > hi), mu, 0.0))
     return np.stack([beta, a, b]), L
+
+
+def estimate_normals_rb(intensity: np.ndarray, light, smoothness: float, max_iter: int = 1500,
+                        tol: float = 1e-5):
+    """Shape-from-shading normals (split/src/split/device/sfs/estimate_normals.cu:251-308)
+    in FP64: the system (L L^T (x) I + 2 smoothness * B (x) I3) x = intensity * L
+    (B: 5-point Poisson matrix, diagonal 4 - [row on border] - [column on border],
+    estimate_normals.cu:124-171) relaxed from x = (0, 0, 1) by red-black block
+    Gauss-Seidel sweeps (each pixel's 3 x 3 block c I + L L^T solved exactly)
+    until |b - A x| <= tol |b| or max_iter sweeps, then normalised with z >= 0.
+    The system is singular (constant fields perpendicular to L are free), so
+    the converged normals depend on the relaxation order: this restates the
+    order the CUDA path uses.  Returns ((3, N) normals, sweeps)."""
+    s = np.asarray(intensity, np.float64)
+    h, w = s.shape
+    L = np.asarray(light, np.float64)
+    L = L / np.sqrt((L * L).sum())
+    lam2 = 2.0 * smoothness
+    rr, cc = np.mgrid[0:h, 0:w]
+    val = 4.0 - ((rr == 0) | (rr == h - 1)) - ((cc == 0) | (cc == w - 1))
+    x = np.zeros((3, h, w))
+    x[2] = 1.0
+
+    def nsum(x):
+        S = np.zeros_like(x)
+        S[:, 1:, :] += x[:, :-1, :]
+        S[:, :-1, :] += x[:, 1:, :]
+        S[:, :, 1:] += x[:, :, :-1]
+        S[:, :, :-1] += x[:, :, 1:]
+        return S
+
+    b = L[:, None, None] * s[None]
+    bn = np.sqrt((b * b).sum())
+    colour = (rr + cc) & 1
+    it = 0
+    while True:
+        S = nsum(x)
+        lx = (L[:, None, None] * x).sum(0)
+        ax = L[:, None, None] * lx[None] + lam2 * (val[None] * x - S)
+        r = b - ax
+        if np.sqrt((r * r).sum()) <= tol * bn or it >= max_iter:
+            break
+        for c in (0, 1):
+            S = nsum(x)
+            rv = b + lam2 * S
+            cdiag = lam2 * val
+            q = (L[:, None, None] * rv).sum(0) / (cdiag + 1.0)
+            new = (rv - L[:, None, None] * q[None]) / cdiag[None]
+            m = colour == c
+            x[:, m] = new[:, m]
+        it += 1
+    n = np.sqrt((x * x).sum(0))
+    out = np.stack([x[0] / n, x[1] / n, np.abs(x[2]) / n]).reshape(3, -1)
+    return out, it

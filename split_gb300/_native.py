@@ -57,6 +57,10 @@ _SIGS = {
     "split_tune_set": (C.c_int, [C.c_void_p, C.c_int]),
     "split_merge_smooth_workspace_size": (C.c_size_t, [C.c_int, C.c_int]),
     "split_pack_lab_beta_workspace_size": (C.c_size_t, [C.c_int64]),
+    "split_estimate_normals_workspace_size": (C.c_size_t, [C.c_int, C.c_int]),
+    "split_estimate_normals": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_float, C.c_float,
+                                         C.c_float, C.c_float, C.c_int, C.c_float, C.c_void_p,
+                                         C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p]),
     "split_pack_lab_beta": (C.c_int, [C.c_void_p, C.c_int64, C.c_float, C.c_int, C.c_void_p,
                                       C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p]),
     "split_merge_smooth": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_float,

@@ -449,3 +449,43 @@ def test_pipeline_lab_beta_features(cuda):
     seg = oracle.ccl(cl.reshape(h, w), 8, 0)
     seg = oracle.merge_small(seg, 32, 0)
     assert np.array_equal(pipe.segment_labels.cpu().numpy(), oracle.erode(seg, 1))
+
+
+@pytest.mark.parametrize("shape,light,lam,tol", [((24, 32), (0.3, -0.2, 1.0), 0.5, 1e-5),
+                                                ((61, 47), (-1.0, 0.5, 2.0), 1.0, 1e-6),
+                                                ((1, 40), (0.0, 0.0, 1.0), 0.25, 1e-5),
+                                                ((33, 1), (0.2, 0.9, 0.4), 2.0, 1e-5)])
+def test_estimate_normals(cuda, shape, light, lam, tol):
+    """SOR shape-from-shading normals against the FP64 restatement of the same
+    relaxation: within 1e-4 rad, sweep counts within one, unit length, z >= 0."""
+    import torch
+    from split_gb300 import sfs
+    rng = np.random.default_rng(shape[0] * 7 + shape[1])
+    s = rng.random(shape, dtype=np.float32)
+    ref, ref_it = oracle.estimate_normals_rb(s, light, lam, 5000, tol)
+    out = torch.empty((3, s.size), dtype=torch.float32, device=cuda)
+    its = torch.zeros(1, dtype=torch.int32, device=cuda)
+    ws = sfs.estimate_normals(_t(s, cuda), light, out, lam, max_iter=5000, tol=tol,
+                              iterations_out=its)
+    torch.cuda.synchronize()
+    ws.check("estimate_normals")
+    got = out.cpu().numpy().astype(np.float64)
+    assert abs(int(its.item()) - ref_it) <= 1, (int(its.item()), ref_it)
+    np.testing.assert_allclose(np.linalg.norm(got, axis=0), 1.0, atol=1e-6)
+    assert (got[2] >= 0).all()
+    ang = np.arctan2(np.linalg.norm(np.cross(got.T, ref.T), axis=1), (got * ref).sum(0))
+    assert ang.max() <= 1e-4
+
+
+def test_estimate_normals_limits(cuda):
+    import torch
+    from split_gb300 import _native, sfs
+    s = torch.rand((8, 8), device=cuda)
+    out = torch.empty((3, 64), device=cuda)
+    sfs.estimate_normals(s, (1.0, 1.0, 1.0), out, 0.5, max_iter=0)   # no sweep: x0
+    torch.cuda.synchronize()
+    assert torch.equal(out[2], torch.ones(64, device=cuda)) and (out[:2] == 0).all()
+    with pytest.raises(_native.SplitError):
+        sfs.estimate_normals(s, (1.0, 1.0, 1.0), out, 0.0)       # no smoothness: singular
+    with pytest.raises(_native.SplitError):
+        sfs.estimate_normals(s, (0.0, 0.0, 0.0), out, 0.5)       # no light direction
