@@ -418,7 +418,7 @@ unsigned long long split_launch_count(void);
 #define SPLIT_TUNE_MAX_ENTRIES 64
 typedef struct {
   int64_t max_pixels;        /* upper bound of the class (entries ascending) */
-  int kmeans_unit_rows;      /* 64 or 128: rows of a k-means work unit       */
+  int kmeans_unit_rows;      /* 16, 32, 64 or 128: rows of a k-means unit    */
   int kmeans_blocks_per_sm;  /* 0 = as many as fit, else 1..8 (capped)       */
 } split_tune_entry;
 

@@ -7,8 +7,8 @@
 // matrix, the radix sort per iteration or the host round trip per iteration.
 //
 // Work decomposition (fixed per image, so a result never depends on what else
-// shares the launch): an image is cut into units (tiles of 64 or 128 rows by
-// 64 columns); blocks take units from a device work counter.  Per unit, every
+// shares the launch): an image is cut into units (tiles of 16, 32, 64 or 128
+// rows by 64 columns); blocks take units from a device work counter.  Per unit, every
 // warp accumulates (x - c_label) over its pixel batches in FP32 registers and
 // a warp-private shared-memory slot (warp butterfly sums per distinct label),
 // and the block sums the 8 warp slots in warp order: the unit partial, a
@@ -16,8 +16,14 @@
 // exactly: each is rounded to a multiple of 2^-24 and added as a 96-bit
 // fixed-point integer (64-bit atomics on a low and a high word).  Integer
 // addition does not depend on order, so the image total is the same whatever
-// order units finish in and whatever else shares the launch.  The last unit
-// of an image forms c_new = c + S / n in FP64, rounded to FP32.
+// order units finish in and whatever else shares the launch.  A unit ends with
+// fire-and-forget adds and one block barrier: no fence, no arrival counter.
+// The grid barrier that ends the iteration publishes the sums; then every
+// block that works on the image in the next iteration forms c_new = c + S / n
+// in FP64, rounded to FP32, from the same inputs (bit-identical in every
+// block), and one owner block publishes it (form_centroids).  The sums are
+// kept in three slots by iteration, so the owner can clear the slot of the
+// iteration after next while the current slot fills and the last one is read.
 #include <limits.h>
 #include <math.h>
 #include <string.h>
@@ -35,7 +41,7 @@ namespace km {
 #endif
 constexpr int kThreads = 256;
 constexpr int kWarps = kThreads / 32;
-// A unit is a tile of unit_rows x kTile pixels (unit_rows = 64 or 128, per
+// A unit is a tile of unit_rows x kTile pixels (unit_rows = 16 to 128, per
 // image from the tuning table); warp w owns rows [w * r, (w + 1) * r) of it,
 // r = unit_rows / 8.
 constexpr int kTile = 64;
@@ -83,12 +89,12 @@ struct Params {
   int nimages;
   int total_units;
   int max_iter;
-  unsigned long long* acc_lo;  // [nimages][kMaxK * kMaxDim] low 32-bit words of the sums
-  unsigned long long* acc_hi;  // [nimages][kMaxK * kMaxDim] high words (signed)
-  unsigned* acc_cnt;           // [nimages][kMaxK] member counts
-  float* cur;                  // [2][nimages][kMaxK * 8]
-  unsigned* image_cnt;         // [nimages] units finished this iteration
-  ImageState* state;     // [nimages]
+  // sums of iteration i live in slot i % 3 (see form_centroids)
+  unsigned long long* acc_lo;  // [3][nimages][kMaxK * kMaxDim] low 32-bit words of the sums
+  unsigned long long* acc_hi;  // [3][nimages][kMaxK * kMaxDim] high words (signed)
+  unsigned* acc_cnt;           // [3][nimages][kMaxK] member counts
+  float* cur;                  // [2][nimages][kMaxK * 8]: centroids of iteration i in i & 1
+  ImageState* state;     // [2][nimages]: state after iteration i - 1 in slot i & 1
   WsHeader* hdr;
   int blocks_per_sm;     // 0: as many as fit (host side only)
 };
@@ -97,6 +103,10 @@ constexpr int cstride(int dim) { return dim == 3 ? 4 : 8; }
 
 __device__ __forceinline__ const Image& image_of(const Params& p, int i) {
   return p.images ? p.images[i] : p.img0;
+}
+
+__device__ __forceinline__ size_t acc_slot(const Params& p, int slot, int img) {
+  return (size_t)slot * p.nimages + img;
 }
 
 __device__ __forceinline__ int find_image(const Params& p, int unit) {
@@ -236,8 +246,8 @@ struct Smem {
   float acc[kWarps][kMaxK * kMaxDim];
   int cnt[kWarps][kMaxK];
   float lut[256];
-  int unit;
-  int flag;
+  int next[2];
+  int more;
 };
 
 // Advance a (row, col) pair by s pixels along the row-major order.
@@ -688,10 +698,10 @@ __device__ void process_unit(const Image& im, int unit, Smem& sm, bool write_lab
 // Sums the block's 8 warp slots in warp order (the unit partial), clears
 // them, and adds the partial into the image accumulators (96-bit fixed point:
 // low 32 bits and the signed rest in two 64-bit words).
-__device__ void block_to_accum(Smem& sm, const Params& p, int img, int K, int dim) {
+__device__ void block_to_accum(Smem& sm, const Params& p, int img, int K, int dim, int slot) {
   __syncthreads();
-  unsigned long long* lo = p.acc_lo + (size_t)img * (kMaxK * kMaxDim);
-  unsigned long long* hi = p.acc_hi + (size_t)img * (kMaxK * kMaxDim);
+  unsigned long long* lo = p.acc_lo + acc_slot(p, slot, img) * (kMaxK * kMaxDim);
+  unsigned long long* hi = p.acc_hi + acc_slot(p, slot, img) * (kMaxK * kMaxDim);
   for (int idx = threadIdx.x; idx < K * kMaxDim; idx += blockDim.x) {
     float s = 0.0f;
 #pragma unroll
@@ -713,7 +723,7 @@ __device__ void block_to_accum(Smem& sm, const Params& p, int img, int K, int di
       c += sm.cnt[w][k];
       sm.cnt[w][k] = 0;
     }
-    if (c) atomicAdd(p.acc_cnt + (size_t)img * kMaxK + k, (unsigned)c);
+    if (c) atomicAdd(p.acc_cnt + acc_slot(p, slot, img) * kMaxK + k, (unsigned)c);
   }
 }
 
@@ -727,17 +737,48 @@ __device__ __forceinline__ void load_centroids(const float* src, int K,
   }
 }
 
-// Image-level finish: new centroids c + S / n (empty cluster: unchanged),
-// convergence test of cluster.cu:71-88, outputs on the last iteration.
+// Centroids of iteration i >= 1 of an image, c(i) = c(i-1) + S(i-1) / n
+// (empty cluster: unchanged; cluster.cu:71-88), formed after the grid barrier
+// that ended iteration i - 1, and the convergence test of that iteration.
+//
+// Every block that works on the image in iteration i calls this with the same
+// inputs, which nobody writes during iteration i (c(i-1) in cur[(i-1) & 1],
+// the sums in slot (i-1) % 3, the state after iteration i-2 in state[(i-1) &
+// 1]), so all of them get bit-identical centroids and the same decision.  The
+// image's owner block (img = blockIdx.x mod gridDim.x) also publishes: c(i) to
+// cur[i & 1], the state after iteration i-1 to state[i & 1], zeros for slot
+// (i+1) % 3 (read for the last time in iteration i-1, written again in
+// iteration i+1), and on convergence the caller's centroids and iteration
+// count.  Returns whether the image runs iteration i (uniform in the block);
+// its centroids are left in `cent` (stride cstride(DIM)).
 template <int DIM, int MODE>
-__device__ void finish_image(const Params& p, int img, const Image& im, int it) {
-  __shared__ float sdelta;
-  const float* c_old = p.cur + ((size_t)(it & 1) * p.nimages + img) * (kMaxK * 8);
-  float* c_new = p.cur + ((size_t)((it + 1) & 1) * p.nimages + img) * (kMaxK * 8);
-  unsigned long long* lo = p.acc_lo + (size_t)img * (kMaxK * kMaxDim);
-  unsigned long long* hi = p.acc_hi + (size_t)img * (kMaxK * kMaxDim);
-  unsigned* cnt = p.acc_cnt + (size_t)img * kMaxK;
+__device__ bool form_centroids(const Params& p, int img, const Image& im, int i, float* cent,
+                               bool owner) {
+  constexpr int CS = cstride(DIM);
   __shared__ float sdiff[kMaxK * kMaxDim];
+  __shared__ int smore, sstopped;
+  const ImageState* prev = p.state + acc_slot(p, (i - 1) & 1, img);
+  ImageState* next = p.state + acc_slot(p, i & 1, img);
+  // one reader, so the whole block takes the same branch
+  if (threadIdx.x == 0) sstopped = __ldcg(&prev->done);
+  __syncthreads();
+  if (sstopped) {
+    // stopped earlier: carry the state forward
+    if (owner && threadIdx.x == 0) {
+      next->delta = __ldcg(&prev->delta);
+      next->old_delta = __ldcg(&prev->old_delta);
+      next->iters = __ldcg(&prev->iters);
+      next->done = 1;
+    }
+    __syncthreads();
+    return false;
+  }
+  const size_t sb = acc_slot(p, (i - 1) % 3, img);
+  const unsigned long long* lo = p.acc_lo + sb * (kMaxK * kMaxDim);
+  const unsigned long long* hi = p.acc_hi + sb * (kMaxK * kMaxDim);
+  const unsigned* cnt = p.acc_cnt + sb * kMaxK;
+  const float* c_old = p.cur + acc_slot(p, (i - 1) & 1, img) * (kMaxK * 8);
+  float* c_new = p.cur + acc_slot(p, i & 1, img) * (kMaxK * 8);
   for (int idx = threadIdx.x; idx < im.K * DIM; idx += blockDim.x) {
     const int k = idx / DIM, d = idx % DIM, a = k * kMaxDim + d;
     const float c = __ldcg(c_old + k * 8 + d);
@@ -750,51 +791,51 @@ __device__ void finish_image(const Params& p, int img, const Image& im, int it) 
       const double S = __dmul_rn(__dadd_rn(__dmul_rn(h, 4294967296.0), l), 1.0 / 16777216.0);
       cn = __double2float_rn(__dadd_rn((double)c, __ddiv_rn(S, (double)n)));
     }
-    __stcg(c_new + k * 8 + d, cn);
+    cent[k * CS + d] = cn;
+    if (owner) __stcg(c_new + k * 8 + d, cn);
     const float df = __fsub_rn(cn, c);
     sdiff[idx] = __fmul_rn(df, df);
   }
-  __syncthreads();
-  // the accumulators start the next iteration at zero (every unit of this
-  // image has been added, and nothing adds to it before the grid barrier)
-  for (int idx = threadIdx.x; idx < im.K * kMaxDim; idx += blockDim.x) {
-    __stcg(lo + idx, 0ull);
-    __stcg(hi + idx, 0ull);
+  if (owner) {
+    const size_t zb = acc_slot(p, (i + 1) % 3, img);
+    for (int idx = threadIdx.x; idx < im.K * kMaxDim; idx += blockDim.x) {
+      __stcg(p.acc_lo + zb * (kMaxK * kMaxDim) + idx, 0ull);
+      __stcg(p.acc_hi + zb * (kMaxK * kMaxDim) + idx, 0ull);
+    }
+    for (int k = threadIdx.x; k < im.K; k += blockDim.x) __stcg(p.acc_cnt + zb * kMaxK + k, 0u);
   }
-  for (int k = threadIdx.x; k < im.K; k += blockDim.x) __stcg(cnt + k, 0u);
+  __syncthreads();
   if (threadIdx.x < 32) {
     // squared centroid shift, summed in a fixed order
     float acc = 0.0f;
     for (int idx = threadIdx.x; idx < im.K * DIM; idx += 32) acc = __fadd_rn(acc, sdiff[idx]);
     acc = warp_sum(acc);
-    if (threadIdx.x == 0) sdelta = acc;
-  }
-  __syncthreads();
-  __shared__ int sdone;
-  if (threadIdx.x == 0) {
-    // state is shared across blocks: volatile accesses bypass the
-    // incoherent L1
-    volatile ImageState* vs = p.state + img;
-    const int iters = vs->iters + 1;
-    const float old_delta = vs->delta;
-    const float delta = sqrtf(sdelta);
-    bool more = iters < im.max_iter && fabsf(delta - old_delta) > im.threshold;
-    if (MODE == kUpdateOnly) more = false;
-    vs->old_delta = old_delta;
-    vs->delta = delta;
-    vs->iters = iters;
-    vs->done = more ? 0 : 1;
-    sdone = more ? 0 : 1;
-    if (im.d_iterations && !more) *im.d_iterations = iters;
-  }
-  __syncthreads();
-  // final centroids back to the caller's planar array
-  if (sdone) {
-    for (int idx = threadIdx.x; idx < im.K * DIM; idx += blockDim.x) {
-      const int k = idx / DIM, d = idx % DIM;
-      im.centroids[d * im.K + k] = __ldcg(c_new + k * 8 + d);
+    if (threadIdx.x == 0) {
+      const float delta = sqrtf(acc);
+      const float old_delta = __ldcg(&prev->delta);
+      bool more = i < im.max_iter && fabsf(delta - old_delta) > im.threshold;
+      if (MODE == kUpdateOnly) more = false;
+      smore = more ? 1 : 0;
+      if (owner) {
+        next->delta = delta;
+        next->old_delta = old_delta;
+        next->iters = i;
+        next->done = more ? 0 : 1;
+        if (im.d_iterations && !more) *im.d_iterations = i;
+      }
     }
   }
+  __syncthreads();
+  const bool more = smore != 0;
+  if (owner && !more) {
+    // final centroids back to the caller's planar array
+    for (int idx = threadIdx.x; idx < im.K * DIM; idx += blockDim.x) {
+      const int k = idx / DIM, d = idx % DIM;
+      im.centroids[d * im.K + k] = cent[k * CS + d];
+    }
+  }
+  __syncthreads();
+  return more;
 }
 
 template <int LAYOUT, int DIM, int MODE>
@@ -807,57 +848,71 @@ __global__ void __launch_bounds__(kThreads, SG_KM_MINBLOCKS) kmeans_kernel(Param
     for (int i = threadIdx.x; i < 256; i += blockDim.x) sm.lut[i] = (float)i / 255.0f;
   __syncthreads();
 
+  bool stopped = false;   // a single image that converged: no iterations left
   for (int it = 0; it < p.max_iter; ++it) {
     if (blockIdx.x == 0 && threadIdx.x == 0) p.hdr->work_counter[(it + 1) & 1] = 0;
     int cached = -1;
-    // the first wave is static (block b takes unit b): only later fetches go
-    // through the work counter, so blocks do not queue on it as they start
-    for (int first = 1;; first = 0) {
-      if (threadIdx.x == 0)
-        sm.unit = first ? (int)blockIdx.x
-                        : (int)gridDim.x + (int)atomicAdd(&p.hdr->work_counter[it & 1], 1u);
-      __syncthreads();
-      const int raw = sm.unit;
-      __syncthreads();
-      if (raw >= p.total_units) break;
+    bool more = false;      // the cached image runs this iteration
+    if (MODE != kAssignOnly && it > 0) {
+      // owners publish their images' centroids first; a single image is
+      // formed by every block here, so all of them see it converge together
+      const int first = p.nimages == 1 ? 0 : (int)blockIdx.x;
+      const bool owner = p.nimages > 1 || blockIdx.x == 0;
+      for (int img = first; img < p.nimages; img += gridDim.x) {
+        more = form_centroids<DIM, MODE>(p, img, image_of(p, img), it, sm.cent, owner);
+        cached = img;
+      }
+      if (p.nimages == 1 && !more) {
+        stopped = true;
+        break;
+      }
+    }
+    // The first wave is static (block b takes unit b): only later fetches go
+    // through the work counter, so blocks do not queue on it as they start.
+    int raw = (int)blockIdx.x;
+    for (int k = 0; raw < p.total_units; ++k) {
       // odd iterations walk the units backwards: they start on the units the
       // previous iteration touched last, which are still resident in L2
       const int u = (it & 1) ? p.total_units - 1 - raw : raw;
       const int img = find_image(p, u);
       const Image& im = image_of(p, img);
-      if (MODE != kAssignOnly && *(volatile int*)&p.state[img].done) continue;
       if (img != cached) {
-        if (MODE == kAssignOnly)
+        if (MODE == kAssignOnly) {
           load_centroids<DIM>(p.cur + (size_t)img * (kMaxK * 8), im.K, sm.cent);
-        else
-          load_centroids<DIM>(p.cur + ((size_t)(it & 1) * p.nimages + img) * (kMaxK * 8),
-                              im.K, sm.cent);
+          more = true;
+        } else if (it == 0) {
+          load_centroids<DIM>(p.cur + acc_slot(p, 0, img) * (kMaxK * 8), im.K, sm.cent);
+          if (threadIdx.x == 0) sm.more = !__ldcg(&p.state[img].done);
+        } else {
+          more = form_centroids<DIM, MODE>(p, img, im, it, sm.cent, false);
+        }
         cached = img;
         __syncthreads();
+        if (MODE != kAssignOnly && it == 0) more = sm.more != 0;
       }
-      const int lu = u - im.unit_begin;
-      const bool wl = (MODE == kAssignOnly) ||
-                      (MODE == kCluster && (im.threshold >= 0.0f || it == im.max_iter - 1));
-      process_unit<LAYOUT, DIM, MODE>(im, lu, sm, wl);
-      if (MODE == kAssignOnly) continue;
-      block_to_accum(sm, p, img, im.K, DIM);
-      // the last unit of the image forms its new centroids
-      __threadfence();
-      __syncthreads();
-      if (threadIdx.x == 0) {
-        const unsigned prev = atomicAdd(&p.image_cnt[img], 1u);
-        sm.flag = (prev == (unsigned)im.nunits - 1);
-        if (sm.flag) p.image_cnt[img] = 0;
+      if (more) {
+        const int lu = u - im.unit_begin;
+        const bool wl = (MODE == kAssignOnly) ||
+                        (MODE == kCluster && (im.threshold >= 0.0f || it == im.max_iter - 1));
+        process_unit<LAYOUT, DIM, MODE>(im, lu, sm, wl);
+        if (MODE != kAssignOnly) block_to_accum(sm, p, img, im.K, DIM, it % 3);
       }
+      // the last warp fetches the next unit (slot k & 1 was last read before
+      // the barrier that ended unit k - 1)
+      if (threadIdx.x == kThreads - 32)
+        sm.next[k & 1] = (int)gridDim.x + (int)atomicAdd(&p.hdr->work_counter[it & 1], 1u);
       __syncthreads();
-      if (!sm.flag) continue;
-      __threadfence();
-      finish_image<DIM, MODE>(p, img, im, it);
-      __syncthreads();
+      raw = sm.next[k & 1];
     }
-    if (MODE == kAssignOnly) break;
+    if (MODE == kAssignOnly) return;
+    // the barrier publishes every block's sums (fire-and-forget adds ordered
+    // by the block barrier before the arrival's release)
     if (!grid_barrier(p.hdr)) return;
   }
+  if (MODE == kAssignOnly || stopped) return;
+  // centroids after the last iteration; every image stops here
+  for (int img = (int)blockIdx.x; img < p.nimages; img += gridDim.x)
+    form_centroids<DIM, MODE>(p, img, image_of(p, img), p.max_iter, sm.cent, true);
 }
 
 // ---------------------------------------------------------------------------
@@ -869,7 +924,6 @@ struct Layout {
   unsigned long long* acc_hi;
   unsigned* acc_cnt;
   float* cur;
-  unsigned* image_cnt;
   ImageState* state;
   Image* images;
   WsHeader* hdr;
@@ -887,26 +941,25 @@ static Layout carve(void* ws, int nimages) {
   Carver c(ws);
   Layout l;
   l.hdr = c.take<WsHeader>(1);
-  l.acc_lo = c.take<unsigned long long>((size_t)nimages * kMaxK * kMaxDim);
-  l.acc_hi = c.take<unsigned long long>((size_t)nimages * kMaxK * kMaxDim);
-  l.acc_cnt = c.take<unsigned>((size_t)nimages * kMaxK);
+  l.acc_lo = c.take<unsigned long long>((size_t)3 * nimages * kMaxK * kMaxDim);
+  l.acc_hi = c.take<unsigned long long>((size_t)3 * nimages * kMaxK * kMaxDim);
+  l.acc_cnt = c.take<unsigned>((size_t)3 * nimages * kMaxK);
   l.cur = c.take<float>((size_t)2 * nimages * kMaxK * 8);
-  l.image_cnt = c.take<unsigned>((size_t)nimages);
-  l.state = c.take<ImageState>((size_t)nimages);
+  l.state = c.take<ImageState>((size_t)2 * nimages);
   l.images = nimages > 1 ? c.take<Image>((size_t)nimages) : nullptr;
   l.bytes = c.size();
   return l;
 }
 
-// Header words used by the barrier and the work counters, the accumulators
-// and the arrival counters start every call at zero (a call that stopped
-// early, or a workspace used by another call, may have left data there).
+// Header words used by the barrier and the work counters and all three
+// accumulator slots start every call at zero (a call that stopped early, or
+// a workspace used by another call, may have left data there).
 static int reset_counters(const Layout& l, int nimages, cudaStream_t st) {
+  (void)nimages;
   SG_CUDA_TRY(cudaMemsetAsync(reinterpret_cast<char*>(l.hdr) + sizeof(int), 0,
                               sizeof(unsigned) * 4, st));
   SG_CUDA_TRY(cudaMemsetAsync(l.acc_lo, 0, reinterpret_cast<char*>(l.cur) -
                                                reinterpret_cast<char*>(l.acc_lo), st));
-  SG_CUDA_TRY(cudaMemsetAsync(l.image_cnt, 0, sizeof(unsigned) * (size_t)nimages, st));
   return SPLIT_OK;
 }
 
@@ -1046,7 +1099,6 @@ static int run(int mode, const void* points, int layout, int dim, int64_t n,
   p.acc_hi = l.acc_hi;
   p.acc_cnt = l.acc_cnt;
   p.cur = l.cur;
-  p.image_cnt = l.image_cnt;
   p.state = l.state;
   p.hdr = l.hdr;
   SG_TRY(reset_counters(l, 1, st));
@@ -1173,8 +1225,8 @@ extern "C" int split_kmeans_propagate(const int32_t* labels, int64_t npoints,
 // file-scope device array of fixed size, so a call needs no workspace.
 //
 // Limits and sharing rules:
-//   - the array holds the state of one image (accumulators, centroids,
-//     counters: about 10 KB); the entry point supports images of at most
+//   - the array holds the state of one image (three accumulator slots,
+//     centroids, state: about 21 KB); the entry point supports images of at most
 //     kStaticTiles 64 x 64 tiles (2048: a 3840 x 2160 frame fits) and rejects
 //     larger ones with SPLIT_ERR_WORKSPACE before anything is launched;
 //   - every GPU that loads the library holds the array until the process
@@ -1195,13 +1247,12 @@ constexpr int kStaticTiles = 2048;
 // 256-byte boundary).
 constexpr size_t round256(size_t v) { return (v + 255) & ~size_t(255); }
 constexpr size_t kStaticBytes =
-    round256(round256(round256(round256(round256(round256(round256(sizeof(WsHeader)) +
-                                                          (size_t)kMaxK * kMaxDim * 8) +
-                                                 (size_t)kMaxK * kMaxDim * 8) +
-                                        (size_t)kMaxK * 4) +
-                               (size_t)2 * kMaxK * 8 * 4) +
-                      4) +
-             sizeof(ImageState));
+    round256(round256(round256(round256(round256(round256(sizeof(WsHeader)) +
+                                                 (size_t)3 * kMaxK * kMaxDim * 8) +
+                                        (size_t)3 * kMaxK * kMaxDim * 8) +
+                               (size_t)3 * kMaxK * 4) +
+                      (size_t)2 * kMaxK * 8 * 4) +
+             (size_t)2 * sizeof(ImageState));
 
 static __device__ __align__(256) unsigned char g_static_scratch[kStaticBytes];
 
@@ -1354,7 +1405,6 @@ int kmeans_batch_run(const KmBatchPlan& plan, void* ws, cudaStream_t st) {
   p.acc_hi = l.acc_hi;
   p.acc_cnt = l.acc_cnt;
   p.cur = l.cur;
-  p.image_cnt = l.image_cnt;
   p.state = l.state;
   p.hdr = l.hdr;
   p.blocks_per_sm = plan.blocks_per_sm;
@@ -1379,7 +1429,9 @@ extern "C" int split_tune_set(const split_tune_entry* entries, int n) {
     const split_tune_entry& e = entries[i];
     if (e.max_pixels <= 0 || (i > 0 && e.max_pixels <= entries[i - 1].max_pixels))
       return SPLIT_ERR_INVALID;
-    if (e.kmeans_unit_rows != 64 && e.kmeans_unit_rows != 128) return SPLIT_ERR_INVALID;
+    if (e.kmeans_unit_rows != 16 && e.kmeans_unit_rows != 32 && e.kmeans_unit_rows != 64 &&
+        e.kmeans_unit_rows != 128)
+      return SPLIT_ERR_INVALID;
     if (e.kmeans_blocks_per_sm < 0 || e.kmeans_blocks_per_sm > 8) return SPLIT_ERR_INVALID;
   }
   sg::km::TuneTable& t = sg::km::tune_table();

@@ -1,9 +1,9 @@
 """Autotuner for the launch choices of the segmentation path.
 
 What it tunes (split_tune_entry, include/split_gb300.h), per image size class:
-  * the k-means work-unit height (64 or 128 rows of 64 columns), which trades
-    per-unit reduction overhead against load balance and the tail of the
-    launch, and
+  * the k-means work-unit height (16, 32, 64 or 128 rows of 64 columns),
+    which trades per-unit reduction overhead against load balance, the
+    parallelism of small images and the tail of the launch, and
   * the resident blocks per SM of the cooperative k-means launch.
 
 Every candidate is timed on the GPU in use with the clustering workload of
@@ -27,7 +27,7 @@ import statistics
 
 from . import _native as N
 
-UNIT_ROWS = (64, 128)
+UNIT_ROWS = (64, 128, 32, 16)
 BLOCKS_PER_SM = (0, 2, 1)
 # representative sizes of the classes (width, height); a class ends halfway
 # (geometrically) between its size and the next one

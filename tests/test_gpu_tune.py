@@ -1,4 +1,4 @@
-"""Tuned launch choices on the GPU: 128-row k-means units keep the parity
+"""Tuned launch choices on the GPU: 16- to 128-row k-means units keep the parity
 bar, an image keeps bit-identical results alone and in a batch whatever the
 table says for other sizes, the allocation-free entry point follows the
 table, and the autotuner produces and caches a valid table."""
@@ -23,11 +23,11 @@ def _t(a, dev):
     return torch.from_numpy(np.ascontiguousarray(a)).to(dev)
 
 
-@pytest.mark.parametrize("layout", [0, 1, 2])
-def test_kmeans_lockstep_128_row_units(cuda, table, layout):
+@pytest.mark.parametrize("rows,layout", [(128, 0), (128, 1), (128, 2), (32, 1), (16, 0), (16, 2)])
+def test_kmeans_lockstep_unit_heights(cuda, table, rows, layout):
     import torch
     from split_gb300 import kmeans
-    table.apply([tune.Entry(tune.INT64_MAX, 128, 2)])
+    table.apply([tune.Entry(tune.INT64_MAX, rows, 2)])
     w, h, k = 300, 333, 12
     rgb = synth.voronoi_rgb8(21, w, h, 40, sigma=4.0)
     feats = synth.features(rgb, 5)
@@ -56,12 +56,13 @@ def test_kmeans_lockstep_128_row_units(cuda, table, layout):
 
 
 def test_batch_equals_single_under_mixed_table(cuda, table):
-    """Small images take 128-row units, large ones 64-row units, and the
-    blocks per SM differ by class: every image still matches its own
-    single-image pipeline bit for bit."""
+    """The four images take 16-, 32-, 64- and 128-row units, and the blocks
+    per SM differ by class: every image still matches its own single-image
+    pipeline bit for bit."""
     import torch
     from split_gb300 import batch, pipeline
-    table.apply([tune.Entry(100_000, 128, 1), tune.Entry(tune.INT64_MAX, 64, 0)])
+    table.apply([tune.Entry(50_000, 16, 1), tune.Entry(100_000, 32, 2),
+                 tune.Entry(500_000, 64, 0), tune.Entry(tune.INT64_MAX, 128, 0)])
     shapes = [(333, 201, 8, 5), (640, 480, 16, 6), (97, 311, 32, 4), (1024, 700, 16, 7)]
     params = pipeline.Params(merge_P=64)
     imgs, cents = [], []

@@ -13,7 +13,8 @@ def restore_table():
 
 
 def test_table_round_trip(restore_table):
-    es = [tune.Entry(1000, 64, 2), tune.Entry(10**9, 128, 0), tune.Entry(tune.INT64_MAX, 64, 1)]
+    es = [tune.Entry(1000, 16, 2), tune.Entry(5000, 32, 1), tune.Entry(10**9, 128, 0),
+          tune.Entry(tune.INT64_MAX, 64, 1)]
     tune.apply(es)
     assert tune.current() == es
     tune.apply([])
@@ -21,7 +22,8 @@ def test_table_round_trip(restore_table):
 
 
 @pytest.mark.parametrize("bad", [
-    [tune.Entry(100, 96, 0)],                              # unit rows not 64 / 128
+    [tune.Entry(100, 96, 0)],                              # unit rows not 16/32/64/128
+    [tune.Entry(100, 8, 0)],
     [tune.Entry(100, 64, 9)],                              # blocks per SM out of range
     [tune.Entry(100, 64, -1)],
     [tune.Entry(0, 64, 0)],                                # empty class
