@@ -18,10 +18,11 @@
 // addition does not depend on order, so the image total is the same whatever
 // order units finish in and whatever else shares the launch.  A unit ends with
 // fire-and-forget adds and one block barrier: no fence, no arrival counter.
-// The grid barrier that ends the iteration publishes the sums; then every
-// block that works on the image in the next iteration forms c_new = c + S / n
-// in FP64, rounded to FP32, from the same inputs (bit-identical in every
-// block), and one owner block publishes it (form_centroids).  The sums are
+// The grid barrier that ends the iteration publishes the sums; then c_new =
+// c + S / n is formed in FP64, rounded to FP32 (form_centroids): for a single
+// image by every block from the same inputs (bit-identical), block 0
+// publishing it; in a batch by one owner block per image, published before a
+// second grid barrier.  The sums are
 // kept in three slots by iteration, so the owner can clear the slot of the
 // iteration after next while the current slot fills and the last one is read.
 #include <limits.h>
@@ -741,11 +742,12 @@ __device__ __forceinline__ void load_centroids(const float* src, int K,
 // (empty cluster: unchanged; cluster.cu:71-88), formed after the grid barrier
 // that ended iteration i - 1, and the convergence test of that iteration.
 //
-// Every block that works on the image in iteration i calls this with the same
-// inputs, which nobody writes during iteration i (c(i-1) in cur[(i-1) & 1],
+// Its inputs are not written during iteration i (c(i-1) in cur[(i-1) & 1],
 // the sums in slot (i-1) % 3, the state after iteration i-2 in state[(i-1) &
-// 1]), so all of them get bit-identical centroids and the same decision.  The
-// image's owner block (img = blockIdx.x mod gridDim.x) also publishes: c(i) to
+// 1]), so every block that calls it gets bit-identical centroids and the same
+// decision: for a single image every block calls it, block 0 as the owner; in
+// a batch only the owner (img = blockIdx.x mod gridDim.x) does.  The owner
+// publishes: c(i) to
 // cur[i & 1], the state after iteration i-1 to state[i & 1], zeros for slot
 // (i+1) % 3 (read for the last time in iteration i-1, written again in
 // iteration i+1), and on convergence the caller's centroids and iteration
@@ -854,17 +856,22 @@ __global__ void __launch_bounds__(kThreads, SG_KM_MINBLOCKS) kmeans_kernel(Param
     int cached = -1;
     bool more = false;      // the cached image runs this iteration
     if (MODE != kAssignOnly && it > 0) {
-      // owners publish their images' centroids first; a single image is
-      // formed by every block here, so all of them see it converge together
-      const int first = p.nimages == 1 ? 0 : (int)blockIdx.x;
-      const bool owner = p.nimages > 1 || blockIdx.x == 0;
-      for (int img = first; img < p.nimages; img += gridDim.x) {
-        more = form_centroids<DIM, MODE>(p, img, image_of(p, img), it, sm.cent, owner);
-        cached = img;
-      }
-      if (p.nimages == 1 && !more) {
-        stopped = true;
-        break;
+      if (p.nimages == 1) {
+        // every block forms the single image's centroids (block 0 publishes),
+        // so all of them see it converge together
+        more = form_centroids<DIM, MODE>(p, 0, image_of(p, 0), it, sm.cent, blockIdx.x == 0);
+        cached = 0;
+        if (!more) {
+          stopped = true;
+          break;
+        }
+      } else {
+        // A batch: owners form and publish their images, then a second grid
+        // barrier, so that a block switching images (often, with small
+        // images) only loads the published centroids.
+        for (int img = (int)blockIdx.x; img < p.nimages; img += gridDim.x)
+          form_centroids<DIM, MODE>(p, img, image_of(p, img), it, sm.cent, true);
+        if (!grid_barrier(p.hdr)) return;
       }
     }
     // The first wave is static (block b takes unit b): only later fetches go
@@ -880,15 +887,15 @@ __global__ void __launch_bounds__(kThreads, SG_KM_MINBLOCKS) kmeans_kernel(Param
         if (MODE == kAssignOnly) {
           load_centroids<DIM>(p.cur + (size_t)img * (kMaxK * 8), im.K, sm.cent);
           more = true;
-        } else if (it == 0) {
-          load_centroids<DIM>(p.cur + acc_slot(p, 0, img) * (kMaxK * 8), im.K, sm.cent);
-          if (threadIdx.x == 0) sm.more = !__ldcg(&p.state[img].done);
         } else {
-          more = form_centroids<DIM, MODE>(p, img, im, it, sm.cent, false);
+          // the published centroids and state of iteration it (a single
+          // image reaches this only in iteration 0)
+          load_centroids<DIM>(p.cur + acc_slot(p, it & 1, img) * (kMaxK * 8), im.K, sm.cent);
+          if (threadIdx.x == 0) sm.more = !__ldcg(&p.state[acc_slot(p, it & 1, img)].done);
         }
         cached = img;
         __syncthreads();
-        if (MODE != kAssignOnly && it == 0) more = sm.more != 0;
+        if (MODE != kAssignOnly) more = sm.more != 0;
       }
       if (more) {
         const int lu = u - im.unit_begin;
