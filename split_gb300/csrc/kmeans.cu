@@ -1416,10 +1416,12 @@ int kmeans_batch_run(const KmBatchPlan& plan, void* ws, cudaStream_t st) {
   p.hdr = l.hdr;
   p.blocks_per_sm = plan.blocks_per_sm;
   SG_TRY(reset_counters(l, plan.nimages, st));
-  init_kernel<<<1, 256, 0, st>>>(p);
+  init_kernel<<<(plan.nimages + 255) / 256, 256, 0, st>>>(p);
   SG_TRY(launch_status());
-  if (plan.dim == 3) load_user_centroids<3><<<1, 256, 0, st>>>(p);
-  else load_user_centroids<5><<<1, 256, 0, st>>>(p);
+  // one block per image (the kernel strides over images past 1024)
+  const int cb = plan.nimages < 1024 ? plan.nimages : 1024;
+  if (plan.dim == 3) load_user_centroids<3><<<cb, 64, 0, st>>>(p);
+  else load_user_centroids<5><<<cb, 64, 0, st>>>(p);
   SG_TRY(launch_status());
   if (plan.max_iter <= 0) return SPLIT_OK;
   return dispatch<kCluster>(plan.layout, plan.dim, p, st);

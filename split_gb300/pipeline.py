@@ -79,3 +79,94 @@ class Pipeline:
 
 def launch_count() -> int:
     return int(N.load().split_launch_count())
+
+
+class HostPipeline:
+    """Frames from pinned host memory through the pipeline, with the copies
+    overlapped with compute.
+
+    `depth` resident pipelines (slots) take frames in turn.  Uploads, compute
+    and downloads run on three CUDA streams joined by events:
+      * a slot's upload waits until the slot's previous frame has been
+        computed (input buffer free) and downloaded (the centroid buffer is
+        both the initial-centroid input and the result);
+      * its compute waits for the upload, and for the previous download (the
+        output buffers are rewritten);
+      * its download waits for the compute.
+    So frame f's compute overlaps frame f-1's download and frame f+1's
+    upload, and no result is overwritten before it has reached the host.
+    submit() returns at once; wait(ticket) blocks until that frame is in the
+    host buffers given to submit()."""
+
+    def __init__(self, width: int, height: int, params: Params, device=None, depth: int = 2):
+        if depth < 1:
+            raise ValueError("depth must be at least 1")
+        self.width, self.height, self.params = width, height, params
+        self.slots = [Pipeline(width, height, params, device) for _ in range(depth)]
+        self.device = self.slots[0].device
+        self.d_rgb = [torch.empty(height * width * 3, dtype=torch.uint8, device=self.device)
+                      for _ in range(depth)]
+        self.upload, self.compute, self.download = (torch.cuda.Stream(self.device)
+                                                    for _ in range(3))
+        self._uploaded = [torch.cuda.Event() for _ in range(depth)]
+        self._computed = [torch.cuda.Event() for _ in range(depth)]
+        self._downloaded = [torch.cuda.Event() for _ in range(depth)]
+        self._frame_of_slot = [-1] * depth
+        self.frames = 0
+
+    def submit(self, rgb: torch.Tensor, centroids: torch.Tensor,
+               segment_labels: torch.Tensor, normals: torch.Tensor | None = None,
+               centroids_out: torch.Tensor | None = None,
+               cluster_labels: torch.Tensor | None = None) -> int:
+        """Enqueue one frame.  rgb: pinned uint8 H*W*3; centroids: pinned
+        (dim, K) initial centroids; outputs: pinned host tensors of the
+        pipeline's shapes (segment labels (H, W) int32, normals (3, H*W)
+        float32, centroids (dim, K), cluster labels H*W int32)."""
+        for name, t in (("rgb", rgb), ("centroids", centroids), ("segment_labels", segment_labels),
+                        ("normals", normals), ("centroids_out", centroids_out),
+                        ("cluster_labels", cluster_labels)):
+            if t is not None and (t.is_cuda or not t.is_pinned()):
+                raise ValueError(f"{name}: expected a pinned host tensor")
+        if normals is not None and self.slots[0].normals is None:
+            raise ValueError("normals requested but the parameters compute none")
+        s = self.frames % len(self.slots)
+        pipe = self.slots[s]
+        busy = self._frame_of_slot[s] >= 0
+        with torch.cuda.stream(self.upload):
+            if busy:
+                self.upload.wait_event(self._computed[s])
+                self.upload.wait_event(self._downloaded[s])
+            self.d_rgb[s].copy_(rgb.reshape(-1), non_blocking=True)
+            pipe.centroids.copy_(centroids, non_blocking=True)
+            self._uploaded[s].record(self.upload)
+        with torch.cuda.stream(self.compute):
+            self.compute.wait_event(self._uploaded[s])
+            if busy:
+                self.compute.wait_event(self._downloaded[s])
+            pipe.run(self.d_rgb[s], stream=self.compute)
+            self._computed[s].record(self.compute)
+        with torch.cuda.stream(self.download):
+            self.download.wait_event(self._computed[s])
+            segment_labels.copy_(pipe.segment_labels, non_blocking=True)
+            if normals is not None:
+                normals.copy_(pipe.normals, non_blocking=True)
+            if centroids_out is not None:
+                centroids_out.copy_(pipe.centroids, non_blocking=True)
+            if cluster_labels is not None:
+                cluster_labels.copy_(pipe.cluster_labels, non_blocking=True)
+            self._downloaded[s].record(self.download)
+        self._frame_of_slot[s] = self.frames
+        self.frames += 1
+        return self.frames - 1
+
+    def wait(self, ticket: int) -> None:
+        """Block until frame `ticket` has reached its host buffers (a later
+        frame of the same slot implies it)."""
+        if ticket < 0 or ticket >= self.frames:
+            raise ValueError("unknown frame")
+        self._downloaded[ticket % len(self.slots)].synchronize()
+
+    def check(self) -> None:
+        """Raise if any slot's workspace recorded a device-side error."""
+        for p in self.slots:
+            p.ws.check("pipeline")

@@ -27,7 +27,13 @@ import statistics
 
 from . import _native as N
 
-UNIT_ROWS = (64, 128, 32, 16)
+# Candidates of the default autotune.  16- and 32-row units cut the latency of
+# a small image alone (512 x 512: 0.29 -> 0.18 ms at 16 rows) but slow batches
+# and serving of the same images (more units, each with a reduction and a
+# fetch), and an image uses one unit height alone and in a batch; pass
+# unit_rows=ALL_UNIT_ROWS to autotune() to tune for single small images.
+UNIT_ROWS = (64, 128)
+ALL_UNIT_ROWS = (64, 128, 32, 16)
 BLOCKS_PER_SM = (0, 2, 1)
 # representative sizes of the classes (width, height); a class ends halfway
 # (geometrically) between its size and the next one
@@ -127,12 +133,13 @@ def ensure_once(device=None) -> None:
 def pick(timings: dict) -> tuple:
     """The fastest candidate; ties go to the earlier candidate in the
     (unit rows, blocks per SM) order listed above."""
-    order = [(r, b) for r in UNIT_ROWS for b in BLOCKS_PER_SM]
+    order = [(r, b) for r in ALL_UNIT_ROWS for b in BLOCKS_PER_SM]
     best = min(order, key=lambda c: (timings.get(c, float("inf")), order.index(c)))
     return best
 
 
-def measure_class(width, height, device, reps=5, warmup=2, iters=20, seed=0x5EED7777):
+def measure_class(width, height, device, reps=5, warmup=2, iters=20, seed=0x5EED7777,
+                  unit_rows=UNIT_ROWS):
     """CUDA-event milliseconds of split_kmeans_cluster on one image of the
     class for every candidate."""
     import torch
@@ -152,7 +159,7 @@ def measure_class(width, height, device, reps=5, warmup=2, iters=20, seed=0x5EED
     saved = current()
     out = {}
     try:
-        for rows in UNIT_ROWS:
+        for rows in unit_rows:
             for bps in BLOCKS_PER_SM:
                 apply([Entry(INT64_MAX, rows, bps)])
                 times = []
@@ -175,7 +182,7 @@ def measure_class(width, height, device, reps=5, warmup=2, iters=20, seed=0x5EED
     return out
 
 
-def autotune(device=None, sizes=CLASS_SIZES, write_cache=True, reps=5):
+def autotune(device=None, sizes=CLASS_SIZES, write_cache=True, reps=5, unit_rows=UNIT_ROWS):
     """Measure every class, apply the winners and cache them.  Returns
     (entries, detail) where detail holds the timings."""
     import torch
@@ -184,7 +191,7 @@ def autotune(device=None, sizes=CLASS_SIZES, write_cache=True, reps=5):
     bounds = class_bounds(sizes)
     entries, detail = [], {}
     for (w, h), bound in zip(sizes, bounds):
-        t = measure_class(w, h, d, reps=reps)
+        t = measure_class(w, h, d, reps=reps, unit_rows=unit_rows)
         rows, bps = pick(t)
         entries.append(Entry(bound, rows, bps))
         detail[f"{w}x{h}"] = {f"rows{r}_bps{b}": round(v, 4) for (r, b), v in t.items()}
