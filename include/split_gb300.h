@@ -293,6 +293,15 @@ int split_sobel_normals_rgb8(const uint8_t* rgb, int width, int height,
 int split_pack_rgb8(const uint8_t* rgb, int64_t npixels, float* features4,
                     float* luminance, void* stream);
 
+/* The sample's intensity and chroma planes (samples/src/main.cu:169-179;
+ * replaces color::convert_color_space(rgb, ic, rgb_to_ic<>()),
+ * split/include/split/device/color/conversion.cuh:58 and
+ * detail/conversion.inl:99-108): RGB8 -> channels byte / 255 clamped to
+ * >= 1/255 -> ic planar 3 x n: intensity (r + g + b) / 3, then r / intensity
+ * and g / intensity (the chroma rows the reference's merge_small_segments
+ * reads).  FP32 in the reference's order of operations. */
+int split_rgb8_to_ic(const uint8_t* rgb, int64_t npixels, float* ic, void* stream);
+
 /* The sample's k-means features (samples/src/main.cu:169-173, :215-225;
  * replaces color::convert_color_space(rgb_to_lab) followed by
  * color::beta_feature, beta_feature.cuh:12-15): RGB8 -> channels clamped to
@@ -328,7 +337,10 @@ typedef struct split_pipeline_params {
   int connectivity;       /* 4 or 8                                          */
   int convention;         /* SPLIT_LABEL_MIN_INDEX / SPLIT_LABEL_MAX_INDEX   */
   int merge_P;            /* merge segments smaller than P; 0 = no merge     */
-  int merge_policy;       /* SPLIT_MERGE_MOST_BOUNDARY                       */
+  int merge_policy;       /* SPLIT_MERGE_MOST_BOUNDARY, or SPLIT_MERGE_REF_CHROMA
+                             on the sample's r / intensity plane
+                             (split_rgb8_to_ic, computed in the pipeline;
+                             single images only, not batches)              */
   int erode_radius;       /* 0 = no erosion                                  */
   int compute_normals;    /* nonzero: normals of L* / 100                    */
   float depth;

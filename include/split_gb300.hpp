@@ -339,5 +339,32 @@ inline int estimate_normals(const_view2d<float> shading_intensity, float3 light_
 
 }  // namespace sfs
 
+// ---- color -----------------------------------------------------------------
+namespace color {
+
+/* The sample's feature preparation from RGB8 bytes (the reference converts
+ * float images with convert_color_space, conversion.cuh:21-58; main.cu:
+ * 169-225).  Inputs are interleaved RGB8, n = the columns of the output. */
+
+/* rgb_to_ic: ic (3 x n) = intensity, r / intensity, g / intensity of the
+ * channels clamped to >= 1/255 (conversion.inl:99-108). */
+inline void rgb8_to_ic(const unsigned char* rgb, view2d<float> ic, cudaStream_t stream = nullptr) {
+  check(split_rgb8_to_ic(rgb, (int64_t)ic.num_cols(), ic.data(), stream), "color::rgb8_to_ic");
+}
+
+/* rgb_to_lab + beta_feature: features (3 x n) = beta, a*, b*; luminance
+ * (optional, n) = L* (beta_feature.cuh:12-15). */
+inline void rgb8_to_lab_beta(const unsigned char* rgb, view2d<float> features, Temp& temp,
+                             float mu = 1e5f, float* luminance = nullptr,
+                             cudaStream_t stream = nullptr) {
+  const int64_t n = (int64_t)features.num_cols();
+  temp.reserve(split_pack_lab_beta_workspace_size(n));
+  check(split_pack_lab_beta(rgb, n, mu, SPLIT_LAYOUT_PLANAR, features.data(), luminance,
+                            temp.get(), temp.size(), stream),
+        "color::rgb8_to_lab_beta");
+}
+
+}  // namespace color
+
 }  // namespace device
 }  // namespace split

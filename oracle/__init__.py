@@ -164,6 +164,22 @@ def merge_smooth(labels: np.ndarray, points: np.ndarray, threshold: float = 0.01
     return a
 
 
+def rgb_to_ic_f32(rgb: np.ndarray) -> np.ndarray:
+    """The sample's intensity / chroma planes in FP32, operation for operation
+    (samples/src/main.cu:169-179; conversion.inl:99-108): RGB8 (..., 3) ->
+    channels byte / 255 clamped to >= 1/255 -> intensity = (r + g + b) *
+    (1/3), ri = 1 / intensity, (intensity, r * ri, g * ri).  Returns (3, N)
+    float32; every step is one IEEE single operation, so the result is exact."""
+    f32 = np.float32
+    v = np.asarray(rgb, np.uint8).reshape(-1, 3).astype(f32) / f32(255.0)
+    v = np.maximum(v, f32(1.0) / f32(255.0))
+    r, g, b = v[:, 0], v[:, 1], v[:, 2]
+    third = f32(1.0) / f32(3.0)
+    inten = ((r + g) + b) * third
+    ri = f32(1.0) / inten
+    return np.stack([inten, r * ri, g * ri]).astype(f32)
+
+
 def lab_beta_f64(rgb: np.ndarray, mu: float = 1e5):
     """The sample's features in FP64 (samples/src/main.cu:169-173, :215-225):
     RGB8 (..., 3) -> channels / 255 clamped to >= 1/255 -> sRGB linearised

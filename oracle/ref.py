@@ -126,6 +126,18 @@ def rgb_to_lab(rgb_planar):
     return out
 
 
+def rgb_to_ic(rgb_planar):
+    """The sample's (intensity, r / i, g / i) planes: (3, N) RGB in [0, 1] ->
+    (3, N) (main.cu:169-179; conversion.inl:99-108)."""
+    a = np.ascontiguousarray(rgb_planar, np.float32)
+    out = np.empty_like(a)
+    lib = load()
+    lib.ref_rgb_to_ic.argtypes = [C.c_void_p, C.c_int, C.c_void_p]
+    lib.ref_rgb_to_ic.restype = C.c_int
+    lib.ref_rgb_to_ic(_p(a), a.shape[1], _p(out))
+    return out
+
+
 def lab_beta(rgb_planar, mu=1e5):
     """The sample's features: (3, N) RGB in [0, 1] -> ((3, N) beta, a*, b*;
     (N,) L*)  (main.cu:169-173, :215-225; beta_feature.cu:47-78)."""

@@ -153,6 +153,18 @@ int ref_rgb_to_lab(const float* rgb, int n, float* lab) {
   return 0;
 }
 
+// The sample's intensity / chroma planes (samples/src/main.cu:169-179): RGB
+// in [0, 1] clamped to >= 1/255, then color::rgb_to_ic.
+int ref_rgb_to_ic(const float* rgb, int n, float* ic) {
+  Mat A(3, n), B(3, n);
+  to_dev(A, rgb, 3 * (std::size_t)n);
+  thrust::transform(A.values.begin(), A.values.end(), A.values.begin(),
+                    split::device::detail::unary_max<real>(1.f / 255.f));
+  split::device::color::convert_color_space(A, B, split::device::color::rgb_to_ic<>());
+  to_host(B, ic, 3 * (std::size_t)n);
+  return 0;
+}
+
 // The sample's feature preparation (samples/src/main.cu:169-173, :215-225):
 // RGB in [0, 1] clamped to >= 1/255, converted to L*a*b*, L* saved, then the
 // beta feature written in place of L*.  features: planar 3 x n (beta, a, b);

@@ -51,6 +51,7 @@ _SIGS = {
     "split_sobel_normals": (_i32, [_vp, _i32, _i32, _f32, _vp, _vp]),
     "split_sobel_normals_rgb8": (_i32, [_vp, _i32, _i32, _f32, _vp, _vp]),
     "split_pack_rgb8": (_i32, [_vp, _i64, _vp, _vp, _vp]),
+    "split_rgb8_to_ic": (_i32, [_vp, _i64, _vp, _vp]),
     "split_pipeline_workspace_size": (_sz, [_i32, _i32, _vp]),
     "split_pipeline_run": (_i32, [_vp, _i32, _i32, _vp, _vp, _vp, _vp, _vp, _vp, _sz, _vp, _vp]),
     "split_launch_count": (C.c_ulonglong, []),

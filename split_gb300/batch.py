@@ -35,12 +35,25 @@ class Arena:
             self.segment_labels = torch.zeros(pixels, dtype=torch.int32, device=d)
             self.normals = torch.zeros(pixels * 3, dtype=torch.float32, device=d) \
                 if self.normals_enabled else None
+            self.labels_host = None   # pinned download buffers, made on first use
         if centroid_floats > self.cf:
             self.cf = centroid_floats
             self.centroids = torch.zeros(centroid_floats, dtype=torch.float32, device=d)
+            self.centroids_host = None
         if workspace_bytes > self.wsb:
             self.wsb = workspace_bytes
             self.ws_buf = torch.zeros(workspace_bytes + 256, dtype=torch.uint8, device=d)
+
+
+    def host_buffers(self):
+        """Pinned host buffers for downloads of a whole arena (segment labels,
+        centroids), made once per capacity: pinning memory takes milliseconds
+        and must stay out of a serving loop."""
+        if getattr(self, "labels_host", None) is None:
+            self.labels_host = torch.empty(self.px, dtype=torch.int32, pin_memory=True)
+        if getattr(self, "centroids_host", None) is None:
+            self.centroids_host = torch.empty(self.cf, dtype=torch.float32, pin_memory=True)
+        return self.labels_host, self.centroids_host
 
 
 class Batch:

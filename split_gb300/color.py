@@ -17,6 +17,21 @@ def pack_rgb8(rgb: torch.Tensor, features4: torch.Tensor | None = None,
     N.check(st, "color.pack_rgb8")
 
 
+def rgb_to_ic(rgb: torch.Tensor, ic: torch.Tensor, stream=None) -> None:
+    """The sample's intensity / chroma planes (samples/src/main.cu:169-179,
+    color::convert_color_space with rgb_to_ic, conversion.inl:99-108): RGB8
+    (N x 3 bytes) -> ic (3, N) float32: intensity, r / intensity,
+    g / intensity of the channels clamped to >= 1/255.  Rows 1-2 are the
+    chroma input of ccl.merge_small_segments' reference rule."""
+    require_cuda(rgb, "rgb", torch.uint8)
+    require_cuda(ic, "ic", torch.float32)
+    n = rgb.numel() // 3
+    if ic.shape != (3, n) or not ic.is_contiguous():
+        raise ValueError("ic must be a contiguous (3, N) float32 tensor")
+    N.check(N.load().split_rgb8_to_ic(ptr(rgb), n, ptr(ic), stream_handle(stream)),
+            "color.rgb_to_ic")
+
+
 def pack_lab_beta(rgb: torch.Tensor, features: torch.Tensor, luminance: torch.Tensor | None = None,
                   mu: float = 1e5, temp: Workspace | None = None, stream=None) -> Workspace:
     """The sample's k-means features (samples/src/main.cu:169-173, :215-225):

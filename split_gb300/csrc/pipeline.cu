@@ -26,6 +26,7 @@ struct Layout {
   size_t ccl_bytes;
   void* mrg_ws;
   size_t mrg_bytes;
+  float* ic;   // intensity / chroma planes for the reference chroma merge rule
   size_t bytes;
 };
 
@@ -44,6 +45,9 @@ static Layout carve(void* ws, int W, int H, const split_pipeline_params& p) {
   l.ccl_ws = c.take<char>(l.ccl_bytes);
   l.mrg_bytes = p.merge_P > 0 ? split_merge_small_workspace_size(W, H) : 0;
   l.mrg_ws = p.merge_P > 0 ? c.take<char>(l.mrg_bytes) : nullptr;
+  l.ic = p.merge_P > 0 && p.merge_policy == SPLIT_MERGE_REF_CHROMA
+             ? c.take<float>((size_t)3 * n)
+             : nullptr;
   l.bytes = c.size();
   return l;
 }
@@ -55,7 +59,10 @@ static bool valid(const split_pipeline_params* p) {
           p->features == kFeaturesLabBeta) &&
          (p->connectivity == 4 || p->connectivity == 8) &&
          (p->convention == SPLIT_LABEL_MIN_INDEX || p->convention == SPLIT_LABEL_MAX_INDEX) &&
-         p->merge_P >= 0 && p->merge_policy == SPLIT_MERGE_MOST_BOUNDARY && p->erode_radius >= 0 &&
+         p->merge_P >= 0 &&
+         (p->merge_policy == SPLIT_MERGE_MOST_BOUNDARY ||
+          p->merge_policy == SPLIT_MERGE_REF_CHROMA) &&
+         p->erode_radius >= 0 &&
          p->erode_radius <= 16;
 }
 
@@ -119,8 +126,12 @@ extern "C" int split_pipeline_run(const uint8_t* rgb, int width, int height,
   SG_TRY(mark(5));
   // 3: merge decision (the relabel is fused into the erosion below)
   SG_TRY(mark(6));
+  // the reference rule compares mean chroma: the sample's r / intensity
+  // plane (row 1 of rgb_to_ic, main.cu:176-193)
+  const float* chroma = l.ic ? l.ic + n : nullptr;
+  if (l.ic) SG_TRY(split_rgb8_to_ic(rgb, n, l.ic, stream));
   if (p.merge_P > 0)
-    SG_TRY(merge_decide_only(l.seg, width, height, p.merge_P, p.merge_policy, nullptr, l.sizes,
+    SG_TRY(merge_decide_only(l.seg, width, height, p.merge_P, p.merge_policy, chroma, l.sizes,
                              l.mrg_ws, l.mrg_bytes, st));
   SG_TRY(mark(7));
   // 4: relabel + erosion
@@ -135,7 +146,7 @@ extern "C" int split_pipeline_run(const uint8_t* rgb, int width, int height,
     SG_CUDA_TRY(cudaMemcpyAsync(segment_labels, l.seg, sizeof(int32_t) * (size_t)n,
                                 cudaMemcpyDeviceToDevice, st));
     if (p.merge_P > 0)
-      SG_TRY(split_merge_small(segment_labels, width, height, p.merge_P, p.merge_policy, nullptr,
+      SG_TRY(split_merge_small(segment_labels, width, height, p.merge_P, p.merge_policy, chroma,
                                l.sizes, l.mrg_ws, l.mrg_bytes, stream));
   }
   SG_TRY(mark(9));

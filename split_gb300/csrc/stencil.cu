@@ -309,6 +309,28 @@ __global__ void pack_kernel(const uint8_t* __restrict__ rgb, int64_t n, float4* 
   }
 }
 
+// ---- intensity / chroma -----------------------------------------------------------
+// The sample's (intensity, r / intensity, g / intensity) planes: channels
+// byte / 255 clamped to >= 1/255 (main.cu:169-173), intensity = (r + g + b)
+// * (1/3), one reciprocal, two products (conversion.inl:99-108), FP32 in the
+// reference's order.  Planar 3 x n output.
+__global__ void ic_kernel(const uint8_t* __restrict__ rgb, int64_t n, float* __restrict__ out) {
+  __shared__ float v8[256];
+  for (int i = threadIdx.x; i < 256; i += blockDim.x)
+    v8[i] = fmaxf(__fdiv_rn((float)i, 255.0f), __fdiv_rn(1.0f, 255.0f));
+  __syncthreads();
+  const float third = __fdiv_rn(1.0f, 3.0f);
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const float r = v8[rgb[3 * i]], g = v8[rgb[3 * i + 1]], b = v8[rgb[3 * i + 2]];
+    const float in = __fmul_rn(__fadd_rn(__fadd_rn(r, g), b), third);
+    const float ri = __fdiv_rn(1.0f, in);
+    out[i] = in;
+    out[n + i] = __fmul_rn(r, ri);
+    out[2 * n + i] = __fmul_rn(g, ri);
+  }
+}
+
 // ---- L*a*b* and the beta feature ------------------------------------------------
 // L*a*b* of an sRGB byte triple after the sample's clamp (conversion.inl:8-25
 // rgb_to_xyz, :46-64 xyz_to_lab; operations in the reference's order, FP32).
@@ -492,6 +514,16 @@ extern "C" int split_sobel_normals_rgb8(const uint8_t* rgb, int width, int heigh
   if (!rgb || !normals || width < 1 || height < 1) return SPLIT_ERR_INVALID;
   if ((int64_t)width * height * 3 > 0x7fffffffLL) return SPLIT_ERR_INVALID;
   return normals_rgb8_geoms(rgb, single_geom(width, height), depth, normals, as_stream(stream));
+}
+
+extern "C" int split_rgb8_to_ic(const uint8_t* rgb, int64_t npixels, float* ic, void* stream) {
+  if (!rgb || !ic || npixels <= 0) return SPLIT_ERR_INVALID;
+  DeviceInfo di;
+  SG_TRY(device_info(&di));
+  int64_t blocks = (npixels + 255) / 256;
+  if (blocks > (int64_t)di.sm_count * 8) blocks = (int64_t)di.sm_count * 8;
+  stn::ic_kernel<<<(int)blocks, 256, 0, as_stream(stream)>>>(rgb, npixels, ic);
+  return launch_status();
 }
 
 extern "C" int split_pack_rgb8(const uint8_t* rgb, int64_t npixels, float* features4,

@@ -166,6 +166,8 @@ class Server:
         del probe
         for a in self.arenas:
             a.ensure(pixels + 64 * max_requests, self.params.dim * 64 * max_requests, wsb)
+            if not self.keep_results:
+                a.host_buffers()
 
     def now(self) -> float:
         return time.perf_counter() - self.t0
@@ -194,8 +196,17 @@ class Server:
         ran.record(self.compute)
         self.d2h.wait_event(ran)
         with torch.cuda.stream(self.d2h):
-            labels_h = torch.empty(b.segment_labels.shape, dtype=torch.int32, pin_memory=True)
-            cents_h = torch.empty(b.centroids.shape, dtype=torch.float32, pin_memory=True)
+            if self.keep_results:
+                # results outlive the batch: buffers of their own
+                labels_h = torch.empty(b.segment_labels.shape, dtype=torch.int32,
+                                       pin_memory=True)
+                cents_h = torch.empty(b.centroids.shape, dtype=torch.float32, pin_memory=True)
+            else:
+                # the slot's buffers, pinned once (the slot is reused only
+                # after this batch has been collected)
+                lh, ch = self.arenas[self.batches % self.depth].host_buffers()
+                labels_h = lh[:b.segment_labels.numel()].view(b.segment_labels.shape)
+                cents_h = ch[:b.centroids.numel()].view(b.centroids.shape)
             labels_h.copy_(b.segment_labels, non_blocking=True)
             cents_h.copy_(b.centroids, non_blocking=True)
             done = torch.cuda.Event()

@@ -6,7 +6,9 @@ and stores their outputs.  Inputs are not stored: they are regenerated from
 the seeds by split_gb300.synth, and a SHA-256 of each generated input is kept
 so a generator change is caught.
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py            # reference_golden.npz
+    python tests/golden/make_golden.py lab_beta   # lab_beta_golden.npz
+    python tests/golden/make_golden.py ic         # ic_golden.npz
 
 Known limit of the CPU build: CCCL 3.0.1's host sort orders negative int keys
 after non-negative ones, so compress_labels is only recorded on non-negative
@@ -26,6 +28,7 @@ sys.path.insert(0, ROOT)
 
 OUT = os.path.join(HERE, "reference_golden.npz")
 OUT_LAB = os.path.join(HERE, "lab_beta_golden.npz")
+OUT_IC = os.path.join(HERE, "ic_golden.npz")
 
 
 def sha(a: np.ndarray) -> str:
@@ -76,6 +79,17 @@ def main_lab_beta():
     print(f"wrote {OUT_LAB}")
 
 
+def main_ic():
+    """Intensity / chroma planes of the Lab + beta input image, from the
+    compiled reference (ref_rgb_to_ic)."""
+    from oracle import ref
+    from split_gb300 import synth
+    rgb = lab_beta_inputs()
+    ic = ref.rgb_to_ic(synth.features(rgb, 3))
+    np.savez_compressed(OUT_IC, rgb_sha=sha(rgb), ic=ic)
+    print(f"wrote {OUT_IC}")
+
+
 def main():
     from oracle import ref
     d = inputs()
@@ -113,5 +127,7 @@ def main():
 
 if __name__ == "__main__" and sys.argv[1:] == ["lab_beta"]:
     main_lab_beta()
+elif __name__ == "__main__" and sys.argv[1:] == ["ic"]:
+    main_ic()
 elif __name__ == "__main__":
     main()

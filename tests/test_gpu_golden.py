@@ -132,3 +132,27 @@ def test_lab_beta_features(cuda, planar):
     assert np.array_equal(f[0], g["features"][0])
     if not planar:
         assert (feats[:, 3] == 0).all()
+
+
+def test_rgb_to_ic(cuda):
+    """Intensity / chroma planes on the GPU equal the reference's own FP32
+    code bit for bit (golden fixture), and the restatement on a larger
+    random image including black and white pixels."""
+    import torch
+    import make_golden
+    from split_gb300 import color
+    g = np.load(os.path.join(HERE, "golden", "ic_golden.npz"))
+    rgb = make_golden.lab_beta_inputs()
+    n = rgb.shape[0] * rgb.shape[1]
+    ic = torch.empty((3, n), dtype=torch.float32, device=cuda)
+    color.rgb_to_ic(torch.from_numpy(rgb).to(cuda), ic)
+    assert np.array_equal(ic.cpu().numpy().view(np.uint32), g["ic"].view(np.uint32))
+    rng = np.random.default_rng(77)
+    big = rng.integers(0, 256, size=(1001, 777, 3), dtype=np.uint8)
+    big[0, :5] = 0
+    big[1, :5] = 255
+    m = big.shape[0] * big.shape[1]
+    ic2 = torch.empty((3, m), dtype=torch.float32, device=cuda)
+    color.rgb_to_ic(torch.from_numpy(big).to(cuda), ic2)
+    ref = oracle.rgb_to_ic_f32(big)
+    assert np.array_equal(ic2.cpu().numpy().view(np.uint32), ref.view(np.uint32))

@@ -489,3 +489,30 @@ def test_estimate_normals_limits(cuda):
         sfs.estimate_normals(s, (1.0, 1.0, 1.0), out, 0.0)       # no smoothness: singular
     with pytest.raises(_native.SplitError):
         sfs.estimate_normals(s, (0.0, 0.0, 0.0), out, 0.5)       # no light direction
+
+
+def test_pipeline_reference_chroma_merge(cuda):
+    """The pipeline with the reference's chroma merge rule: the merge reads
+    the sample's r / intensity plane (rgb_to_ic), and the segment labels
+    equal the oracle's CCL -> chroma merge -> erosion of the pipeline's own
+    k-means labels."""
+    import torch
+    from split_gb300 import _native, pipeline
+    w, h = 301, 187
+    # colour-only features on a noisy image: hundreds of small fragments
+    rgb = synth.voronoi_rgb8(91, w, h, 60, sigma=8.0)
+    p = pipeline.Params(nclusters=12, dim=3, kmeans_iters=6, merge_P=48,
+                        merge_policy=_native.MERGE_REF_CHROMA)
+    c0 = synth.pick_centroids(91, rgb, p.nclusters, p.dim)
+    pipe = pipeline.Pipeline(w, h, p, cuda)
+    pipe.run(torch.from_numpy(rgb).to(cuda), torch.from_numpy(c0).to(cuda))
+    torch.cuda.synchronize()
+    pipe.ws.check("pipeline")
+    cl = pipe.cluster_labels.cpu().numpy().reshape(h, w)
+    seg = oracle.ccl(cl, 8, 0)
+    chroma = oracle.rgb_to_ic_f32(rgb)[1:]
+    merged = oracle.merge_small(seg, 48, 1, chroma)
+    assert len(np.unique(merged)) < len(np.unique(seg))     # something merged
+    # and the rule is the chroma one, not the boundary one
+    assert not np.array_equal(merged, oracle.merge_small(seg, 48, 0))
+    assert np.array_equal(pipe.segment_labels.cpu().numpy(), oracle.erode(merged, 1))

@@ -117,3 +117,19 @@ def test_lab_beta_restatement_against_reference():
     np.testing.assert_allclose(feats[1:], g["features"][1:], atol=2e-3)
     assert np.array_equal(feats[0], g["features"][0])
     assert set(np.unique(feats[0])) == {-1e5, 0.0, 1e5}
+
+
+def test_ic_restatement_against_reference():
+    """The FP32 restatement of the sample's intensity / chroma planes equals
+    the reference's own code (clamp, rgb_to_ic) bit for bit."""
+    import make_golden
+    g = np.load(os.path.join(HERE, "golden", "ic_golden.npz"))
+    rgb = make_golden.lab_beta_inputs()
+    assert make_golden.sha(rgb) == str(g["rgb_sha"])
+    ic = oracle.rgb_to_ic_f32(rgb)
+    assert ic.dtype == np.float32 and ic.shape == g["ic"].shape
+    assert np.array_equal(ic.view(np.uint32), g["ic"].view(np.uint32))
+    # black pixels take the clamp: intensity 1/255 and chroma 1, up to the
+    # FP32 rounding of (3 / 255) * (1 / 3) and its reciprocal
+    black = oracle.rgb_to_ic_f32(np.zeros((1, 3), np.uint8))
+    np.testing.assert_allclose(black[:, 0], [1 / 255, 1.0, 1.0], rtol=1e-6)
