@@ -70,10 +70,43 @@ __device__ __forceinline__ bool stage(T* dst, const CUtensorMap* map, const T* s
     }
     return true;
   }
-  for (int i = threadIdx.x; i < sw * sh; i += blockDim.x) {
-    const int r = i / sw, c = i % sw;
-    const int gx = x0 + c, gy = y0 + r;
-    dst[i] = (gx >= 0 && gy >= 0 && gx < W && gy < H) ? src[(size_t)gy * W + gx] : T(0);
+  if (sizeof(T) == 1 && sw % 4 == 0) {
+    // bytes: a warp per staged row, 4 bytes per lane and load.  A group wholly
+    // inside the image row is read as one 32-bit word (two words and a funnel
+    // shift when the row is not 4-byte aligned; both words hold bytes of the
+    // row, so they lie in mapped memory); edge groups go byte by byte.
+    const int lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    for (int r = threadIdx.x >> 5; r < sh; r += nw) {
+      const int gy = y0 + r;
+      uint32_t* drow = reinterpret_cast<uint32_t*>(dst + r * sw);
+      if (gy < 0 || gy >= H) {
+        for (int c = lane; c < sw / 4; c += 32) drow[c] = 0u;
+        continue;
+      }
+      const unsigned char* srow = reinterpret_cast<const unsigned char*>(src) + (size_t)gy * W;
+      for (int c = lane; c < sw / 4; c += 32) {
+        const int gx = x0 + 4 * c;
+        uint32_t v;
+        if (gx >= 0 && gx + 3 < W) {
+          const uintptr_t a = reinterpret_cast<uintptr_t>(srow + gx);
+          const uint32_t* w = reinterpret_cast<const uint32_t*>(a & ~(uintptr_t)3);
+          const unsigned sh8 = 8u * (unsigned)(a & 3);
+          v = sh8 ? __funnelshift_r(__ldg(w), __ldg(w + 1), sh8) : __ldg(w);
+        } else {
+          v = 0u;
+#pragma unroll
+          for (int q = 0; q < 4; ++q)
+            if (gx + q >= 0 && gx + q < W) v |= (uint32_t)srow[gx + q] << (8 * q);
+        }
+        drow[c] = v;
+      }
+    }
+  } else {
+    for (int i = threadIdx.x; i < sw * sh; i += blockDim.x) {
+      const int r = i / sw, c = i % sw;
+      const int gx = x0 + c, gy = y0 + r;
+      dst[i] = (gx >= 0 && gy >= 0 && gx < W && gy < H) ? src[(size_t)gy * W + gx] : T(0);
+    }
   }
   __syncthreads();
   return true;

@@ -141,13 +141,16 @@ def test_sobel_normals(cuda, shape):
     assert np.arccos(cosang).max() <= 1e-4
 
 
-def test_sobel_normals_rgb8(cuda):
+# widths: 256 (TMA staging); 257, 333, 98, 1 (row pitch not a multiple of 16
+# bytes: plain staging, with rows at every 4-byte misalignment)
+@pytest.mark.parametrize("w,h", [(256, 96), (257, 95), (333, 71), (98, 40), (1, 9)])
+def test_sobel_normals_rgb8(cuda, w, h):
     import torch
     from split_gb300 import sfs
-    rgb = synth.voronoi_rgb8(9, 256, 96, 16, sigma=3.0)
-    out = torch.empty((3, 256 * 96), dtype=torch.float32, device=cuda)
+    rgb = synth.voronoi_rgb8(9 + w, w, h, 16, sigma=3.0)
+    out = torch.empty((3, w * h), dtype=torch.float32, device=cuda)
     sfs.sobel_normals_rgb8(_t(rgb, cuda), out, 1.0)
-    lum = oracle.luminance_f64(rgb).reshape(96, 256)
+    lum = oracle.luminance_f64(rgb).reshape(h, w)
     # FP64 normals of the FP64 luminance; the device computes L* in FP32
     ref = oracle.sobel_normals_f64(lum.astype(np.float32), 1.0)
     got = out.cpu().numpy().astype(np.float64)
