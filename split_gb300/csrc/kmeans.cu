@@ -457,6 +457,23 @@ __device__ __forceinline__ void accumulate_valid(Smem& sm, int warp, const float
   }
 }
 
+// ---- asynchronous copies into shared memory (no registers hold the data)
+__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() {
+  asm volatile("cp.async.commit_group;" ::: "memory");
+}
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+// Staging of the float4 fast path: per warp two batches of kPx x 32 float4,
+// pixel j of lane l at [j][l] (conflict-free copies and reads).
+constexpr int kStageFloat4 = kWarps * 2 * 4 * 32;   // float4 elements per block
+constexpr size_t kStageBytes = (size_t)kStageFloat4 * 16;
+
 // A warp span that lies wholly inside the image, with packed features (float4,
 // or RGB8 read as three 32-bit words per 4 pixels) and a candidate mask known
 // for the whole span: no per-pixel bounds checks, one pointer step per batch,
@@ -471,13 +488,52 @@ __device__ __forceinline__ void fast_span(const Image& im, Smem& sm, int warp, i
   float fx[kPx];
 #pragma unroll
   for (int j = 0; j < kPx; ++j) fx[j] = __fmul_rn(im.xy_scale, (float)(col + j));
+  // float4: the next batch is copied into shared memory while this one runs.
+  // Lane l copies batch pixels l + 32 j (each copy a contiguous 512 bytes of
+  // one row) and reads its own pixels 4 l + j; slots are swizzled so that
+  // both are free of bank conflicts.
+  extern __shared__ float4 km_stage[];
+  const int ln = threadIdx.x & 31;
+  float4* stage = km_stage + warp * (2 * kPx * 32);
+  const int64_t gw = (int64_t)im.width;
+  // batch pixel q = 64 r + c of the batch's first row (row_first - lrow)
+  const float4* gb0 = static_cast<const float4*>(im.points) + (px0 - (int64_t)(ln / kLanesPerRow) * gw
+                                                               - (ln % kLanesPerRow) * kPx);
+  // slot(q) = (q & ~7) | ((q + (q >> 3)) & 7), in closed form for the lane's
+  // copies (q = ln + 32 j) and reads (q = 4 ln + j)
+  const int cs0 = (ln & ~7) + ((ln + (ln >> 3)) & 7), cs1 = cs0 ^ 4;
+  const int rs0 = 8 * (ln >> 1), rt = (4 * ln + (ln >> 1)) & 7;
+  const float4* grow1 = gb0 + gw;
+  if (LAYOUT == SPLIT_LAYOUT_FLOAT4) {
+    cp_async16(stage + cs0, gb0 + ln);
+    cp_async16(stage + 32 + cs1, gb0 + ln + 32);
+    cp_async16(stage + 64 + cs0, grow1 + ln);
+    cp_async16(stage + 96 + cs1, grow1 + ln + 32);
+    cp_async_commit();
+  }
   for (int b = 0; b < nbatches; ++b, px0 += step) {
     float f[kPx][DIM];
     if (LAYOUT == SPLIT_LAYOUT_FLOAT4) {
-      const float4* p = static_cast<const float4*>(im.points) + px0;
+      // every lane has read the buffer about to be refilled (batch b - 1)
+      __syncwarp();
+      if (b + 1 < nbatches) {
+        const float4* g = gb0 + (int64_t)(b + 1) * step + ln;
+        float4* dst = stage + ((b + 1) & 1) * (kPx * 32);
+        cp_async16(dst + cs0, g);
+        cp_async16(dst + 32 + cs1, g + 32);
+        cp_async16(dst + 64 + cs0, g + gw);
+        cp_async16(dst + 96 + cs1, g + gw + 32);
+        cp_async_commit();
+        cp_async_wait<1>();
+      } else {
+        cp_async_wait<0>();
+      }
+      // the copies of the other lanes must have landed too
+      __syncwarp();
+      const float4* src = stage + (b & 1) * (kPx * 32);
 #pragma unroll
       for (int j = 0; j < kPx; ++j) {
-        const float4 v = __ldg(p + j);
+        const float4 v = src[rs0 + ((rt + j) & 7)];
         f[j][0] = v.x;
         f[j][1] = v.y;
         f[j][2] = v.z;
@@ -1018,24 +1074,52 @@ split_tune_entry tuned(int64_t npix) {
   return split_tune_entry{INT64_MAX, kTile, 0};
 }
 
+// The float4 kernels stage features in kStageBytes of dynamic shared memory,
+// above the default 48 KB limit with their static part: the attribute is set
+// once per device, before any launch (and outside any graph capture: batch
+// preparation calls this too).
+static int stage_attributes() {
+  static std::mutex mu;
+  static bool done[64] = {false};
+  int dev = 0;
+  SG_CUDA_TRY(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) return SPLIT_ERR_CUDA;
+  std::lock_guard<std::mutex> lock(mu);
+  if (done[dev]) return SPLIT_OK;
+  const void* kerns[] = {
+      (const void*)kmeans_kernel<SPLIT_LAYOUT_FLOAT4, 3, kCluster>,
+      (const void*)kmeans_kernel<SPLIT_LAYOUT_FLOAT4, 5, kCluster>,
+      (const void*)kmeans_kernel<SPLIT_LAYOUT_FLOAT4, 3, kUpdateOnly>,
+      (const void*)kmeans_kernel<SPLIT_LAYOUT_FLOAT4, 5, kUpdateOnly>,
+      (const void*)kmeans_kernel<SPLIT_LAYOUT_FLOAT4, 3, kAssignOnly>,
+      (const void*)kmeans_kernel<SPLIT_LAYOUT_FLOAT4, 5, kAssignOnly>};
+  for (const void* k : kerns)
+    SG_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)kStageBytes));
+  done[dev] = true;
+  return SPLIT_OK;
+}
+
 template <int LAYOUT, int DIM, int MODE>
 static int launch(Params& p, cudaStream_t st) {
   DeviceInfo di;
   SG_TRY(device_info(&di));
   auto kern = kmeans_kernel<LAYOUT, DIM, MODE>;
+  const size_t dyn = LAYOUT == SPLIT_LAYOUT_FLOAT4 ? kStageBytes : 0;
+  if (dyn) SG_TRY(stage_attributes());
   int per_sm = 0;
-  SG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kThreads, 0));
+  SG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kThreads, dyn));
   if (per_sm < 1) return SPLIT_ERR_UNSUPPORTED;
   if (p.blocks_per_sm > 0 && p.blocks_per_sm < per_sm) per_sm = p.blocks_per_sm;
   int grid = di.sm_count * per_sm;
   if (grid > p.total_units) grid = p.total_units > 0 ? p.total_units : 1;
   if (MODE == kAssignOnly) {
-    kern<<<grid, kThreads, 0, st>>>(p);
+    kern<<<grid, kThreads, dyn, st>>>(p);
     return launch_status();
   }
   void* args[] = {&p};
   SG_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)kern, dim3(grid), dim3(kThreads),
-                                          args, 0, st));
+                                          args, dyn, st));
   return launch_status();
 }
 
@@ -1349,6 +1433,8 @@ int kmeans_batch_prepare(const KmBatchImage* imgs, int nimages, int layout, int 
                          KmBatchPlan* plan) {
   using namespace km;
   if (!imgs || nimages < 1 || (dim != 3 && dim != 5)) return SPLIT_ERR_INVALID;
+  // kernel attributes now: the batch's launches may be captured into a graph
+  SG_TRY(stage_attributes());
   const int unit_range = (layout & SPLIT_FEATURES_UNIT_RANGE) ? 1 : 0;
   layout &= ~SPLIT_FEATURES_UNIT_RANGE;
   const BatchCounts c = batch_counts(imgs, nimages, true);
