@@ -251,6 +251,27 @@ __device__ __forceinline__ float lum_from_lin(float r, float g, float b) {
 __device__ __forceinline__ void sobel_tile(const float* h, int hp, int tx0, int ty0, int W, int H,
                                            float zinv, float* out) {
   const size_t n = (size_t)W * H;
+  if (tx0 >= 1 && ty0 >= 1 && tx0 + TW < W && ty0 + TH < H) {
+    // the tile and its one-pixel ring lie inside the image: no clamping and
+    // no bounds checks; the same sums in the same order as below
+    const float zz = __fmul_rn(zinv, zinv), za = fabsf(zinv);
+    for (int i = threadIdx.x; i < TH * TW; i += blockDim.x) {
+      const int r = i / TW, c = i % TW;
+      const float* p = h + (r + 1) * hp + (c + 1);
+      const float sb = __fadd_rn(__fadd_rn(p[hp - 1], __fmul_rn(2.0f, p[hp])), p[hp + 1]);
+      const float st = __fadd_rn(__fadd_rn(p[-hp - 1], __fmul_rn(2.0f, p[-hp])), p[-hp + 1]);
+      const float tr = __fadd_rn(__fadd_rn(p[-hp + 1], __fmul_rn(2.0f, p[1])), p[hp + 1]);
+      const float tl = __fadd_rn(__fadd_rn(p[-hp - 1], __fmul_rn(2.0f, p[-1])), p[hp - 1]);
+      const float gy = __fsub_rn(sb, st);
+      const float gx = __fsub_rn(tr, tl);
+      const float rm = rsqrtf(__fmaf_rn(gx, gx, __fmaf_rn(gy, gy, zz)));
+      const size_t g = (size_t)(ty0 + r) * W + tx0 + c;
+      out[g] = __fmul_rn(gx, rm);
+      out[n + g] = __fmul_rn(gy, rm);
+      out[2 * n + g] = __fmul_rn(za, rm);
+    }
+    return;
+  }
   for (int i = threadIdx.x; i < TH * TW; i += blockDim.x) {
     const int r = i / TW, c = i % TW;
     const int x = tx0 + c, y = ty0 + r;
@@ -268,7 +289,7 @@ __device__ __forceinline__ void sobel_tile(const float* h, int hp, int tx0, int 
     const float gy = __fsub_rn(sb, st);
     const float gx = __fsub_rn(tr, tl);
     const float m2 = __fmaf_rn(gx, gx, __fmaf_rn(gy, gy, __fmul_rn(zinv, zinv)));
-    const float rm = 1.0f / sqrtf(m2);
+    const float rm = rsqrtf(m2);
     const size_t g = (size_t)y * W + x;
     out[g] = __fmul_rn(gx, rm);
     out[n + g] = __fmul_rn(gy, rm);
