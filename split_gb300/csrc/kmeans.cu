@@ -751,7 +751,6 @@ __device__ void process_unit(const Image& im, int unit, Smem& sm, bool write_lab
   if (MODE != kAssignOnly && acc_l >= 0) flush_acc<DIM>(sm, warp, acc_l, acc, acc_n);
 }
 
-// Sum the warp slots in warp order into a unit record; clear the slots.
 // Sums the block's 8 warp slots in warp order (the unit partial), clears
 // them, and adds the partial into the image accumulators (96-bit fixed point:
 // low 32 bits and the signed rest in two 64-bit words).
