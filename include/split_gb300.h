@@ -333,7 +333,7 @@ typedef struct split_pipeline_params {
                              SPLIT_LAYOUT_RGB8: read the bytes directly;
                              SPLIT_PIPELINE_FEATURES_LAB_BETA: the sample's
                              (beta, a*, b*) features (split_pack_lab_beta;
-                             single images only, not batches)              */
+                             in a batch with per-image maxima)             */
   int connectivity;       /* 4 or 8                                          */
   int convention;         /* SPLIT_LABEL_MIN_INDEX / SPLIT_LABEL_MAX_INDEX   */
   int merge_P;            /* merge segments smaller than P; 0 = no merge     */
@@ -346,6 +346,10 @@ typedef struct split_pipeline_params {
   float depth;
   float beta_mu;          /* mu of the beta feature (the reference: 1e5)     */
 } split_pipeline_params;
+
+/* Errors recorded on the device by any stage of split_pipeline_run or
+ * split_batch_run are reported through the status word of the call's own
+ * workspace (split_workspace_status), each once. */
 
 /* split_pipeline_params.features value for the sample's Lab + beta features. */
 #define SPLIT_PIPELINE_FEATURES_LAB_BETA 3

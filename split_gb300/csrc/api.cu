@@ -58,6 +58,35 @@ extern "C" const char* split_status_string(int status) {
   }
 }
 
+namespace sg {
+// first error in source order wins, as with set_status
+__global__ void fold_status_kernel(int* dst, StatusSources s) {
+  if (threadIdx.x != 0) return;
+  for (int i = 0; i < s.n; ++i) {
+    volatile int* q = s.p[i];
+    const int v = *q;
+    if (v) {
+      set_status(dst, v);
+      *q = 0;
+    }
+  }
+}
+
+int fold_status(int* dst, const StatusSources& s, cudaStream_t st) {
+  fold_status_kernel<<<1, 32, 0, st>>>(dst, s);
+  return launch_status();
+}
+
+__global__ void clear_status_kernel(StatusSources s) {
+  if ((int)threadIdx.x < s.n) *s.p[threadIdx.x] = 0;
+}
+
+int clear_status(const StatusSources& s, cudaStream_t st) {
+  clear_status_kernel<<<1, 32, 0, st>>>(s);
+  return launch_status();
+}
+}  // namespace sg
+
 extern "C" int split_workspace_status(void* workspace, void* stream, int* out_status) {
   if (!workspace || !out_status) return SPLIT_ERR_INVALID;
   cudaStream_t st = as_stream(stream);

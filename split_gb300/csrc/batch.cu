@@ -25,6 +25,14 @@ int normals_rgb8_geoms(const uint8_t* rgb, const Geoms& gs, float depth, float* 
                        cudaStream_t st);
 int batch_image_maps(const int32_t* labels, const uint8_t* rgb, int W, int H, int radius,
                      CUtensorMap* lab_map, CUtensorMap* rgb_map);
+int lab_beta_geoms(const uint8_t* rgb, const Geoms& gs, float mu, float* features4,
+                   unsigned* maxima, cudaStream_t st);
+// split_pipeline_params.features value of the sample's Lab + beta features
+constexpr int kFeaturesLabBeta = SPLIT_PIPELINE_FEATURES_LAB_BETA;
+// the batch packs float4 features (RGB / 255, or Lab + beta) before k-means
+inline bool packs_float4(const split_pipeline_params& p) {
+  return p.features == SPLIT_LAYOUT_FLOAT4 || p.features == kFeaturesLabBeta;
+}
 }  // namespace sg
 
 using namespace sg;
@@ -55,6 +63,7 @@ namespace {
 struct Layout {
   WsHeader* hdr;
   float* features4;
+  unsigned* maxima;   // Lab + beta: L*max and |a*|max keys per image
   int32_t* seg;
   int32_t* sizes;
   void* km_ws;
@@ -72,7 +81,8 @@ Layout carve(void* ws, const split_batch& b) {
   const size_t n = (size_t)b.arena_px;
   const size_t ni = b.images.size();
   l.hdr = c.take<WsHeader>(1);
-  l.features4 = b.params.features == SPLIT_LAYOUT_FLOAT4 ? c.take<float>(n * 4) : nullptr;
+  l.features4 = packs_float4(b.params) ? c.take<float>(n * 4) : nullptr;
+  l.maxima = b.params.features == kFeaturesLabBeta ? c.take<unsigned>(2 * ni) : nullptr;
   l.seg = c.take<int32_t>(n);
   l.sizes = c.take<int32_t>(n);
   l.km_ws = c.take<char>(b.km_bytes);
@@ -90,7 +100,7 @@ std::vector<KmBatchImage> km_images(const split_batch& b, const Layout& l) {
   for (size_t i = 0; i < b.images.size(); ++i) {
     const split_batch_image& im = b.images[i];
     KmBatchImage& k = v[i];
-    k.points = b.params.features == SPLIT_LAYOUT_FLOAT4
+    k.points = packs_float4(b.params)
                    ? static_cast<const void*>(l.features4 ? l.features4 + 4 * b.pix_off[i] : nullptr)
                    : static_cast<const void*>(b.rgb ? b.rgb + 3 * b.pix_off[i] : nullptr);
     k.npoints = (int64_t)im.width * im.height;
@@ -130,7 +140,8 @@ extern "C" int split_batch_create(const split_batch_image* images, int nimages,
   if (!images || nimages < 1 || !params || !out) return SPLIT_ERR_INVALID;
   const split_pipeline_params& p = *params;
   if ((p.dim != 3 && p.dim != 5) || (p.connectivity != 4 && p.connectivity != 8) ||
-      (p.features != SPLIT_LAYOUT_FLOAT4 && p.features != SPLIT_LAYOUT_RGB8) ||
+      (p.features != SPLIT_LAYOUT_FLOAT4 && p.features != SPLIT_LAYOUT_RGB8 &&
+       p.features != kFeaturesLabBeta) ||
       p.erode_radius < 1 || p.erode_radius > 16 || p.merge_P < 0 ||
       p.merge_policy != SPLIT_MERGE_MOST_BOUNDARY)
     return SPLIT_ERR_INVALID;
@@ -204,9 +215,11 @@ extern "C" int split_batch_bind(split_batch* b, const uint8_t* rgb, float* centr
   b->normals = normals;
   b->ws = workspace;
   std::vector<KmBatchImage> kmi = km_images(*b, l);
+  // byte / 255 features lie in the unit cube; Lab + beta ones do not
   const int layout = b->params.features == SPLIT_LAYOUT_FLOAT4
                          ? (SPLIT_LAYOUT_FLOAT4 | SPLIT_FEATURES_UNIT_RANGE)
-                         : SPLIT_LAYOUT_RGB8;
+                         : b->params.features == kFeaturesLabBeta ? SPLIT_LAYOUT_FLOAT4
+                                                                  : SPLIT_LAYOUT_RGB8;
   SG_TRY(kmeans_batch_prepare(kmi.data(), (int)kmi.size(), layout, b->params.dim,
                               b->params.xy_scale, l.km_ws, b->km_bytes, st, &b->km));
   const size_t ni = b->images.size();
@@ -239,8 +252,18 @@ extern "C" int split_batch_run(split_batch* b, void* stream) {
   const split_pipeline_params& p = b->params;
   Layout l = carve(b->ws, *b);
   cudaStream_t st = as_stream(stream);
+  // the stages' own status words (sub-workspace headers): cleared first (a
+  // rebound arena may hold anything there), folded into the batch's at the end
+  StatusSources ss{};
+  ss.p[ss.n++] = &static_cast<WsHeader*>(l.km_ws)->status;
+  ss.p[ss.n++] = &static_cast<WsHeader*>(l.ccl_ws)->status;
+  if (l.mrg_ws) ss.p[ss.n++] = &static_cast<WsHeader*>(l.mrg_ws)->status;
+  SG_TRY(clear_status(ss, st));
   if (p.features == SPLIT_LAYOUT_FLOAT4)
     SG_TRY(split_pack_rgb8(b->rgb, b->arena_px, l.features4, nullptr, stream));
+  else if (p.features == kFeaturesLabBeta)
+    SG_TRY(lab_beta_geoms(b->rgb, device_geoms(*b, l, nullptr), p.beta_mu, l.features4, l.maxima,
+                          st));
   SG_TRY(kmeans_batch_run(b->km, l.km_ws, st));
   const Geoms gs = device_geoms(*b, l, nullptr);
   SG_TRY(ccl_geoms(b->cluster_labels, gs, p.connectivity, SPLIT_LABEL_MIN_INDEX, l.seg,
@@ -258,5 +281,7 @@ extern "C" int split_batch_run(split_batch* b, void* stream) {
                      mstate, mfin, 1, st));
   if (p.compute_normals)
     SG_TRY(normals_rgb8_geoms(b->rgb, device_geoms(*b, l, l.rgb_maps), p.depth, b->normals, st));
-  return SPLIT_OK;
+  // errors the stages recorded in their own workspace headers, into the
+  // batch's status word
+  return fold_status(&l.hdr->status, ss, st);
 }

@@ -90,6 +90,21 @@ __device__ __forceinline__ void set_status(int* st, int code) {
   atomicCAS(st, 0, code);
 }
 
+// Status words of the sub-workspaces a composite call (pipeline, batch)
+// carves from its own: fold_status moves the first error among them into the
+// composite workspace's own status word (read by split_workspace_status) and
+// clears them, so that a sub-stage error is never lost and never reported
+// twice.
+struct StatusSources {
+  int* p[8];
+  int n;
+};
+__global__ void fold_status_kernel(int* dst, StatusSources s);
+int fold_status(int* dst, const StatusSources& s, cudaStream_t st);
+// Clears the sources' status words before the stages run: a reused
+// workspace may hold anything where this call's sub-workspace headers lie.
+int clear_status(const StatusSources& s, cudaStream_t st);
+
 // Iteration limit of every spin wait (about a second with the back-off below).
 constexpr unsigned kSpinLimit = 1u << 24;
 

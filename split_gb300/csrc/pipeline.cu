@@ -94,6 +94,12 @@ extern "C" int split_pipeline_run(const uint8_t* rgb, int width, int height,
   l = pipe::carve(workspace, width, height, p);
   cudaStream_t st = as_stream(stream);
   const int64_t n = (int64_t)width * height;
+  // the stages' own status words (sub-workspace headers), cleared first and
+  // folded into the pipeline's status word at the end
+  StatusSources ss{};
+  ss.p[ss.n++] = &static_cast<WsHeader*>(l.km_ws)->status;
+  ss.p[ss.n++] = &static_cast<WsHeader*>(l.ccl_ws)->status;
+  if (l.mrg_ws) ss.p[ss.n++] = &static_cast<WsHeader*>(l.mrg_ws)->status;
   auto mark = [&](int i) -> int {
     if (stage_events)
       SG_CUDA_TRY(cudaEventRecord(reinterpret_cast<cudaEvent_t>(stage_events[i]), st));
@@ -101,6 +107,7 @@ extern "C" int split_pipeline_run(const uint8_t* rgb, int width, int height,
   };
   // 0: features
   SG_TRY(mark(0));
+  SG_TRY(clear_status(ss, st));
   if (p.features == SPLIT_LAYOUT_FLOAT4)
     SG_TRY(split_pack_rgb8(rgb, n, l.features4, nullptr, stream));
   else if (p.features == pipe::kFeaturesLabBeta)
@@ -153,6 +160,9 @@ extern "C" int split_pipeline_run(const uint8_t* rgb, int width, int height,
   // 5: normals of the luminance plane, straight from the bytes
   SG_TRY(mark(10));
   if (p.compute_normals) SG_TRY(split_sobel_normals_rgb8(rgb, width, height, p.depth, normals, stream));
+  // errors the stages recorded in their own workspace headers, into the
+  // pipeline's status word
+  SG_TRY(fold_status(&l.hdr->status, ss, st));
   SG_TRY(mark(11));
   return SPLIT_OK;
 }

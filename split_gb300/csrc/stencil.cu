@@ -471,7 +471,70 @@ __global__ void lab_beta_kernel(const uint8_t* __restrict__ rgb, int64_t n, cons
   }
 }
 
+// Batches: the same two passes over the tile grid of many images, with
+// per-image maxima (2 words per image: L*max and |a*|max keys).  A block is
+// one 32 x 64 tile of one image, so no pixel searches for its image.
+__global__ void __launch_bounds__(kThreads)
+lab_max_geoms_kernel(const uint8_t* __restrict__ rgb, Geoms gs, unsigned* maxima) {
+  __shared__ float lin[256];
+  for (int i = threadIdx.x; i < 256; i += blockDim.x) lin[i] = lin100(i);
+  __syncthreads();
+  const TileRef t = tile_ref(gs, blockIdx.x);
+  unsigned kl = 0, ka = 0;
+  for (int i = threadIdx.x; i < TH * TW; i += blockDim.x) {
+    const int x = t.tx0 + (i % TW), y = t.ty0 + i / TW;
+    if (x >= t.W || y >= t.H) continue;
+    const uint8_t* p = rgb + 3 * (t.off + (long long)y * t.W + x);
+    const Lab c = lab_from_lin(lin[p[0]], lin[p[1]], lin[p[2]]);
+    kl = max(kl, okey(c.L));
+    ka = max(ka, okey(fabsf(c.a)));
+  }
+  kl = __reduce_max_sync(0xffffffffu, kl);
+  ka = __reduce_max_sync(0xffffffffu, ka);
+  if ((threadIdx.x & 31) == 0 && kl) {
+    atomicMax(maxima + 2 * t.img, kl);
+    atomicMax(maxima + 2 * t.img + 1, ka);
+  }
+}
+
+__global__ void __launch_bounds__(kThreads)
+lab_beta_geoms_kernel(const uint8_t* __restrict__ rgb, Geoms gs, const unsigned* maxima, float mu,
+                      float4* __restrict__ out) {
+  __shared__ float lin[256];
+  for (int i = threadIdx.x; i < 256; i += blockDim.x) lin[i] = lin100(i);
+  __syncthreads();
+  const TileRef t = tile_ref(gs, blockIdx.x);
+  const float lmax = okey_inv(maxima[2 * t.img]);
+  const float lambda = __fmul_rn(0.2f, okey_inv(maxima[2 * t.img + 1]));
+  const float lo = __fmul_rn(lmax, 0.20f), hi = __fmul_rn(lmax, 0.95f);
+  for (int i = threadIdx.x; i < TH * TW; i += blockDim.x) {
+    const int x = t.tx0 + (i % TW), y = t.ty0 + i / TW;
+    if (x >= t.W || y >= t.H) continue;
+    const long long g = t.off + (long long)y * t.W + x;
+    const uint8_t* p = rgb + 3 * g;
+    const Lab c = lab_from_lin(lin[p[0]], lin[p[1]], lin[p[2]]);
+    float beta = 0.0f;
+    if (fabsf(c.a) < lambda && fabsf(c.b) < lambda) {
+      if (c.L < lo) beta = -mu;
+      else if (c.L > hi) beta = mu;
+    }
+    out[g] = make_float4(beta, c.a, c.b, 0.0f);
+  }
+}
+
 }  // namespace stn
+
+// The sample's Lab + beta features of every image of a batch into its float4
+// arena (maxima: 2 words per image, cleared here).
+int lab_beta_geoms(const uint8_t* rgb, const Geoms& gs, float mu, float* features4,
+                   unsigned* maxima, cudaStream_t st) {
+  SG_CUDA_TRY(cudaMemsetAsync(maxima, 0, sizeof(unsigned) * 2 * (size_t)gs.n, st));
+  stn::lab_max_geoms_kernel<<<gs.total_tiles, stn::kThreads, 0, st>>>(rgb, gs, maxima);
+  SG_TRY(launch_status());
+  stn::lab_beta_geoms_kernel<<<gs.total_tiles, stn::kThreads, 0, st>>>(
+      rgb, gs, maxima, mu, reinterpret_cast<float4*>(features4));
+  return launch_status();
+}
 }  // namespace sg
 
 using namespace sg;

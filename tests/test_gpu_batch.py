@@ -31,6 +31,7 @@ def _single(torch, rgb, c0, k, iters, params, dev):
     pipe = pipeline.Pipeline(w, h, p, dev)
     pipe.run(torch.from_numpy(rgb).to(dev), torch.from_numpy(c0).to(dev))
     torch.cuda.synchronize()
+    pipe.ws.check("pipeline")
     return (pipe.cluster_labels.cpu().numpy(), pipe.centroids.cpu().numpy(),
             pipe.segment_labels.cpu().numpy(), pipe.normals.cpu().numpy())
 
@@ -100,3 +101,68 @@ def test_arena_reuse_across_compositions(cuda):
             assert torch.equal(a.segment_labels_of(i), f.segment_labels_of(i))
             assert torch.equal(a.centroids_of(i), f.centroids_of(i))
             assert torch.equal(a.normals_of(i), f.normals_of(i))
+
+
+# K = 32 on the 97 x 311 image fragments it into ~8500 segments of ~3.5 px
+# (more (segment, neighbour) pairs than the merge table holds; see below)
+LAB_SHAPES = [s if s != (97, 311, 32, 4) else (97, 311, 8, 4) for s in SHAPES]
+
+
+def _lab_inputs(torch, cuda, shapes, params, seed=300):
+    from split_gb300 import color
+    imgs = [synth.voronoi_rgb8(seed + i, w, h, max(4, (w * h) // 4000), npalette=8,
+                               illum_gradient=True, sigma=4.0) for i, (w, h, _, _) in enumerate(shapes)]
+    cents = []
+    for (w, h, k, _), rgb in zip(shapes, imgs):
+        # initial centroids: the Lab + beta features of k evenly spaced pixels
+        n = w * h
+        f4 = torch.empty((n, 4), dtype=torch.float32, device=cuda)
+        color.pack_lab_beta(torch.from_numpy(rgb).to(cuda), f4, mu=params.beta_mu)
+        idx = np.linspace(0, n - 1, k).astype(np.int64)
+        c = f4[:, :3].cpu().numpy()[idx].T
+        if params.dim == 5:
+            xy = np.stack([idx % w, idx // w]).astype(np.float32) * np.float32(params.xy_scale)
+            c = np.concatenate([c, xy])
+        cents.append(np.ascontiguousarray(c, np.float32))
+    return imgs, cents
+
+
+@pytest.mark.parametrize("dim", [3, 5])
+def test_batch_lab_beta_equals_single(cuda, dim):
+    """The sample's Lab + beta features in a batch (per-image maxima over the
+    tile grid): every image's cluster labels, centroids, segments and normals
+    equal its single-image pipeline run bit for bit."""
+    import torch
+    from split_gb300 import _native, batch, pipeline
+    params = pipeline.Params(features=_native.FEATURES_LAB_BETA, dim=dim, merge_P=64)
+    imgs, cents = _lab_inputs(torch, cuda, LAB_SHAPES, params)
+    b = batch.Batch(LAB_SHAPES, params, cuda)
+    b.load(imgs, cents)
+    b.run()
+    torch.cuda.synchronize()
+    b.ws.check("batch")
+    for i, (w, h, k, iters) in enumerate(LAB_SHAPES):
+        cl, ce, sl, nr = _single(torch, imgs[i], cents[i], k, iters, params, cuda)
+        assert np.array_equal(b.cluster_labels_of(i).cpu().numpy(), cl), f"image {i} labels"
+        assert np.array_equal(b.centroids_of(i).cpu().numpy(), ce), f"image {i} centroids"
+        assert np.array_equal(b.segment_labels_of(i).cpu().numpy(), sl), f"image {i} segments"
+        assert np.array_equal(b.normals_of(i).cpu().numpy(), nr), f"image {i} normals"
+
+
+def test_merge_table_overflow_is_reported(cuda):
+    """A 97 x 311 image cut into ~8500 segments of ~3.5 px has more (segment,
+    neighbour) pairs than the single-image merge table (2^ceil(log2 N)
+    slots): the pipeline reports SPLIT_ERR_OVERFLOW through its own status
+    word (the stage's error is folded into it) instead of returning a wrong
+    merge silently."""
+    import torch
+    from split_gb300 import _native, pipeline
+    params = pipeline.Params(features=_native.FEATURES_LAB_BETA, dim=3, merge_P=64)
+    shape = [(97, 311, 32, 4)]
+    imgs, cents = _lab_inputs(torch, cuda, shape, params, seed=303)
+    p = pipeline.Params(**{**params.__dict__, "nclusters": 32, "kmeans_iters": 4})
+    pipe = pipeline.Pipeline(97, 311, p, cuda)
+    pipe.run(torch.from_numpy(imgs[0]).to(cuda), torch.from_numpy(cents[0]).to(cuda))
+    torch.cuda.synchronize()
+    assert pipe.ws.status() == _native.ERR_OVERFLOW
+    assert pipe.ws.status() == _native.OK      # reported once, then cleared
