@@ -279,10 +279,10 @@ __global__ void guard_kernel(const WsHeader* h, unsigned long long stamp, Layout
     L.best[i] = 0ull;
 }
 
-__global__ void stamp_kernel(WsHeader* h, unsigned long long stamp) { h->stamp = stamp; }
-
-__global__ void set_state_kernel(State* st, const int32_t* sizes, int P, int policy, int cap_log2,
-                                 int n) {
+// the layout stamp (after the guard's clear) and the run's parameters
+__global__ void set_state_kernel(WsHeader* h, unsigned long long stamp, State* st,
+                                 const int32_t* sizes, int P, int policy, int cap_log2, int n) {
+  h->stamp = stamp;
   st->n = n;
   st->sizes = sizes;
   st->P = P;
@@ -342,11 +342,12 @@ static int merge_run(int32_t* labels, const Geoms& gs, int P, int policy, const 
   const int32_t* sizes = d_sizes ? d_sizes : l.size;
   const bool ref = policy == SPLIT_MERGE_REF_CHROMA;
   const unsigned long long stamp = ((unsigned long long)l.cap_log2 << 40) | (unsigned long long)n;
-  mrg::guard_kernel<<<grid, mrg::kThreads, 0, st>>>(l.hdr, stamp, l, n);
+  // the guard usually finds the stamp unchanged and exits: one block per SM
+  // is enough for the rare full clear
+  mrg::guard_kernel<<<di.sm_count, mrg::kThreads, 0, st>>>(l.hdr, stamp, l, n);
   SG_TRY(launch_status());
-  mrg::stamp_kernel<<<1, 1, 0, st>>>(l.hdr, stamp);
-  SG_TRY(launch_status());
-  mrg::set_state_kernel<<<1, 1, 0, st>>>(l.state, sizes, P, policy, l.cap_log2, (int)n);
+  mrg::set_state_kernel<<<1, 1, 0, st>>>(l.hdr, stamp, l.state, sizes, P, policy, l.cap_log2,
+                                         (int)n);
   SG_TRY(launch_status());
   if (!d_sizes) SG_CUDA_TRY(cudaMemsetAsync(l.size, 0, sizeof(int32_t) * (size_t)n, st));
   if (ref) SG_CUDA_TRY(cudaMemsetAsync(l.sum, 0, sizeof(double) * (size_t)n, st));
