@@ -242,6 +242,14 @@ extern "C" int split_batch_bind(split_batch* b, const uint8_t* rgb, float* centr
                               cudaMemcpyHostToDevice, st));
   SG_CUDA_TRY(cudaMemcpyAsync(l.rgb_maps, rgb_maps.data(), sizeof(CUtensorMap) * ni,
                               cudaMemcpyHostToDevice, st));
+  // a rebound arena may hold anything where this layout's stage headers lie
+  {
+    StatusSources ss{};
+    ss.p[ss.n++] = &static_cast<WsHeader*>(l.km_ws)->status;
+    ss.p[ss.n++] = &static_cast<WsHeader*>(l.ccl_ws)->status;
+    if (l.mrg_ws) ss.p[ss.n++] = &static_cast<WsHeader*>(l.mrg_ws)->status;
+    SG_TRY(clear_status(ss, st));
+  }
   SG_CUDA_TRY(cudaStreamSynchronize(st));
   b->bound = true;
   return SPLIT_OK;
@@ -252,13 +260,12 @@ extern "C" int split_batch_run(split_batch* b, void* stream) {
   const split_pipeline_params& p = b->params;
   Layout l = carve(b->ws, *b);
   cudaStream_t st = as_stream(stream);
-  // the stages' own status words (sub-workspace headers): cleared first (a
-  // rebound arena may hold anything there), folded into the batch's at the end
+  // the stages' own status words (sub-workspace headers, cleared at bind),
+  // folded into the batch's at the end
   StatusSources ss{};
   ss.p[ss.n++] = &static_cast<WsHeader*>(l.km_ws)->status;
   ss.p[ss.n++] = &static_cast<WsHeader*>(l.ccl_ws)->status;
   if (l.mrg_ws) ss.p[ss.n++] = &static_cast<WsHeader*>(l.mrg_ws)->status;
-  SG_TRY(clear_status(ss, st));
   if (p.features == SPLIT_LAYOUT_FLOAT4)
     SG_TRY(split_pack_rgb8(b->rgb, b->arena_px, l.features4, nullptr, stream));
   else if (p.features == kFeaturesLabBeta)

@@ -104,6 +104,11 @@ int fold_status(int* dst, const StatusSources& s, cudaStream_t st);
 // Clears the sources' status words before the stages run: a reused
 // workspace may hold anything where this call's sub-workspace headers lie.
 int clear_status(const StatusSources& s, cudaStream_t st);
+// Whether `workspace` was last used with layout `key` (a small direct-mapped
+// memo; records the key).  After the first run of a layout the fold leaves
+// the stage status words at zero, so the clear is needed only on a change
+// (a miss only costs a clear).
+bool layout_unchanged(const void* workspace, unsigned long long key);
 
 // Iteration limit of every spin wait (about a second with the back-off below).
 constexpr unsigned kSpinLimit = 1u << 24;

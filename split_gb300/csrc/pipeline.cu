@@ -107,7 +107,11 @@ extern "C" int split_pipeline_run(const uint8_t* rgb, int width, int height,
   };
   // 0: features
   SG_TRY(mark(0));
-  SG_TRY(clear_status(ss, st));
+  const unsigned long long layout_key =
+      ((unsigned long long)(unsigned)width << 32 | (unsigned)height) ^
+      ((unsigned long long)l.bytes << 7) ^ ((unsigned long long)p.features << 3) ^
+      (unsigned long long)(p.merge_P > 0) ^ ((unsigned long long)p.merge_policy << 1);
+  if (!layout_unchanged(workspace, layout_key)) SG_TRY(clear_status(ss, st));
   if (p.features == SPLIT_LAYOUT_FLOAT4)
     SG_TRY(split_pack_rgb8(rgb, n, l.features4, nullptr, stream));
   else if (p.features == pipe::kFeaturesLabBeta)
