@@ -440,6 +440,23 @@ def run_serving(dev, nimages, nrequests, seed=SEED + 2000):
     return out
 
 
+# ---- replicas (N > 1 under torchrun): each rank runs its own image; the step
+# time is the slowest rank's and the rate counts every rank's pixels
+def max_over_ranks(x: float, dist, device) -> float:
+    """The largest `x` over the ranks of the process group (x itself alone)."""
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_rate_mpix_s(world: int, px_per_rank: int, ms: float) -> float:
+    """Whole-job Mpix/s: every rank's pixels over the slowest rank's time."""
+    return world * px_per_rank / (ms * 1e-3) / 1e6
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -537,12 +554,8 @@ def main():
         for i, name in enumerate(_native.PIPELINE_STAGES):
             stage_ms[name] += ev[s][2 * i].elapsed_time(ev[s][2 * i + 1]) / args.steps
         total_ms += ev[s][0].elapsed_time(ev[s][-1]) / args.steps
-    step_ms = total_ms
-    if dist is not None:
-        t = torch.tensor([step_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        step_ms = float(t.item())
-    value = world * npx / (step_ms * 1e-3) / 1e6
+    step_ms = max_over_ranks(total_ms, dist, dev)
+    value = job_rate_mpix_s(world, npx, step_ms)
 
     # ---- end-to-end through the public call with host buffers
     h_rgb = torch.from_numpy(rgb_np).pin_memory()
@@ -565,12 +578,8 @@ def main():
     e1.synchronize()
     hp.check()
     barrier()
-    e2e_ms = e0.elapsed_time(e1) / e2e_steps
-    if dist is not None:
-        t = torch.tensor([e2e_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_ms = float(t.item())
-    e2e_value = world * npx / (e2e_ms * 1e-3) / 1e6
+    e2e_ms = max_over_ranks(e0.elapsed_time(e1) / e2e_steps, dist, dev)
+    e2e_value = job_rate_mpix_s(world, npx, e2e_ms)
 
     # ---- roofline of the dominant kernel (k-means, one cooperative launch)
     iters = params.kmeans_iters
