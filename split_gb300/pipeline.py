@@ -76,6 +76,29 @@ class Pipeline:
             self.ws.nbytes, ev, stream_handle(stream))
         N.check(st, "pipeline.run")
 
+    def capture(self, rgb: torch.Tensor):
+        """Capture one run on `rgb` into a CUDA graph; replay() then reruns it
+        on whatever that buffer and self.centroids hold (copy the next frame
+        and its initial centroids in first).  The graph replaces the launch
+        sequence's host work and launch gaps."""
+        require_cuda(rgb, "rgb", torch.uint8)
+        torch.cuda.synchronize(self.device)
+        s = torch.cuda.Stream(self.device)
+        c0 = self.centroids.clone()
+        with torch.cuda.stream(s):
+            self.run(rgb, stream=s)        # warm the launch path outside capture
+        s.synchronize()
+        self.centroids.copy_(c0)
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g, stream=s):
+            self.run(rgb, stream=torch.cuda.current_stream())
+        self.graph = g
+        self._graph_rgb = rgb
+        return g
+
+    def replay(self) -> None:
+        self.graph.replay()
+
 
 def launch_count() -> int:
     return int(N.load().split_launch_count())
@@ -95,10 +118,13 @@ class HostPipeline:
       * its download waits for the compute.
     So frame f's compute overlaps frame f-1's download and frame f+1's
     upload, and no result is overwritten before it has reached the host.
-    submit() returns at once; wait(ticket) blocks until that frame is in the
-    host buffers given to submit()."""
+    With `graphs` (default), each slot's launch sequence is captured once into
+    a CUDA graph and every frame replays it.  submit() returns at once;
+    wait(ticket) blocks until that frame is in the host buffers given to
+    submit()."""
 
-    def __init__(self, width: int, height: int, params: Params, device=None, depth: int = 2):
+    def __init__(self, width: int, height: int, params: Params, device=None, depth: int = 2,
+                 graphs: bool = True):
         if depth < 1:
             raise ValueError("depth must be at least 1")
         self.width, self.height, self.params = width, height, params
@@ -113,6 +139,12 @@ class HostPipeline:
         self._downloaded = [torch.cuda.Event() for _ in range(depth)]
         self._frame_of_slot = [-1] * depth
         self.frames = 0
+        self.graphs = graphs
+        if graphs:
+            for pipe, buf in zip(self.slots, self.d_rgb):
+                buf.zero_()
+                pipe.centroids.zero_()
+                pipe.capture(buf)
 
     def submit(self, rgb: torch.Tensor, centroids: torch.Tensor,
                segment_labels: torch.Tensor, normals: torch.Tensor | None = None,
@@ -143,7 +175,10 @@ class HostPipeline:
             self.compute.wait_event(self._uploaded[s])
             if busy:
                 self.compute.wait_event(self._downloaded[s])
-            pipe.run(self.d_rgb[s], stream=self.compute)
+            if self.graphs:
+                pipe.replay()
+            else:
+                pipe.run(self.d_rgb[s], stream=self.compute)
             self._computed[s].record(self.compute)
         with torch.cuda.stream(self.download):
             self.download.wait_event(self._computed[s])
