@@ -344,6 +344,125 @@ def run_batched(dev, nimages, steps, seed=SEED + 1000):
 
 
 # ------------------------------------------------------------------------ GPU
+def run_next_rows(dev, pipe, rgb, reps=7):
+    """The survey's 'next' rows on the 4K frame, device-resident, CUDA-event
+    timed (L2 flushed before every repetition, inputs restored outside the
+    events): segment mean-colour render (compress -> segment means ->
+    propagate), smooth-boundary merge, the sample's Lab + beta and
+    intensity/chroma transforms, and SOR shape-from-shading normals (on the
+    1920x1080 luminance crop, fixed sweep counts).  gb_s counts algorithmic
+    bytes per pixel as stated in each entry."""
+    import ctypes as C
+    import torch
+    from split_gb300 import _native as N, ccl, color, kmeans, sfs
+    from split_gb300._util import Workspace, ptr, stream_handle
+    lib = N.load()
+    H, W = pipe.segment_labels.shape
+    n = W * H
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+
+    def timed(fn, prep=None):
+        ts = []
+        for r in range(reps + 2):
+            if prep is not None:
+                prep()
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            fn()
+            e1.record()
+            torch.cuda.synchronize()
+            if r >= 2:
+                ts.append(e0.elapsed_time(e1))
+        return statistics.median(ts)
+
+    def entry(ms, bpp, px=n):
+        return {"ms": round(ms, 4), "mpix_s": round(px / (ms * 1e-3) / 1e6, 1),
+                "bytes_per_px": bpp, "gb_s": round(px * bpp / (ms * 1e-3) / 1e9, 1)}
+
+    out = {}
+    feats = torch.empty((n, 4), dtype=torch.float32, device=dev)
+    color.pack_rgb8(rgb, feats)
+    planar = feats[:, :3].T.contiguous()
+    # the labelling before the small-segment merge (min-index, 8-connected)
+    lab0 = torch.empty((H, W), dtype=torch.int32, device=dev)
+    ccl.connected_components(pipe.cluster_labels.view(H, W), None, lab0, connectivity=8,
+                             convention=ccl.MIN_INDEX)
+    cws = Workspace(lib.split_compress_labels_workspace_size(n), dev)
+    count = torch.zeros(1, dtype=torch.int32, device=dev)
+
+    def render(labels2d):
+        """1: compress (in place, count left on the device), segment means of
+        the colour features, render"""
+        seg0 = labels2d.reshape(-1).clone()
+        seg = torch.empty_like(seg0)
+        t_c = timed(lambda: N.check(lib.split_compress_labels(ptr(seg), n, ptr(count), cws.ptr,
+                                                              cws.nbytes, stream_handle()),
+                                    "compress"), prep=lambda: seg.copy_(seg0))
+        nseg = int(count.item())
+        means = torch.zeros((3, nseg), dtype=torch.float32, device=dev)
+        mws = kmeans.calculate_centroids(seg, planar, means, width=W)
+        t_m = timed(lambda: kmeans.calculate_centroids(seg, planar, means, mws, width=W))
+        img = torch.empty((3, n), dtype=torch.float32, device=dev)
+        t_p = timed(lambda: kmeans.propagate_centroids(seg, means, img))
+        mws.check("segment means")
+        return {"segments": nseg,
+                "compress_labels": entry(t_c, 8),         # labels in, ranks out
+                "calculate_centroids": entry(t_m, 16),    # labels + 3 float features
+                "propagate_centroids": entry(t_p, 16)}    # labels in, 3 floats out
+
+    # a colour-only (3-D) clustering of the same frame fragments it into many
+    # components: segment means over more than 64 clusters (per-cluster
+    # fixed-point accumulators)
+    c3 = pipe.centroids[:3].contiguous().clone()
+    lab3 = torch.empty(n, dtype=torch.int32, device=dev)
+    kmeans.cluster(feats, c3, lab3, None, max_iter=5, threshold=-1.0,
+                   layout=N.LAYOUT_FLOAT4 | kmeans.UNIT_RANGE, dim=3, width=W)
+    frag = torch.empty((H, W), dtype=torch.int32, device=dev)
+    ccl.connected_components(lab3.view(H, W), None, frag, connectivity=8,
+                             convention=ccl.MIN_INDEX)
+    out["segment_mean_render"] = {"final_segments": render(pipe.segment_labels),
+                                  "colour_only_components": render(frag)}
+    # 2: smooth-boundary merge on the labelling before the small-segment merge
+    lab = torch.empty_like(lab0)
+    lab.copy_(lab0)
+    sws = ccl.merge_smooth_boundaries(planar, 0, lab)
+    t_s = timed(lambda: ccl.merge_smooth_boundaries(planar, 0, lab, sws),
+                prep=lambda: lab.copy_(lab0))
+    out["merge_smooth_boundaries"] = entry(t_s, 20)     # labels + 3 floats in, labels out
+    # 3: the sample's feature transforms from RGB8
+    lab_f = torch.empty((n, 4), dtype=torch.float32, device=dev)
+    lws = color.pack_lab_beta(rgb, lab_f)
+    t_l = timed(lambda: color.pack_lab_beta(rgb, lab_f, None, temp=lws))
+    ic = torch.empty((3, n), dtype=torch.float32, device=dev)
+    t_i = timed(lambda: color.rgb_to_ic(rgb, ic))
+    out["lab_beta"] = entry(t_l, 22)                    # RGB8 read twice, float4 out
+    out["rgb_to_ic"] = entry(t_i, 15)                   # RGB8 in, 3 floats out
+    # 4: SOR normals on a 1920 x 1080 crop of the L* plane, 50 and 200 sweeps
+    hh, ww = 1080, 1920
+    lum = torch.empty(n, dtype=torch.float32, device=dev)
+    color.pack_rgb8(rgb, None, lum)
+    shading = lum.view(H, W)[:hh, :ww].contiguous()
+    nrm = torch.empty((3, hh * ww), dtype=torch.float32, device=dev)
+    its = torch.zeros(1, dtype=torch.int32, device=dev)
+    ews = sfs.estimate_normals(shading, (0.3, -0.2, 1.0), nrm, 1.0, max_iter=1, tol=0.0,
+                               iterations_out=its)
+    sor = {}
+    for sweeps in (50, 200):
+        t_e = timed(lambda: sfs.estimate_normals(shading, (0.3, -0.2, 1.0), nrm, 1.0,
+                                                 max_iter=sweeps, tol=0.0, temp=ews,
+                                                 iterations_out=its))
+        # per sweep: two colour passes and the residual pass each read the
+        # 3 unknown planes (12 B) and the shading (4 B); the colour passes write 6 B
+        sor[f"{sweeps}_sweeps"] = {"ms": round(t_e, 3),
+                                   "mpix_sweeps_s": round(hh * ww * sweeps / (t_e * 1e-3) / 1e6, 1),
+                                   "gb_s": round(hh * ww * sweeps * (3 * 16 + 12) / (t_e * 1e-3) / 1e9, 1)}
+    out["estimate_normals_1080p"] = sor
+    for ws in (cws, sws, lws, ews):
+        ws.check("next rows")
+    return out
+
+
 def run_stress(dev, side=8192, steps=10, seed=2024):
     """Labelling stress case: side x side maze + blob labels (one serpentine
     corridor over half the pixels), 4- and 8-connected min-index CCL with
@@ -476,6 +595,8 @@ def main():
     ap.add_argument("--serve-requests", type=int, default=1024)
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--no-stress", action="store_true")
+    ap.add_argument("--no-next", action="store_true",
+                    help="skip the timings of the survey's next rows")
     ap.add_argument("--tune", default="auto", choices=["auto", "off"],
                     help="auto: this GPU's cached launch table, else measure it now; "
                          "off: the library defaults")
@@ -621,6 +742,10 @@ def main():
     if not args.no_batch and args.batch_images > 0:
         batched = run_batched(dev, args.batch_images, steps=5)
     stress = None if args.no_stress else run_stress(dev)
+    next_rows = None
+    if not args.no_next:
+        next_rows = run_next_rows(dev, pipe, rgb)
+
     serving = None
     if not args.no_serve and args.serve_requests > 0:
         serving = run_serving(dev, min(args.batch_images, 256) or 64, args.serve_requests)
@@ -654,6 +779,7 @@ def main():
             "batched": batched,
             "serving": serving,
             "stress": stress,
+            "next_rows": next_rows,
             "tuning": tuning,
             "wall_s_timed_region": round(t_wall, 3),
         }

@@ -32,6 +32,13 @@ def calculate_centroids_workspace(npoints: int, ncentroids: int, dim: int = 3) -
     return N.load().split_kmeans_update_workspace_size(npoints, ncentroids, dim)
 
 
+def default_width(n: int) -> int:
+    """A feature list without an image behind it is tiled as rows of this
+    width (as include/split_gb300.hpp does); pass the image width for 5-D
+    features, whose xy come from it."""
+    return n if 0 < n < 4096 else (4096 if n > 0 else 1)
+
+
 def _features(points: torch.Tensor, layout: int, dim: int | None):
     """Returns (npoints, dim) for a points tensor in the given layout."""
     require_cuda(points, "points")
@@ -53,7 +60,7 @@ def _features(points: torch.Tensor, layout: int, dim: int | None):
 
 def cluster(points: torch.Tensor, centroids: torch.Tensor, labels: torch.Tensor,
             temp: Workspace | None = None, max_iter: int = 10, threshold: float = 1.0, *,
-            layout: int = PLANAR, dim: int | None = None, width: int = 1,
+            layout: int = PLANAR, dim: int | None = None, width: int | None = None,
             xy_scale: float = 0.1, iterations_out: torch.Tensor | None = None,
             stream=None) -> Workspace:
     """split::device::kmeans::cluster (cluster.cuh:31-37, cluster.cu:27-93).
@@ -65,6 +72,7 @@ def cluster(points: torch.Tensor, centroids: torch.Tensor, labels: torch.Tensor,
     Returns the workspace used (pass it back in to reuse it).
     """
     n, d = _features(points, layout, dim)
+    width = default_width(n) if width is None else width
     require_cuda(centroids, "centroids", torch.float32)
     require_cuda(labels, "labels", torch.int32)
     if centroids.dim() != 2 or centroids.shape[0] != d:
@@ -82,9 +90,10 @@ def cluster(points: torch.Tensor, centroids: torch.Tensor, labels: torch.Tensor,
 
 def label_points(centroids: torch.Tensor, points: torch.Tensor, labels: torch.Tensor,
                  temp: Workspace | None = None, *, layout: int = PLANAR, dim: int | None = None,
-                 width: int = 1, xy_scale: float = 0.1, stream=None) -> Workspace:
+                 width: int | None = None, xy_scale: float = 0.1, stream=None) -> Workspace:
     """split::device::kmeans::label_points (label.cuh:27-31, label.cu:74-106)."""
     n, d = _features(points, layout, dim)
+    width = default_width(n) if width is None else width
     require_cuda(centroids, "centroids", torch.float32)
     require_cuda(labels, "labels", torch.int32)
     k = centroids.shape[1]
@@ -98,7 +107,8 @@ def label_points(centroids: torch.Tensor, points: torch.Tensor, labels: torch.Te
 
 def calculate_centroids(labels: torch.Tensor, points: torch.Tensor, centroids: torch.Tensor,
                         temp: Workspace | None = None, *, layout: int = PLANAR,
-                        dim: int | None = None, width: int = 1, xy_scale: float = 0.1,
+                        dim: int | None = None, width: int | None = None,
+                        xy_scale: float = 0.1,
                         stream=None) -> Workspace:
     """split::device::kmeans::calculate_centroids (centroids.cuh:26-30).
 
@@ -107,6 +117,7 @@ def calculate_centroids(labels: torch.Tensor, points: torch.Tensor, centroids: t
     accumulators.  Empty clusters keep their previous centroid (documented
     divergence); labels outside [0, K) are ignored."""
     n, d = _features(points, layout, dim)
+    width = default_width(n) if width is None else width
     require_cuda(centroids, "centroids", torch.float32)
     require_cuda(labels, "labels", torch.int32)
     k = centroids.shape[1]
