@@ -1581,6 +1581,11 @@ __device__ __forceinline__ unsigned long long shfl_xor_u64(unsigned long long v,
   const unsigned b = __shfl_xor_sync(0xffffffffu, (unsigned)(v >> 32), o);
   return ((unsigned long long)b << 32) | a;
 }
+__device__ __forceinline__ unsigned long long shfl_down_u64(unsigned long long v, int o) {
+  const unsigned a = __shfl_down_sync(0xffffffffu, (unsigned)v, o);
+  const unsigned b = __shfl_down_sync(0xffffffffu, (unsigned)(v >> 32), o);
+  return ((unsigned long long)b << 32) | a;
+}
 
 template <int LAYOUT, int DIM>
 __global__ void __launch_bounds__(kThreads)
@@ -1648,13 +1653,40 @@ accumulate_kernel(const int32_t* __restrict__ labels, const void* __restrict__ p
         }
         atomicAdd(L.cnt + l0, 32u);
       }
-    } else if (l >= 0) {
+    } else {
+      // Several labels: lanes hold consecutive pixels, so labels come in runs.
+      // A segmented reduction leaves each run's sums in its first lane (each
+      // lane adds from lane + o while that lane is still in its run), and only
+      // run heads issue atomics.  Integer sums: the same totals as per-pixel
+      // adds.
+      const int lprev = __shfl_up_sync(0xffffffffu, l, 1);
+      const unsigned heads = __ballot_sync(0xffffffffu, lane == 0 || l != lprev);
+      const unsigned after = heads & ~(0xffffffffu >> (31 - lane));   // heads right of this lane
+      const int run_end = after ? __ffs(after) - 1 : 32;
+      unsigned cnt = l >= 0 ? 1u : 0u;
 #pragma unroll
-      for (int d = 0; d < DIM; ++d) {
-        atomicAdd(L.lo + (size_t)l * DIM + d, qlo[d]);
-        atomicAdd(L.hi + (size_t)l * DIM + d, qhi[d]);
+      for (int o = 1; o < 32; o <<= 1) {
+        const bool in_run = lane + o < run_end;
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) {
+          const unsigned long long a = shfl_down_u64(qlo[d], o);
+          const unsigned long long b = shfl_down_u64(qhi[d], o);
+          if (in_run) {
+            qlo[d] += a;
+            qhi[d] += b;
+          }
+        }
+        const unsigned c = __shfl_down_sync(0xffffffffu, cnt, o);
+        if (in_run) cnt += c;
       }
-      atomicAdd(L.cnt + l, 1u);
+      if (l >= 0 && ((heads >> lane) & 1u)) {
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) {
+          atomicAdd(L.lo + (size_t)l * DIM + d, qlo[d]);
+          atomicAdd(L.hi + (size_t)l * DIM + d, qhi[d]);
+        }
+        atomicAdd(L.cnt + l, cnt);
+      }
     }
   }
 }
