@@ -12,13 +12,17 @@
 //
 // Passes (labels_out doubles as the global parent array):
 //   tile   : one block per TH x TW tile; labels staged in shared memory; local
-//            union-find on shared parents; every pixel writes the global
-//            index of its local root; local roots clear their size counter.
+//            union-find on shared parents.  A local root stores its own
+//            global index, every other pixel the bitwise complement of its
+//            local root's (a negative entry), and local roots store their
+//            tile-local pixel count as their size.
 //   border : per tile, edges to earlier tiles (W, NW, N, NE across the tile
-//            edge) are merged with lock-free atomicMin/atomicMax hooking.
-//   flatten: every pixel follows its parent chain to the root and stores it
-//            (in place; a concurrent reader sees an ancestor either way);
-//            optional per-component pixel counts, aggregated per warp.
+//            edge) are merged with lock-free atomicMin/atomicMax hooking of
+//            local roots (entries read at edge pixels are decoded first).
+//   flatten: every pixel follows its local root's chain to the final root
+//            and stores it (in place; a concurrent reader sees an ancestor
+//            either way); a local root hooked under another adds its count
+//            to the final root's size.
 //
 // compress_labels (compress_labels.cu:10-35) is a flag / scan / gather over
 // the label range [-1, n).
@@ -215,6 +219,9 @@ tile_kernel(const int32_t* __restrict__ in, Geoms gs, int* __restrict__ P,
   // are kept as bits; the unions (divergent, retried) come afterwards with
   // no warp-synchronous instruction behind them.
   unsigned links = 0;   // bit 6k + 3h + j: row k, half h, link j (N, NW, NE)
+  // bit 2k + h: the pixel that counts its row run (the run's last pixel for
+  // the minimum convention, whose node is the first; the first for maximum)
+  unsigned counts = 0;
 #pragma unroll
   for (int k = 0; k < kRowsPerWarp; ++k) {
     const int r = r0 + k;
@@ -233,6 +240,11 @@ tile_kernel(const int32_t* __restrict__ in, Geoms gs, int* __restrict__ P,
     const int urb = __shfl_down_sync(kFull, ub, 1);
     const int lb = lane == 0 ? a31 : lb0, ulb = lane == 0 ? ua31 : ulb0;
     const int ra = lane == 31 ? b0 : ra0, ura = lane == 31 ? ub0 : ura0;
+    if (r < th) {
+      const bool xa = ca && (MAXC ? (lane == 0 || la != a) : (lane + 1 >= tw || ra != a));
+      const bool xb = cb && (MAXC ? lb != b : (lane + 33 >= tw || rb != b));
+      counts |= ((unsigned)xa | ((unsigned)xb << 1)) << (2 * k);
+    }
     if (rok && ca) {
       const bool hasW = lane > 0, hasE = lane + 1 < tw;
       const Links l = needed<CONN>(ua == a, hasW && la == a, hasW && ula == a,
@@ -268,6 +280,8 @@ tile_kernel(const int32_t* __restrict__ in, Geoms gs, int* __restrict__ P,
     const int ia = r * TW + lane, ib = ia + 32;
     roota[k] = (r < th && ca && na[k] == ia) ? sroot(par, ia) : -1;
     rootb[k] = (r < th && cb && nb[k] == ib) ? sroot(par, ib) : -1;
+    lab[ia] = 0;   // labels are no longer read: lab counts pixels per root
+    lab[ib] = 0;
   }
   __syncthreads();
 #pragma unroll
@@ -277,22 +291,34 @@ tile_kernel(const int32_t* __restrict__ in, Geoms gs, int* __restrict__ P,
     if (rootb[k] >= 0) par[ia + 32] = rootb[k];
   }
   __syncthreads();
+  unsigned isroot = 0;   // bit 2k + h
 #pragma unroll
   for (int k = 0; k < kRowsPerWarp; ++k) {
     const int r = r0 + k;
     if (r >= th) continue;
     const long long rowg = off + (long long)(ty0 + r) * W + tx0;
-    if (ca) {
-      const int root = par[na[k]];
-      const long long g = rowg + lane;
-      __stcg(P + g, (int)(off + (long long)(ty0 + root / TW) * W + tx0 + root % TW));
-      if (sizes && root == r * TW + lane) sizes[g] = 0;
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      if (!(h ? cb : ca)) continue;
+      const int c = lane + 32 * h, nd = h ? nb[k] : na[k];
+      const int root = par[nd];
+      const int gr = (int)(off + (long long)(ty0 + root / TW) * W + tx0 + root % TW);
+      const bool own = root == r * TW + c;
+      __stcg(P + rowg + c, own ? gr : ~gr);
+      isroot |= (unsigned)own << (2 * k + h);
+      if (sizes && ((counts >> (2 * k + h)) & 1u)) {
+        const int ndc = nd - r * TW;
+        atomicAdd(&lab[root], MAXC ? ndc - c + 1 : c - ndc + 1);
+      }
     }
-    if (cb) {
-      const int root = par[nb[k]];
-      const long long g = rowg + lane + 32;
-      __stcg(P + g, (int)(off + (long long)(ty0 + root / TW) * W + tx0 + root % TW));
-      if (sizes && root == r * TW + lane + 32) sizes[g] = 0;
+  }
+  if (sizes) {
+    __syncthreads();
+    while (isroot) {
+      const int bit = __ffs(isroot) - 1;
+      isroot &= isroot - 1;
+      const int r = r0 + (bit >> 1), c = lane + 32 * (bit & 1);
+      sizes[off + (long long)(ty0 + r) * W + tx0 + c] = lab[r * TW + c];
     }
   }
 }
@@ -304,6 +330,10 @@ tile_kernel(const int32_t* __restrict__ in, Geoms gs, int* __restrict__ P,
 // at the local roots the tile pass stored and skip links implied by others
 // (the same rules as inside a tile, with neighbours read across the edge).
 constexpr int kBorderThreads = 128;
+
+// The local root named by a tile-pass entry (a non-root pixel stores its local
+// root's complement; a local root, hooked or not, stores a root index).
+__device__ __forceinline__ int local_root(int e) { return e < 0 ? ~e : e; }
 
 template <bool MAXC, int CONN>
 __global__ void __launch_bounds__(kBorderThreads)
@@ -330,10 +360,10 @@ border_kernel(const int32_t* __restrict__ in, Geoms gs, int* P, int* status) {
     // is made by that edge's warp; the rule still holds across tiles
     const Links l = needed<CONN>(N, Wq, NW, NE, E);
     if (l.n || l.nw || l.ne) {
-      const int a = __ldcg(P + g);
-      if (l.n) gunite<MAXC>(P, a, __ldcg(P + g - W), status);
-      if (l.nw) gunite<MAXC>(P, a, __ldcg(P + g - W - 1), status);
-      if (l.ne) gunite<MAXC>(P, a, __ldcg(P + g - W + 1), status);
+      const int a = local_root(__ldcg(P + g));
+      if (l.n) gunite<MAXC>(P, a, local_root(__ldcg(P + g - W)), status);
+      if (l.nw) gunite<MAXC>(P, a, local_root(__ldcg(P + g - W - 1)), status);
+      if (l.ne) gunite<MAXC>(P, a, local_root(__ldcg(P + g - W + 1)), status);
     }
   } else if (warp == 2) {
     if (tx0 == 0 || lane >= th) return;
@@ -343,7 +373,7 @@ border_kernel(const int32_t* __restrict__ in, Geoms gs, int* P, int* status) {
     const bool Wq = __ldg(in + g - 1) == v;
     if (lane == 0) {
       // the corner pixel: its N / NW links belong to the top-edge warps
-      if (Wq) gunite<MAXC>(P, __ldcg(P + g), __ldcg(P + g - 1), status);
+      if (Wq) gunite<MAXC>(P, local_root(__ldcg(P + g)), local_root(__ldcg(P + g - 1)), status);
       return;
     }
     const bool N = __ldg(in + g - W) == v;
@@ -353,9 +383,9 @@ border_kernel(const int32_t* __restrict__ in, Geoms gs, int* P, int* status) {
     const bool lw = Wq && !(N && NW);
     const bool lnw = CONN == 8 && NW && !Wq && !N;
     if (lw || lnw) {
-      const int a = __ldcg(P + g);
-      if (lw) gunite<MAXC>(P, a, __ldcg(P + g - 1), status);
-      if (lnw) gunite<MAXC>(P, a, __ldcg(P + g - W - 1), status);
+      const int a = local_root(__ldcg(P + g));
+      if (lw) gunite<MAXC>(P, a, local_root(__ldcg(P + g - 1)), status);
+      if (lnw) gunite<MAXC>(P, a, local_root(__ldcg(P + g - W - 1)), status);
     }
   } else if (CONN == 8) {
     // right column, rows 1 .. th - 1: the NE link into the tile to the right
@@ -365,124 +395,52 @@ border_kernel(const int32_t* __restrict__ in, Geoms gs, int* P, int* status) {
     const int v = __ldg(in + g);
     const bool NE = __ldg(in + g - W + 1) == v;
     if (NE && __ldg(in + g - W) != v && __ldg(in + g + 1) != v)
-      gunite<MAXC>(P, __ldcg(P + g), __ldcg(P + g - W + 1), status);
+      gunite<MAXC>(P, local_root(__ldcg(P + g)), local_root(__ldcg(P + g - W + 1)), status);
   }
 }
 
 // Flatten pass, one block per tile, same pixel mapping as the tile pass.
-// After the border pass every pixel's entry points at a local root of its
-// own tile (or, for a local root joined across tiles, at another tile's
-// local root).  Each local component is resolved once: pixels whose entry
-// leaves the tile chase the global forest (read-only: entries of other
-// tiles are being finalised concurrently, always to their root), the rest
-// follow entries inside the tile through shared memory.  Component sizes
-// are counted per tile and added with one atomic per local component.
-// Maps a global index to its local index in the tile, or -1 outside it,
-// without integer division: rows from a float reciprocal of the width, then
-// corrected by one (the offset is below 32 rows, so the estimate is within
-// one row).
-struct TileFrame {
-  long long base;   // global index of the tile's first pixel
-  int W, tw, th;
-  float invW;
-  __device__ __forceinline__ int local(long long v) const {
-    const long long d = v - base;
-    if (d < 0 || d >= (long long)(th - 1) * W + tw) return -1;
-    const int di = (int)d;
-    int r = __float2int_rz((float)di * invW);
-    int c = di - r * W;
-    if (c < 0) { --r; c += W; } else if (c >= W) { ++r; c -= W; }
-    return c < tw ? r * TW + c : -1;
-  }
-};
-
-__device__ __forceinline__ int groot(const int* P, int x, unsigned& budget) {
-  int p = __ldcg(P + x);
-  while (p != x && budget) {
-    --budget;
-    x = p;
-    p = __ldcg(P + x);
-  }
-  return x;
-}
-
+// Every pixel starts from its local root (its complemented entry, or itself
+// when the entry is a root index) and follows root entries to the final
+// root: one hop for components that stay within the tile or whose local
+// root is the final root.  Pixels of one local component chase the same
+// chain, so the loads go through L1; entries are only ever replaced by
+// ancestors, so a stale line still leads to the final root.  Non-root entries
+// are never on a chain, so storing their final roots in place is safe.  A
+// local root hooked under another adds its tile-local count to the final
+// root's size (nobody adds to a hooked root, so its count is final).
 __global__ void __launch_bounds__(kThreads)
 flatten_kernel(int* P, Geoms gs, int32_t* __restrict__ sizes, int* status) {
-  __shared__ int ent[TH * TW];   // the pixel's entry (global index)
-  __shared__ int res[TH * TW];   // resolved root of a terminal pixel, else -1
-  __shared__ int cnt[TH * TW];   // pixels that resolved through this terminal
   const TileRef t = tile_ref(gs, blockIdx.x);
   const int W = t.W, tx0 = t.tx0, ty0 = t.ty0;
-  const long long off = t.off;
   const int tw = min(TW, W - tx0), th = min(TH, t.H - ty0);
   const int lane = threadIdx.x & 31, r0 = (threadIdx.x >> 5) * kRowsPerWarp;
-  const TileFrame fr{off + (long long)ty0 * W + tx0, W, tw, th, 1.0f / (float)W};
-  int e[2 * kRowsPerWarp];
+  const int base = (int)(t.off + (long long)ty0 * W + tx0);
+  int g[2 * kRowsPerWarp], e[2 * kRowsPerWarp], x[2 * kRowsPerWarp], p[2 * kRowsPerWarp];
 #pragma unroll
   for (int k = 0; k < 2 * kRowsPerWarp; ++k) {
     const int r = r0 + (k >> 1), c = lane + 32 * (k & 1);
-    const int i = r * TW + c;
-    const bool ok = r < th && c < tw;
-    const long long g = off + (long long)(ty0 + r) * W + tx0 + c;
-    e[k] = ok ? __ldcg(P + g) : -1;
-    ent[i] = e[k];
-    cnt[i] = 0;
-    int rv = -1;
-    if (ok && e[k] == (int)g) rv = (int)g;
-    res[i] = rv;
+    g[k] = (r < th && c < tw) ? base + r * W + c : -1;
+    e[k] = g[k] >= 0 ? __ldcg(P + g[k]) : 0;
   }
-  __syncthreads();
-  // pixels whose entry leaves the tile: local roots joined elsewhere
 #pragma unroll
   for (int k = 0; k < 2 * kRowsPerWarp; ++k) {
-    const int r = r0 + (k >> 1), c = lane + 32 * (k & 1);
-    if (r < th && c < tw && res[r * TW + c] < 0 &&
-        fr.local(e[k]) < 0) {
-      unsigned budget = kFindCap;
-      res[r * TW + c] = groot(P, e[k], budget);
-      if (!budget) set_status(status, SPLIT_ERR_NOT_CONVERGED);
-    }
+    x[k] = local_root(e[k]);
+    p[k] = g[k] >= 0 && x[k] != g[k] ? P[x[k]] : x[k];
   }
-  __syncthreads();
-  // chase (divergent) first; warp-wide matching only once the warp has
-  // reconverged
-  int fin[2 * kRowsPerWarp], term[2 * kRowsPerWarp];
+  unsigned budget = kFindCap;
 #pragma unroll
   for (int k = 0; k < 2 * kRowsPerWarp; ++k) {
-    const int r = r0 + (k >> 1), c = lane + 32 * (k & 1);
-    int x = -1;
-    if (r < th && c < tw) {
-      x = r * TW + c;
-      for (unsigned hop = 0; res[x] < 0; ++hop) {
-        const int nx = fr.local(ent[x]);
-        if (nx < 0 || hop >= TH * TW) {   // cannot happen for a consistent forest
-          set_status(status, SPLIT_ERR_NOT_CONVERGED);
-          break;
-        }
-        x = nx;
-      }
+    if (g[k] < 0 || e[k] == g[k]) continue;   // outside, or a final root
+    while (p[k] != x[k] && budget) {
+      --budget;
+      x[k] = p[k];
+      p[k] = P[x[k]];
     }
-    term[k] = x;
-    fin[k] = (x >= 0 && res[x] >= 0) ? res[x] : -1;
+    P[g[k]] = x[k];
+    if (sizes && e[k] >= 0) atomicAdd(sizes + x[k], __ldcg(sizes + g[k]));
   }
-  __syncwarp();
-  if (sizes) {
-#pragma unroll
-    for (int k = 0; k < 2 * kRowsPerWarp; ++k) {
-      const unsigned peers = __match_any_sync(kFull, term[k]);
-      if (term[k] >= 0 && lane == __ffs(peers) - 1) atomicAdd(&cnt[term[k]], __popc(peers));
-    }
-  }
-  __syncthreads();
-#pragma unroll
-  for (int k = 0; k < 2 * kRowsPerWarp; ++k) {
-    const int r = r0 + (k >> 1), c = lane + 32 * (k & 1);
-    if (r < th && c < tw) {
-      const int i = r * TW + c;
-      __stcg(P + off + (long long)(ty0 + r) * W + tx0 + c, fin[k]);
-      if (sizes && cnt[i] > 0) atomicAdd(sizes + res[i], cnt[i]);
-    }
-  }
+  if (!budget) set_status(status, SPLIT_ERR_NOT_CONVERGED);
 }
 
 struct Layout {
