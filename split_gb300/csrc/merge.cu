@@ -24,6 +24,7 @@ namespace sg {
 namespace mrg {
 
 constexpr int kThreads = 256;
+static_assert(kTileH * kTileW % kThreads == 0, "whole pixels per thread in a tile");
 constexpr int kProbeCap = 1 << 16;
 constexpr unsigned kChainCap = 1u << 24;
 
@@ -129,13 +130,23 @@ pair_kernel(const int32_t* __restrict__ lab, Geoms gs, Layout L, const int32_t* 
   const long long n = gs.total_px;
   const TileRef tr = tile_ref(gs, blockIdx.x);
   const int W = tr.W, H = tr.H;
-  for (int q = threadIdx.x; q < kTileH * kTileW; q += blockDim.x) {
+  // all label loads, then all size gathers, before any pixel is examined:
+  // the eight pixels' dependent load pairs overlap instead of serialising
+  constexpr int kPer = kTileH * kTileW / kThreads;
+  int seg[kPer], sz[kPer];
+#pragma unroll
+  for (int j = 0; j < kPer; ++j) {
+    const int q = threadIdx.x + j * kThreads;
     const int x = tr.tx0 + q % kTileW, y = tr.ty0 + q / kTileW;
-    if (x >= W || y >= H) continue;
-    const long long i = tr.off + (long long)y * W + x;
-    const int s = __ldg(lab + i);
-    if (s < 0 || s >= n) continue;
-    if (__ldg(sizes + s) >= P) continue;
+    seg[j] = (x < W && y < H) ? __ldg(lab + tr.off + (long long)y * W + x) : -1;
+  }
+#pragma unroll
+  for (int j = 0; j < kPer; ++j) sz[j] = (seg[j] >= 0 && seg[j] < n) ? __ldg(sizes + seg[j]) : P;
+  for (int j = 0; j < kPer; ++j) {
+    if (sz[j] >= P) continue;
+    const int q = threadIdx.x + j * kThreads;
+    const int x = tr.tx0 + q % kTileW, y = tr.ty0 + q / kTileW;
+    const int s = seg[j];
     L.fin[s] = s;
     int t[8];
     int nt = 0;
