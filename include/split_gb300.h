@@ -364,7 +364,10 @@ size_t split_pipeline_workspace_size(int width, int height,
  * (segment_labels = merged, eroded labels; -1 = eroded).  normals: planar
  * 3 x w*h float out (may be null when compute_normals == 0).
  * stage_events: null, or 2 * SPLIT_PIPELINE_STAGES cudaEvent_t recorded
- * before/after each stage (a skipped stage records both back to back). */
+ * before/after each stage (a skipped stage records both back to back).  With
+ * SPLIT_LAYOUT_FLOAT4 features and compute_normals set, one pass over the
+ * bytes writes both the features and the normals: the first stage times it
+ * and the normals stage is empty. */
 int split_pipeline_run(const uint8_t* rgb, int width, int height,
                        const split_pipeline_params* params, float* centroids,
                        int32_t* cluster_labels, int32_t* segment_labels,

@@ -21,8 +21,6 @@ int ccl_geoms(const int32_t* in, const Geoms& gs, int connectivity, int conventi
               int32_t* sizes, WsHeader* hdr, cudaStream_t st);
 int erode_geoms(const int32_t* in, int32_t* out, const Geoms& gs, int radius, const void* mstate,
                 const int32_t* mfin, int local_labels, cudaStream_t st);
-int normals_rgb8_geoms(const uint8_t* rgb, const Geoms& gs, float depth, float* normals,
-                       cudaStream_t st);
 int batch_image_maps(const int32_t* labels, const uint8_t* rgb, int W, int H, int radius,
                      CUtensorMap* lab_map, CUtensorMap* rgb_map);
 int lab_beta_geoms(const uint8_t* rgb, const Geoms& gs, float mu, float* features4,
@@ -266,7 +264,12 @@ extern "C" int split_batch_run(split_batch* b, void* stream) {
   ss.p[ss.n++] = &static_cast<WsHeader*>(l.km_ws)->status;
   ss.p[ss.n++] = &static_cast<WsHeader*>(l.ccl_ws)->status;
   if (l.mrg_ws) ss.p[ss.n++] = &static_cast<WsHeader*>(l.mrg_ws)->status;
-  if (p.features == SPLIT_LAYOUT_FLOAT4)
+  // byte / 255 features with the normals, from one read of the bytes
+  const bool fused = p.features == SPLIT_LAYOUT_FLOAT4 && p.compute_normals;
+  if (fused)
+    SG_TRY(normals_rgb8_geoms(b->rgb, device_geoms(*b, l, l.rgb_maps), p.depth, b->normals,
+                              l.features4, st));
+  else if (p.features == SPLIT_LAYOUT_FLOAT4)
     SG_TRY(split_pack_rgb8(b->rgb, b->arena_px, l.features4, nullptr, stream));
   else if (p.features == kFeaturesLabBeta)
     SG_TRY(lab_beta_geoms(b->rgb, device_geoms(*b, l, nullptr), p.beta_mu, l.features4, l.maxima,
@@ -286,8 +289,9 @@ extern "C" int split_batch_run(split_batch* b, void* stream) {
   }
   SG_TRY(erode_geoms(l.seg, b->segment_labels, device_geoms(*b, l, l.lab_maps), p.erode_radius,
                      mstate, mfin, 1, st));
-  if (p.compute_normals)
-    SG_TRY(normals_rgb8_geoms(b->rgb, device_geoms(*b, l, l.rgb_maps), p.depth, b->normals, st));
+  if (p.compute_normals && !fused)
+    SG_TRY(normals_rgb8_geoms(b->rgb, device_geoms(*b, l, l.rgb_maps), p.depth, b->normals,
+                              nullptr, st));
   // errors the stages recorded in their own workspace headers, into the
   // batch's status word
   return fold_status(&l.hdr->status, ss, st);

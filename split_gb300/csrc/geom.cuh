@@ -85,4 +85,9 @@ __device__ __forceinline__ TileRef tile_ref(const Geoms& gs, int tile) {
   return r;
 }
 
+// Sobel normals of the L* plane straight from RGB8 over a geometry table;
+// with features4 set, the same pass writes the float4 byte / 255 features.
+int normals_rgb8_geoms(const uint8_t* rgb, const Geoms& gs, float depth, float* normals,
+                       float* features4, cudaStream_t st);
+
 }  // namespace sg

@@ -2,6 +2,7 @@
 // packing, k-means, connected components, small-segment merge decision,
 // fused relabel + erosion, and Sobel normals of the luminance plane.
 // Mirrors the stage order of samples/src/main.cu:154-314.
+#include "geom.cuh"
 #include "merge_state.cuh"
 
 namespace sg {
@@ -112,7 +113,13 @@ extern "C" int split_pipeline_run(const uint8_t* rgb, int width, int height,
       ((unsigned long long)l.bytes << 7) ^ ((unsigned long long)p.features << 3) ^
       (unsigned long long)(p.merge_P > 0) ^ ((unsigned long long)p.merge_policy << 1);
   if (!layout_unchanged(workspace, layout_key)) SG_TRY(clear_status(ss, st));
-  if (p.features == SPLIT_LAYOUT_FLOAT4)
+  // byte / 255 features with the normals, from one read of the bytes (the
+  // normals stage below is then empty)
+  const bool fused = p.features == SPLIT_LAYOUT_FLOAT4 && p.compute_normals;
+  if (fused)
+    SG_TRY(normals_rgb8_geoms(rgb, single_geom(width, height), p.depth, normals, l.features4,
+                              st));
+  else if (p.features == SPLIT_LAYOUT_FLOAT4)
     SG_TRY(split_pack_rgb8(rgb, n, l.features4, nullptr, stream));
   else if (p.features == pipe::kFeaturesLabBeta)
     SG_TRY(split_pack_lab_beta(rgb, n, p.beta_mu, SPLIT_LAYOUT_FLOAT4, l.features4, nullptr,
@@ -163,7 +170,8 @@ extern "C" int split_pipeline_run(const uint8_t* rgb, int width, int height,
   SG_TRY(mark(9));
   // 5: normals of the luminance plane, straight from the bytes
   SG_TRY(mark(10));
-  if (p.compute_normals) SG_TRY(split_sobel_normals_rgb8(rgb, width, height, p.depth, normals, stream));
+  if (p.compute_normals && !fused)
+    SG_TRY(split_sobel_normals_rgb8(rgb, width, height, p.depth, normals, stream));
   // errors the stages recorded in their own workspace headers, into the
   // pipeline's status word
   SG_TRY(fold_status(&l.hdr->status, ss, st));

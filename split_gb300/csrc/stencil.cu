@@ -303,6 +303,7 @@ struct NormArgs {
   float* out;            // per image: 3 planes at 3 * (arena offset)
   float zinv;
   int* status;
+  float4* features;      // optional, arena: (byte / 255) x 3, 0 per pixel
 };
 
 // heights (float) -> normals; staged box (TW + 8) x (TH + 2) from (tx0-4, ty0-1)
@@ -321,7 +322,9 @@ normals_kernel(const __grid_constant__ CUtensorMap tmap, bool use_tma, NormArgs 
 }
 
 // RGB8 -> luminance tile -> normals; staged bytes (3 TW + 32) x (TH + 2)
-// from byte column 3 tx0 - 16.
+// from byte column 3 tx0 - 16.  With a.features set, the tile's pixels also
+// get the float4 features pack_kernel writes (same table, same values), so a
+// pipeline that needs both reads the bytes once.
 __global__ void __launch_bounds__(kThreads)
 normals_rgb8_kernel(const __grid_constant__ CUtensorMap tmap, bool use_tma, NormArgs a,
                     Geoms gs) {
@@ -329,9 +332,13 @@ normals_rgb8_kernel(const __grid_constant__ CUtensorMap tmap, bool use_tma, Norm
   __shared__ __align__(128) unsigned char bytes[SWB * SH];
   __shared__ float lum[SH * HP];
   __shared__ float lin[256];
+  __shared__ float u8[256];
   __shared__ __align__(8) uint64_t bar;
   const TileRef t = tile_ref(gs, blockIdx.x);
-  for (int i = threadIdx.x; i < 256; i += blockDim.x) lin[i] = lin100(i);
+  for (int i = threadIdx.x; i < 256; i += blockDim.x) {
+    lin[i] = lin100(i);
+    u8[i] = (float)i / 255.0f;
+  }
   const CUtensorMap* map = pick_map(gs, t, use_tma ? &tmap : nullptr, kTmaRgb);
   if (!stage<unsigned char>(bytes, map, a.rgb + 3 * t.off, 3 * t.W, t.H, 3 * t.tx0 - 16,
                             t.ty0 - 1, SWB, SH, &bar, a.status))
@@ -340,6 +347,16 @@ normals_rgb8_kernel(const __grid_constant__ CUtensorMap tmap, bool use_tma, Norm
     const int r = i / HP, c = i % HP;  // pixel x = tx0 - 1 + c
     const unsigned char* p = bytes + r * SWB + 3 * c + 13;
     lum[i] = lum_from_lin(lin[p[0]], lin[p[1]], lin[p[2]]);
+  }
+  if (a.features) {
+    float4* f4 = a.features + t.off;
+    for (int i = threadIdx.x; i < TH * TW; i += blockDim.x) {
+      const int r = i / TW, c = i % TW;
+      const int x = t.tx0 + c, y = t.ty0 + r;
+      if (x >= t.W || y >= t.H) continue;
+      const unsigned char* p = bytes + (r + 1) * SWB + 3 * c + 16;   // pixel x
+      f4[(size_t)y * t.W + x] = make_float4(u8[p[0]], u8[p[1]], u8[p[2]], 0.0f);
+    }
   }
   __syncthreads();
   sobel_tile(lum, HP, t.tx0, t.ty0, t.W, t.H, a.zinv, a.out + 3 * t.off);
@@ -587,7 +604,7 @@ extern "C" int split_sobel_normals(const float* heights, int width, int height, 
 
 namespace sg {
 int normals_rgb8_geoms(const uint8_t* rgb, const Geoms& gs, float depth, float* normals,
-                       cudaStream_t st) {
+                       float* features4, cudaStream_t st) {
   CUtensorMap map;
   memset(&map, 0, sizeof(map));
   bool use_tma = false;
@@ -595,7 +612,8 @@ int normals_rgb8_geoms(const uint8_t* rgb, const Geoms& gs, float depth, float* 
     use_tma = make_tmap_2d(&map, CU_TENSOR_MAP_DATA_TYPE_UINT8, 1, rgb, (uint64_t)gs.one.W * 3,
                            (uint64_t)gs.one.H, (uint64_t)gs.one.W * 3, 3 * stn::TW + 32,
                            stn::TH + 2) == SPLIT_OK;
-  stn::NormArgs a{nullptr, rgb, normals, 1.0f / fmaxf(0.001f, depth), nullptr};
+  stn::NormArgs a{nullptr, rgb, normals, 1.0f / fmaxf(0.001f, depth),
+                  nullptr, reinterpret_cast<float4*>(features4)};
   stn::normals_rgb8_kernel<<<gs.total_tiles, stn::kThreads, 0, st>>>(map, use_tma, a, gs);
   return launch_status();
 }
@@ -630,7 +648,8 @@ extern "C" int split_sobel_normals_rgb8(const uint8_t* rgb, int width, int heigh
                                         float* normals, void* stream) {
   if (!rgb || !normals || width < 1 || height < 1) return SPLIT_ERR_INVALID;
   if ((int64_t)width * height * 3 > 0x7fffffffLL) return SPLIT_ERR_INVALID;
-  return normals_rgb8_geoms(rgb, single_geom(width, height), depth, normals, as_stream(stream));
+  return normals_rgb8_geoms(rgb, single_geom(width, height), depth, normals, nullptr,
+                            as_stream(stream));
 }
 
 extern "C" int split_rgb8_to_ic(const uint8_t* rgb, int64_t npixels, float* ic, void* stream) {
