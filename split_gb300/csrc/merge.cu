@@ -178,7 +178,7 @@ __device__ __forceinline__ float seg_mean(const Layout& L, const int32_t* sizes,
   return (float)L.sum[s] / (float)__ldg(sizes + s);
 }
 
-__global__ void bid_kernel(Layout L, const int32_t* sizes, int policy) {
+__device__ void bid_phase(const Layout& L, const int32_t* sizes, int policy) {
   const unsigned cnt = *(volatile unsigned*)&L.state->list_count;
   for (unsigned j = blockIdx.x * blockDim.x + threadIdx.x; j < cnt; j += gridDim.x * blockDim.x) {
     const int h = L.list[j];
@@ -201,7 +201,7 @@ __device__ __forceinline__ int bid_target(unsigned long long b, int policy) {
   return (int)(unsigned)((~b) & 0xffffffffull);
 }
 
-__global__ void decide_kernel(Layout L, int policy) {
+__device__ void decide_phase(const Layout& L, int policy) {
   const unsigned cnt = *(volatile unsigned*)&L.state->list_count;
   for (unsigned j = blockIdx.x * blockDim.x + threadIdx.x; j < cnt; j += gridDim.x * blockDim.x) {
     const unsigned long long k = L.keys[L.list[j]];
@@ -225,7 +225,7 @@ __device__ __forceinline__ int next_of(const Layout& L, const int32_t* sizes, in
 }
 
 // mutual pairs: the larger id keeps itself (fix_map_cycles.cuh:28-43)
-__global__ void cycle_kernel(Layout L, const int32_t* sizes, int P, int policy) {
+__device__ void cycle_phase(const Layout& L, const int32_t* sizes, int P, int policy) {
   const unsigned cnt = *(volatile unsigned*)&L.state->list_count;
   for (unsigned j = blockIdx.x * blockDim.x + threadIdx.x; j < cnt; j += gridDim.x * blockDim.x) {
     const unsigned long long k = L.keys[L.list[j]];
@@ -235,7 +235,8 @@ __global__ void cycle_kernel(Layout L, const int32_t* sizes, int P, int policy) 
   }
 }
 
-__global__ void resolve_kernel(Layout L, const int32_t* sizes, int P, int policy, int* status) {
+__device__ void resolve_phase(const Layout& L, const int32_t* sizes, int P, int policy,
+                              int* status) {
   const unsigned cnt = *(volatile unsigned*)&L.state->list_count;
   for (unsigned j = blockIdx.x * blockDim.x + threadIdx.x; j < cnt; j += gridDim.x * blockDim.x) {
     const unsigned long long k = L.keys[L.list[j]];
@@ -257,7 +258,7 @@ __global__ void resolve_kernel(Layout L, const int32_t* sizes, int P, int policy
 }
 
 // return the table and the bids to zero
-__global__ void cleanup_kernel(Layout L) {
+__device__ void cleanup_phase(const Layout& L) {
   const unsigned cnt = *(volatile unsigned*)&L.state->list_count;
   for (unsigned j = blockIdx.x * blockDim.x + threadIdx.x; j < cnt; j += gridDim.x * blockDim.x) {
     const int h = L.list[j];
@@ -268,6 +269,24 @@ __global__ void cleanup_kernel(Layout L) {
   }
 }
 
+// The decision over the pair list, one cooperative launch (one block per
+// SM): bids, decisions, mutual-pair fix, chains, cleanup, each phase behind a
+// bounded grid barrier.  The last step records the layout the guard cleared for.
+__global__ void __launch_bounds__(kThreads)
+list_kernel(Layout L, const int32_t* sizes, int P, int policy, unsigned long long stamp) {
+  WsHeader* h = L.hdr;
+  bid_phase(L, sizes, policy);
+  if (!grid_barrier(h)) return;
+  decide_phase(L, policy);
+  if (!grid_barrier(h)) return;
+  cycle_phase(L, sizes, P, policy);
+  if (!grid_barrier(h)) return;
+  resolve_phase(L, sizes, P, policy, &h->status);
+  if (!grid_barrier(h)) return;
+  cleanup_phase(L);
+  if (blockIdx.x == 0 && threadIdx.x == 0) h->stamp = stamp;
+}
+
 __global__ void relabel_kernel(int32_t* lab, int64_t n, const State* stp, const int32_t* fin) {
   const State st = *stp;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
@@ -275,10 +294,23 @@ __global__ void relabel_kernel(int32_t* lab, int64_t n, const State* stp, const 
     lab[i] = relabel(st, fin, lab[i]);
 }
 
-// Clears the state that every call leaves at zero (hash table, bids) when the
-// workspace was last used with another layout (or never): reusing one
-// workspace for images of different sizes moves these regions.
-__global__ void guard_kernel(const WsHeader* h, unsigned long long stamp, Layout L, long long n) {
+// Sets the run's parameters (block 0) and clears the state that every call
+// leaves at zero (hash table, bids) when the workspace was last used with
+// another layout (or never): reusing one workspace for images of different
+// sizes moves these regions.  list_kernel records the new layout at its end.
+__global__ void guard_kernel(WsHeader* h, unsigned long long stamp, Layout L, long long n,
+                             const int32_t* sizes, int P, int policy) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    State* st = L.state;
+    st->n = (int)n;
+    st->sizes = sizes;
+    st->P = P;
+    st->policy = policy;
+    st->unsorted = 0;
+    st->list_count = 0;
+    st->cap_log2 = L.cap_log2;
+    h->barrier_count = 0;
+  }
   if (*(volatile const unsigned long long*)&h->stamp == stamp) return;
   const long long cap = 1ll << L.cap_log2;
   const long long stride = (long long)gridDim.x * blockDim.x;
@@ -288,19 +320,6 @@ __global__ void guard_kernel(const WsHeader* h, unsigned long long stamp, Layout
   }
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += stride)
     L.best[i] = 0ull;
-}
-
-// the layout stamp (after the guard's clear) and the run's parameters
-__global__ void set_state_kernel(WsHeader* h, unsigned long long stamp, State* st,
-                                 const int32_t* sizes, int P, int policy, int cap_log2, int n) {
-  h->stamp = stamp;
-  st->n = n;
-  st->sizes = sizes;
-  st->P = P;
-  st->policy = policy;
-  st->unsorted = 0;
-  st->list_count = 0;
-  st->cap_log2 = cap_log2;
 }
 
 }  // namespace mrg
@@ -355,10 +374,7 @@ static int merge_run(int32_t* labels, const Geoms& gs, int P, int policy, const 
   const unsigned long long stamp = ((unsigned long long)l.cap_log2 << 40) | (unsigned long long)n;
   // the guard usually finds the stamp unchanged and exits: one block per SM
   // is enough for the rare full clear
-  mrg::guard_kernel<<<di.sm_count, mrg::kThreads, 0, st>>>(l.hdr, stamp, l, n);
-  SG_TRY(launch_status());
-  mrg::set_state_kernel<<<1, 1, 0, st>>>(l.hdr, stamp, l.state, sizes, P, policy, l.cap_log2,
-                                         (int)n);
+  mrg::guard_kernel<<<di.sm_count, mrg::kThreads, 0, st>>>(l.hdr, stamp, l, n, sizes, P, policy);
   SG_TRY(launch_status());
   if (!d_sizes) SG_CUDA_TRY(cudaMemsetAsync(l.size, 0, sizeof(int32_t) * (size_t)n, st));
   if (ref) SG_CUDA_TRY(cudaMemsetAsync(l.sum, 0, sizeof(double) * (size_t)n, st));
@@ -370,15 +386,19 @@ static int merge_run(int32_t* labels, const Geoms& gs, int P, int policy, const 
   mrg::pair_kernel<<<gs.total_tiles, mrg::kThreads, 0, st>>>(labels, gs, l, sizes, P,
                                                               &l.hdr->status);
   SG_TRY(launch_status());
-  mrg::bid_kernel<<<grid, mrg::kThreads, 0, st>>>(l, sizes, policy);
-  SG_TRY(launch_status());
-  mrg::decide_kernel<<<grid, mrg::kThreads, 0, st>>>(l, policy);
-  SG_TRY(launch_status());
-  mrg::cycle_kernel<<<grid, mrg::kThreads, 0, st>>>(l, sizes, P, policy);
-  SG_TRY(launch_status());
-  mrg::resolve_kernel<<<grid, mrg::kThreads, 0, st>>>(l, sizes, P, policy, &l.hdr->status);
-  SG_TRY(launch_status());
-  mrg::cleanup_kernel<<<grid, mrg::kThreads, 0, st>>>(l);
+  {
+    // one co-resident block per SM
+    int per_sm = 0;
+    SG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mrg::list_kernel,
+                                                              mrg::kThreads, 0));
+    if (per_sm < 1) return SPLIT_ERR_UNSUPPORTED;
+    unsigned long long stamp_arg = stamp;
+    int P_arg = P, policy_arg = policy;
+    const int32_t* sizes_arg = sizes;
+    void* args[] = {&l, &sizes_arg, &P_arg, &policy_arg, &stamp_arg};
+    SG_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)mrg::list_kernel, dim3(di.sm_count),
+                                            dim3(mrg::kThreads), args, 0, st));
+  }
   SG_TRY(launch_status());
   if (relabel_labels) {
     mrg::relabel_kernel<<<grid, mrg::kThreads, 0, st>>>(labels, n, l.state, l.fin);
