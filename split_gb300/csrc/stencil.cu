@@ -147,22 +147,53 @@ erode_kernel(const __grid_constant__ CUtensorMap tmap, bool use_tma, ErodeArgs a
     return;
   if (a.mstate) {
     const mrg::State ms = *a.mstate;
-    for (int i = threadIdx.x; i < SW * SH; i += blockDim.x) lab[i] = mrg::relabel(ms, a.mfin, lab[i]);
+    if (R1) {
+      // 72 x 34 entries, four per step (the staged tile is 16-byte aligned)
+      static_assert((TW + 8) * (TH + 2) % 4 == 0, "whole int4 steps");
+      int4* l4 = reinterpret_cast<int4*>(lab);
+      for (int i = threadIdx.x; i < SW * SH / 4; i += blockDim.x) {
+        int4 v = l4[i];
+        v.x = mrg::relabel(ms, a.mfin, v.x);
+        v.y = mrg::relabel(ms, a.mfin, v.y);
+        v.z = mrg::relabel(ms, a.mfin, v.z);
+        v.w = mrg::relabel(ms, a.mfin, v.w);
+        l4[i] = v;
+      }
+    } else {
+      for (int i = threadIdx.x; i < SW * SH; i += blockDim.x)
+        lab[i] = mrg::relabel(ms, a.mfin, lab[i]);
+    }
     __syncthreads();
   }
   const int base = a.local_labels ? (int)t.off : 0;
   int32_t* out = a.out + t.off;
   if (R1) {
-    for (int i = threadIdx.x; i < TH * TW; i += blockDim.x) {
-      const int r = i / TW, c = i % TW;
-      const int x = tx0 + c, y = ty0 + r;
-      if (x >= W || y >= H) continue;
-      const int* p = lab + (r + 1) * SW + (c + XP);
-      const int v = p[0];
-      bool keep = x >= 1 && y >= 1 && x + 1 < W && y + 1 < H;
-      keep = keep && p[-SW - 1] == v && p[-SW] == v && p[-SW + 1] == v && p[-1] == v &&
-             p[1] == v && p[SW - 1] == v && p[SW] == v && p[SW + 1] == v;
-      out[(size_t)y * W + x] = keep ? v - base : -1;
+    // thread: column c of the tile, rows [r0, r0 + kStrip); the 3 x 3 window
+    // slides down the column in registers, each row as its centre value and
+    // a flag for "left == centre == right"
+    constexpr int kGroups = kThreads / TW, kStrip = TH / kGroups;
+    static_assert(kThreads % TW == 0 && TH % kGroups == 0, "whole column strips");
+    const int c = threadIdx.x % TW, r0 = (threadIdx.x / TW) * kStrip;
+    const int x = tx0 + c;
+    if (x >= W) return;
+    const bool xin = x >= 1 && x + 1 < W;
+    const int* q = lab + r0 * SW + (c + XP);   // staged row r0 = image row ty0 + r0 - 1
+    int up = q[0], cu = q[SW];
+    bool tu = q[-1] == up && q[1] == up;
+    bool tc = q[SW - 1] == cu && q[SW + 1] == cu;
+#pragma unroll
+    for (int k = 0; k < kStrip; ++k) {
+      const int y = ty0 + r0 + k;
+      if (y >= H) break;
+      const int* d = q + (k + 2) * SW;
+      const int dn = d[0];
+      const bool td = d[-1] == dn && d[1] == dn;
+      const bool keep = xin && y >= 1 && y + 1 < H && tu && tc && td && up == cu && dn == cu;
+      out[(size_t)y * W + x] = keep ? cu - base : -1;
+      up = cu;
+      cu = dn;
+      tu = tc;
+      tc = td;
     }
     return;
   }
