@@ -379,7 +379,7 @@ int split_pipeline_run(const uint8_t* rgb, int width, int height,
 /* ======================================================================== */
 
 /* Many images of uneven size and per-image K / iteration count through the
- * segmentation path in one fixed launch sequence (about 16 launches whatever
+ * segmentation path in one fixed launch sequence (about 12 launches whatever
  * the image count; the k-means stage is one cooperative launch over every
  * image's tiles).  Each image's results are identical to running it alone. */
 typedef struct split_batch_image {
