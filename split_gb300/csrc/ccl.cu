@@ -485,37 +485,56 @@ int ccl_geoms(const int32_t* in, const Geoms& gs, int connectivity, int conventi
 // ---- label compression ----------------------------------------------------
 namespace cmp {
 
+// Ranks from a bitmask over the value range [-1, n): bit v + 1 is set when
+// some label equals v; the rank of v is the number of set bits below v + 1,
+// a per-word exclusive prefix of popcounts plus a popcount within the word.
+// The mask and the prefix are 1/32 of the label array each, so the scan is
+// short and the gather's lookups stay in L2.
 constexpr int kThreads = 256;
-constexpr int kTile = 4096;  // elements per scan tile
+constexpr int kTile = 4096;  // words per scan tile
 
 struct Layout {
   WsHeader* hdr;
-  int32_t* flags;       // [n + 1] -> ranks after the scan
-  int32_t* tile_sums;   // [ntiles]
+  uint32_t* bits;       // [nwords]
+  int32_t* prefix;      // [nwords]: set bits in the words before
+  int32_t* tile_sums;   // [ntiles + 1]
   size_t bytes;
 };
+
+inline int64_t words_of(int64_t n) { return (n + 1 + 31) / 32; }
 
 static Layout carve(void* ws, int64_t n) {
   Carver c(ws);
   Layout l;
+  const int64_t nw = words_of(n);
   l.hdr = c.take<WsHeader>(1);
-  l.flags = c.take<int32_t>((size_t)n + 1);
-  const int64_t tiles = (n + 1 + kTile - 1) / kTile;
+  l.bits = c.take<uint32_t>((size_t)nw);
+  l.prefix = c.take<int32_t>((size_t)nw);
+  const int64_t tiles = (nw + kTile - 1) / kTile;
   l.tile_sums = c.take<int32_t>((size_t)tiles + 1);
   l.bytes = c.size();
   return l;
 }
 
+// Sets the bit of every label value.  Only the first lane of a run of equal
+// values in the warp touches the mask, and only when it reads the bit clear
+// (a stale read just costs a redundant atomicOr).
 __global__ void mark_kernel(const int32_t* __restrict__ labels, int64_t n,
-                            int32_t* __restrict__ flags, int* status) {
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
-       i += (int64_t)gridDim.x * blockDim.x) {
-    const int v = labels[i];
-    if (v < -1 || v >= n) {
+                            uint32_t* bits, int* status) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < n; base += stride) {
+    const int64_t i = base + threadIdx.x;
+    int v = i < n ? labels[i] : -2;
+    if (i < n && (v < -1 || v >= n)) {
       set_status(status, SPLIT_ERR_INVALID);
-      continue;
+      v = -2;
     }
-    flags[v + 1] = 1;
+    const int prev = __shfl_up_sync(0xffffffffu, v, 1);
+    if (v >= -1 && ((threadIdx.x & 31) == 0 || prev != v)) {
+      const int p = v + 1;
+      const uint32_t bit = 1u << (p & 31);
+      if (!(bits[p >> 5] & bit)) atomicOr(bits + (p >> 5), bit);
+    }
   }
 }
 
@@ -545,15 +564,15 @@ __device__ __forceinline__ int block_exclusive_scan(int v, int* warp_tot, int& t
   return before + x - v;
 }
 
-// per-tile totals of the flags
-__global__ void tile_sum_kernel(const int32_t* __restrict__ flags, int64_t m,
+// per-tile totals of the set bits
+__global__ void tile_sum_kernel(const uint32_t* __restrict__ bits, int64_t nw,
                                 int32_t* __restrict__ sums) {
   __shared__ int red[kThreads / 32];
   const int64_t t0 = (int64_t)blockIdx.x * kTile;
   int s = 0;
   for (int i = threadIdx.x; i < kTile; i += kThreads) {
     const int64_t j = t0 + i;
-    if (j < m) s += flags[j];
+    if (j < nw) s += __popc(bits[j]);
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
@@ -584,26 +603,31 @@ __global__ void scan_sums_kernel(int32_t* sums, int64_t ntiles, int32_t* d_count
   }
 }
 
-// flags -> exclusive ranks, tile by tile
-__global__ void tile_scan_kernel(int32_t* flags, int64_t m, const int32_t* __restrict__ sums) {
+// per-word exclusive prefix of the popcounts, tile by tile
+__global__ void tile_scan_kernel(const uint32_t* __restrict__ bits, int64_t nw,
+                                 const int32_t* __restrict__ sums, int32_t* __restrict__ prefix) {
   __shared__ int warp_tot[kThreads / 32];
   const int64_t t0 = (int64_t)blockIdx.x * kTile;
   int carry = sums[blockIdx.x];
   for (int base = 0; base < kTile; base += kThreads) {
     const int64_t j = t0 + base + threadIdx.x;
-    const int v = j < m ? flags[j] : 0;
+    const int v = j < nw ? __popc(bits[j]) : 0;
     int total;
     const int ex = block_exclusive_scan(v, warp_tot, total);
-    if (j < m) flags[j] = carry + ex;
+    if (j < nw) prefix[j] = carry + ex;
     carry += total;
   }
 }
 
-__global__ void gather_kernel(int32_t* labels, int64_t n, const int32_t* __restrict__ ranks) {
+__global__ void gather_kernel(int32_t* labels, int64_t n, const uint32_t* __restrict__ bits,
+                              const int32_t* __restrict__ prefix) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
     const int v = labels[i];
-    if (v >= -1 && v < n) labels[i] = __ldg(ranks + v + 1);
+    if (v >= -1 && v < n) {
+      const int p = v + 1;
+      labels[i] = __ldg(prefix + (p >> 5)) + __popc(__ldg(bits + (p >> 5)) & ((1u << (p & 31)) - 1u));
+    }
   }
 }
 
@@ -650,19 +674,20 @@ extern "C" int split_compress_labels(int32_t* labels, int64_t n, int32_t* d_coun
   cudaStream_t st = as_stream(stream);
   DeviceInfo di;
   SG_TRY(device_info(&di));
-  const int64_t m = n + 1;
-  const int64_t ntiles = (m + cmp::kTile - 1) / cmp::kTile;
+  const int64_t nw = cmp::words_of(n);
+  const int64_t ntiles = (nw + cmp::kTile - 1) / cmp::kTile;
   int64_t blocks = (n + 255) / 256;
   if (blocks > (int64_t)di.sm_count * 16) blocks = (int64_t)di.sm_count * 16;
-  SG_CUDA_TRY(cudaMemsetAsync(l.flags, 0, sizeof(int32_t) * (size_t)m, st));
-  cmp::mark_kernel<<<(int)blocks, 256, 0, st>>>(labels, n, l.flags, &l.hdr->status);
+  SG_CUDA_TRY(cudaMemsetAsync(l.bits, 0, sizeof(uint32_t) * (size_t)nw, st));
+  cmp::mark_kernel<<<(int)blocks, 256, 0, st>>>(labels, n, l.bits, &l.hdr->status);
   SG_TRY(launch_status());
-  cmp::tile_sum_kernel<<<(int)ntiles, cmp::kThreads, 0, st>>>(l.flags, m, l.tile_sums);
+  cmp::tile_sum_kernel<<<(int)ntiles, cmp::kThreads, 0, st>>>(l.bits, nw, l.tile_sums);
   SG_TRY(launch_status());
   cmp::scan_sums_kernel<<<1, cmp::kThreads, 0, st>>>(l.tile_sums, ntiles, d_count);
   SG_TRY(launch_status());
-  cmp::tile_scan_kernel<<<(int)ntiles, cmp::kThreads, 0, st>>>(l.flags, m, l.tile_sums);
+  cmp::tile_scan_kernel<<<(int)ntiles, cmp::kThreads, 0, st>>>(l.bits, nw, l.tile_sums,
+                                                              l.prefix);
   SG_TRY(launch_status());
-  cmp::gather_kernel<<<(int)blocks, 256, 0, st>>>(labels, n, l.flags);
+  cmp::gather_kernel<<<(int)blocks, 256, 0, st>>>(labels, n, l.bits, l.prefix);
   return launch_status();
 }

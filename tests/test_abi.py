@@ -45,7 +45,10 @@ def test_workspace_queries():
     # without the width the bound covers the worst case (width 1)
     assert lib.split_kmeans_cluster_workspace_size(3840 * 2160, 16, 5) >= ws
     assert lib.split_merge_small_workspace_size(3840, 2160) > 3840 * 2160 * 16
-    assert lib.split_compress_labels_workspace_size(1000) >= 4 * 1001
+    # a bit per value in [-1, n) and a prefix per 32-bit word, after the header
+    words = (1000 + 1 + 31) // 32
+    assert lib.split_compress_labels_workspace_size(1000) >= 256 + 8 * words
+    assert lib.split_compress_labels_workspace_size(3840 * 2160) < 4 * 3840 * 2160 // 8
     p = _native.PipelineParams(16, 5, 0.1, 20, -1.0, 1, 8, 0, 256, 0, 1, 1, 1.0)
     assert lib.split_pipeline_workspace_size(3840, 2160, C.byref(p)) > 0
     bad = _native.PipelineParams(65, 5, 0.1, 20, -1.0, 1, 8, 0, 256, 0, 1, 1, 1.0)
