@@ -204,7 +204,7 @@ __device__ __forceinline__ float slot_mean(const Layout& L, int h) {
   return __double2float_rn(__ddiv_rn(__dmul_rn(S, 1.0 / 4294967296.0), (double)L.counts[h]));
 }
 
-__global__ void bid_kernel(Layout L, float threshold) {
+__device__ void bid_phase(const Layout& L, float threshold) {
   const unsigned cnt = *(volatile unsigned*)L.list_count;
   const float D = __fmul_rn(threshold, __fsqrt_rn(__uint_as_float(*(volatile unsigned*)L.maxsq)));
   for (unsigned j = blockIdx.x * blockDim.x + threadIdx.x; j < cnt; j += gridDim.x * blockDim.x) {
@@ -221,7 +221,7 @@ __device__ __forceinline__ int bid_target(unsigned long long b) {
   return (int)(unsigned)((~b) & 0xffffffffull);
 }
 
-__global__ void decide_kernel(Layout L) {
+__device__ void decide_phase(const Layout& L) {
   const unsigned cnt = *(volatile unsigned*)L.list_count;
   for (unsigned j = blockIdx.x * blockDim.x + threadIdx.x; j < cnt; j += gridDim.x * blockDim.x) {
     const unsigned long long k = L.keys[L.list[j]];
@@ -242,7 +242,7 @@ __device__ __forceinline__ int next_of(const Layout& L, int n, int r) {
 }
 
 // mutual pairs: the larger id keeps itself
-__global__ void cycle_kernel(Layout L, int n) {
+__device__ void cycle_phase(const Layout& L, int n) {
   const unsigned cnt = *(volatile unsigned*)L.list_count;
   for (unsigned j = blockIdx.x * blockDim.x + threadIdx.x; j < cnt; j += gridDim.x * blockDim.x) {
     const unsigned long long k = L.keys[L.list[j]];
@@ -253,7 +253,7 @@ __global__ void cycle_kernel(Layout L, int n) {
   }
 }
 
-__global__ void resolve_kernel(Layout L, int n) {
+__device__ void resolve_phase(const Layout& L, int n) {
   const unsigned cnt = *(volatile unsigned*)L.list_count;
   for (unsigned j = blockIdx.x * blockDim.x + threadIdx.x; j < cnt; j += gridDim.x * blockDim.x) {
     const unsigned long long k = L.keys[L.list[j]];
@@ -272,6 +272,19 @@ __global__ void resolve_kernel(Layout L, int n) {
     }
     L.fin[s] = r;
   }
+}
+
+// The decision over the (segment, neighbour) list, one cooperative launch (one
+// block per SM): bids, decisions, mutual-pair fix, chains, each phase behind a
+// bounded grid barrier.
+__global__ void __launch_bounds__(kThreads) list_kernel(Layout L, float threshold, int n) {
+  bid_phase(L, threshold);
+  if (!grid_barrier(L.hdr)) return;
+  decide_phase(L);
+  if (!grid_barrier(L.hdr)) return;
+  cycle_phase(L, n);
+  if (!grid_barrier(L.hdr)) return;
+  resolve_phase(L, n);
 }
 
 __global__ void __launch_bounds__(kThreads)
@@ -337,13 +350,17 @@ extern "C" int split_merge_smooth(int32_t* labels, int width, int height, const 
   edge_kernel<<<gs.total_tiles, kThreads, 0, st>>>(labels, points, gs, l, &l.hdr->status);
   SG_TRY(launch_status());
   const int grid = di.sm_count * 4;
-  bid_kernel<<<grid, kThreads, 0, st>>>(l, threshold);
-  SG_TRY(launch_status());
-  decide_kernel<<<grid, kThreads, 0, st>>>(l);
-  SG_TRY(launch_status());
-  cycle_kernel<<<grid, kThreads, 0, st>>>(l, (int)n);
-  SG_TRY(launch_status());
-  resolve_kernel<<<grid, kThreads, 0, st>>>(l, (int)n);
+  {
+    // one co-resident block per SM; the header clear above zeroed the barrier
+    int per_sm = 0;
+    SG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, list_kernel, kThreads, 0));
+    if (per_sm < 1) return SPLIT_ERR_UNSUPPORTED;
+    float thr = threshold;
+    int n32 = (int)n;
+    void* args[] = {&l, &thr, &n32};
+    SG_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)list_kernel, dim3(di.sm_count),
+                                            dim3(kThreads), args, 0, st));
+  }
   SG_TRY(launch_status());
   relabel_kernel<<<(int)blocks, kThreads, 0, st>>>(labels, n, l);
   SG_TRY(launch_status());
