@@ -284,22 +284,39 @@ __device__ __forceinline__ void sobel_tile(const float* h, int hp, int tx0, int 
   const size_t n = (size_t)W * H;
   if (tx0 >= 1 && ty0 >= 1 && tx0 + TW < W && ty0 + TH < H) {
     // the tile and its one-pixel ring lie inside the image: no clamping and
-    // no bounds checks; the same sums in the same order as below
+    // no bounds checks; the same sums in the same order as below.  Thread:
+    // column c, rows [r0, r0 + kStrip); the 3 x 3 window and the rows'
+    // horizontal [1 2 1] sums slide down the column in registers.
+    constexpr int kGroups = kThreads / TW, kStrip = TH / kGroups;
+    static_assert(kThreads % TW == 0 && TH % kGroups == 0, "whole column strips");
     const float zz = __fmul_rn(zinv, zinv), za = fabsf(zinv);
-    for (int i = threadIdx.x; i < TH * TW; i += blockDim.x) {
-      const int r = i / TW, c = i % TW;
-      const float* p = h + (r + 1) * hp + (c + 1);
-      const float sb = __fadd_rn(__fadd_rn(p[hp - 1], __fmul_rn(2.0f, p[hp])), p[hp + 1]);
-      const float st = __fadd_rn(__fadd_rn(p[-hp - 1], __fmul_rn(2.0f, p[-hp])), p[-hp + 1]);
-      const float tr = __fadd_rn(__fadd_rn(p[-hp + 1], __fmul_rn(2.0f, p[1])), p[hp + 1]);
-      const float tl = __fadd_rn(__fadd_rn(p[-hp - 1], __fmul_rn(2.0f, p[-1])), p[hp - 1]);
-      const float gy = __fsub_rn(sb, st);
+    const int c = threadIdx.x % TW, r0 = (threadIdx.x / TW) * kStrip;
+    const float* q = h + r0 * hp + (c + 1);   // the row above pixel row r0
+    float al = q[-1], ar = q[1];
+    float bl = q[hp - 1], bm = q[hp], br = q[hp + 1];
+    float sa = __fadd_rn(__fadd_rn(al, __fmul_rn(2.0f, q[0])), ar);
+    float sbm = __fadd_rn(__fadd_rn(bl, __fmul_rn(2.0f, bm)), br);
+    size_t g = (size_t)(ty0 + r0) * W + tx0 + c;
+#pragma unroll
+    for (int k = 0; k < kStrip; ++k, g += W) {
+      const float* d = q + (k + 2) * hp;   // the row below pixel row r0 + k
+      const float dl = d[-1], dm = d[0], dr = d[1];
+      const float sd = __fadd_rn(__fadd_rn(dl, __fmul_rn(2.0f, dm)), dr);
+      const float tr = __fadd_rn(__fadd_rn(ar, __fmul_rn(2.0f, br)), dr);
+      const float tl = __fadd_rn(__fadd_rn(al, __fmul_rn(2.0f, bl)), dl);
+      const float gy = __fsub_rn(sd, sa);
       const float gx = __fsub_rn(tr, tl);
       const float rm = rsqrtf(__fmaf_rn(gx, gx, __fmaf_rn(gy, gy, zz)));
-      const size_t g = (size_t)(ty0 + r) * W + tx0 + c;
       out[g] = __fmul_rn(gx, rm);
       out[n + g] = __fmul_rn(gy, rm);
       out[2 * n + g] = __fmul_rn(za, rm);
+      al = bl;
+      ar = br;
+      bl = dl;
+      bm = dm;
+      br = dr;
+      sa = sbm;
+      sbm = sd;
     }
     return;
   }

@@ -158,6 +158,32 @@ def test_sobel_normals_rgb8(cuda, w, h):
     assert np.arccos(cosang).max() <= 1e-4
 
 
+# With float4 features and normals both requested, the pipeline writes the
+# features in the normals pass (one read of the bytes).  Everything must equal
+# a run that packs the features alone, and the normals the standalone RGB8
+# normals, bit for bit.  Widths cover TMA staging (512) and plain staging.
+@pytest.mark.parametrize("w,h", [(512, 384), (333, 250), (98, 61)])
+def test_pipeline_features_in_normals_pass_match_separate_passes(cuda, w, h):
+    import torch
+    from split_gb300 import pipeline, sfs
+    rgb = synth.voronoi_rgb8(41 + w, w, h, 24, sigma=4.0)
+    c0 = synth.pick_centroids(41 + w, rgb, 16, 5)
+    g = _t(rgb, cuda)
+    fused = pipeline.Pipeline(w, h, pipeline.Params(merge_P=64), cuda)
+    fused.run(g, _t(c0, cuda))
+    sep = pipeline.Pipeline(w, h, pipeline.Params(merge_P=64, compute_normals=False), cuda)
+    sep.run(g, _t(c0, cuda))
+    ref = torch.empty((3, w * h), dtype=torch.float32, device=cuda)
+    sfs.sobel_normals_rgb8(g, ref, 1.0)
+    torch.cuda.synchronize()
+    fused.ws.check("fused pipeline")
+    sep.ws.check("separate passes")
+    assert torch.equal(fused.cluster_labels, sep.cluster_labels)
+    assert torch.equal(fused.segment_labels, sep.segment_labels)
+    assert torch.equal(fused.centroids, sep.centroids)
+    assert torch.equal(fused.normals.view(3, -1), ref)
+
+
 @pytest.mark.parametrize("k", [1, 5, 16, 33, 64])
 def test_kmeans_assign_pruning_exact(cuda, k):
     """Candidate pruning must not change any argmin: arbitrary planar 5-D
