@@ -148,16 +148,19 @@ erode_kernel(const __grid_constant__ CUtensorMap tmap, bool use_tma, ErodeArgs a
   if (a.mstate) {
     const mrg::State ms = *a.mstate;
     if (R1) {
-      // 72 x 34 entries, four per step (the staged tile is 16-byte aligned)
+      // 72 x 34 entries, four consecutive ones per step (the staged tile is
+      // 16-byte aligned); an entry equal to the one before it takes that
+      // one's result instead of gathering again
       static_assert((TW + 8) * (TH + 2) % 4 == 0, "whole int4 steps");
       int4* l4 = reinterpret_cast<int4*>(lab);
       for (int i = threadIdx.x; i < SW * SH / 4; i += blockDim.x) {
-        int4 v = l4[i];
-        v.x = mrg::relabel(ms, a.mfin, v.x);
-        v.y = mrg::relabel(ms, a.mfin, v.y);
-        v.z = mrg::relabel(ms, a.mfin, v.z);
-        v.w = mrg::relabel(ms, a.mfin, v.w);
-        l4[i] = v;
+        const int4 v = l4[i];
+        int4 o;
+        o.x = mrg::relabel(ms, a.mfin, v.x);
+        o.y = v.y == v.x ? o.x : mrg::relabel(ms, a.mfin, v.y);
+        o.z = v.z == v.y ? o.y : mrg::relabel(ms, a.mfin, v.z);
+        o.w = v.w == v.z ? o.z : mrg::relabel(ms, a.mfin, v.w);
+        l4[i] = o;
       }
     } else {
       for (int i = threadIdx.x; i < SW * SH; i += blockDim.x)
