@@ -345,7 +345,7 @@ def run_batched(dev, nimages, steps, seed=SEED + 1000):
 
 # ------------------------------------------------------------------------ GPU
 def run_next_rows(dev, pipe, rgb, reps=7):
-    """The survey's 'next' rows on the 4K frame, device-resident, CUDA-event
+    """The entry points downstream of the path on the 4K frame, device-resident, CUDA-event
     timed (L2 flushed before every repetition, inputs restored outside the
     events): segment mean-colour render (compress -> segment means ->
     propagate), smooth-boundary merge, the sample's Lab + beta and
@@ -596,7 +596,8 @@ def main():
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--no-stress", action="store_true")
     ap.add_argument("--no-next", action="store_true",
-                    help="skip the timings of the survey's next rows")
+                    help="skip the timings of the downstream entry points "
+                         "(segment-mean render, smooth merge, colour features, SOR normals)")
     ap.add_argument("--tune", default="auto", choices=["auto", "off"],
                     help="auto: this GPU's cached launch table, else measure it now; "
                          "off: the library defaults")
