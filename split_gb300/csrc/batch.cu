@@ -170,8 +170,6 @@ extern "C" int split_batch_create(const split_batch_image* images, int nimages,
   b->arena_px = off;
   b->cen_floats = coff;
   b->total_tiles = tiles;
-  Layout l0{};
-  (void)l0;
   std::vector<KmBatchImage> kmi = km_images(*b, Layout{});
   b->km_bytes = kmeans_batch_workspace(kmi.data(), nimages);
   b->ccl_bytes = split_ccl_workspace_size(1, 1);
