@@ -60,6 +60,18 @@ enum {
  * measuring each batch.  Features outside [0, 1] under this flag may be
  * mislabelled. */
 #define SPLIT_FEATURES_UNIT_RANGE 0x100
+/* Flag or-ed into the layout of split_kmeans_cluster: measure the centroid
+ * shift of the convergence test the way the reference's cluster() does
+ * (cluster.cu:40-50, :73-87).  It keeps the previous centroids in workspace
+ * words that label_points and calculate_centroids overwrite within the same
+ * iteration (label.cu:80-88, centroids.cu:40-63), so its "shift" compares the
+ * new centroids with 1 / (cluster sizes) and with the distances of two or
+ * three pixels near index 2N / K to the iteration's input centroids.  With
+ * this flag a threshold >= 0 stops at the reference's iteration (3-D
+ * features, K >= 3 only; anything else is SPLIT_ERR_INVALID).  Without it the
+ * shift is the L2 change of the centroid matrix, as cluster.cu's comments
+ * describe. */
+#define SPLIT_KMEANS_REFERENCE_SHIFT 0x200
 
 /* ---- label conventions / policies -------------------------------------- */
 enum {
@@ -113,18 +125,19 @@ int split_kmeans_cluster(const void* points, int layout, int dim,
 
 /* Allocation-free variant of split_kmeans_cluster (same arguments and
  * results, no workspace).  It has no counterpart in the reference.  It is for
- * callers that cannot allocate device memory where they cluster: code running
- * during CUDA graph capture or inside a latency-critical serving loop (where
- * cudaMalloc / cudaFree would synchronise the device), and host plugins whose
- * device memory belongs to a pool they may not touch.  Its scratch is one
- * fixed-size device array in the library, held by every GPU that loads the
- * library until the process exits.
- *   - Limit: the image may span at most 2048 tiles of 64 x 64 pixels (for
- *     example 3840 x 2160); larger images return SPLIT_ERR_WORKSPACE before
- *     any work is queued.
+ * callers that cannot allocate device memory where they cluster: a
+ * latency-critical serving loop (cudaMalloc / cudaFree synchronise the
+ * device) and host plugins whose device memory belongs to a pool they may
+ * not touch.  Its scratch is one fixed-size device array in the library
+ * (20736 bytes), held by every GPU that loads the library until the process
+ * exits.
+ *   - Limit: the array holds one image's clustering state for up to 64
+ *     clusters of 3 or 5 dimensions, whatever the image size.  Larger K (or
+ *     another D) returns SPLIT_ERR_INVALID before any work is queued.
  *   - The first call on each device looks up the array's device address
  *     (cudaGetSymbolAddress) with that device current; make that first call
- *     before any stream capture.
+ *     before any stream capture.  A cudaDeviceReset may move the array:
+ *     after resetting a device, do not call this entry point on it again.
  *   - All calls share the array and overwrite it: calls whose work overlaps
  *     on the GPU race.  Order them on one stream.
  *   - d_status (device int, optional) receives the device-side status word

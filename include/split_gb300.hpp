@@ -134,17 +134,31 @@ inline std::size_t cluster_workspace(int npoints, int nclusters, int dim, int wi
       npoints, width > 0 ? width : detail::default_width(npoints), nclusters, dim);
 }
 
+/* How cluster() measures the centroid shift of its convergence test.
+ * reference: as the reference's own code does (SPLIT_KMEANS_REFERENCE_SHIFT),
+ *   so a threshold >= 0 stops at the reference's iteration; used where that
+ *   rule is defined (threshold >= 0, 3-D points, K >= 3), the L2 change
+ *   elsewhere (a threshold < 0 runs exactly max_iter iterations either way).
+ * l2_change: the L2 change of the centroid matrix. */
+enum class Convergence { reference, l2_change };
+
 /* kmeans/cluster.cuh:31-37.  Planar D x N points (D = 3 or 5, all rows read
  * from memory), D x K centroids in/out.  Returns the iterations performed
  * (the reference returns nothing; reading the count synchronises `stream`). */
 inline int cluster(const_view2d<float> points, view2d<float> centroids, view1d<int> labels,
                    Temp& temp, int max_iter, float threshold = 1.f, int width = 0,
-                   cudaStream_t stream = nullptr) {
+                   cudaStream_t stream = nullptr,
+                   Convergence convergence = Convergence::reference) {
   const int64_t n = points.num_cols();
   const int w = width > 0 ? width : detail::default_width(n);
+  const int k = (int)centroids.num_cols();
+  const bool ref_rule = convergence == Convergence::reference && threshold >= 0.f &&
+                        points.num_rows() == 3 && k >= 3 && n * (k - 2) >= 3 * (int64_t)k;
   temp.reserve(split_kmeans_cluster_workspace_size_2d(n, w, (int)centroids.num_cols(),
                                                       (int)points.num_rows()));
-  check(split_kmeans_cluster(points.data(), SPLIT_LAYOUT_PLANAR, (int)points.num_rows(), n, w,
+  check(split_kmeans_cluster(points.data(),
+                             SPLIT_LAYOUT_PLANAR | (ref_rule ? SPLIT_KMEANS_REFERENCE_SHIFT : 0),
+                             (int)points.num_rows(), n, w,
                              0.f, centroids.data(), (int)centroids.num_cols(), labels.data(),
                              temp.get(), temp.size(), max_iter, threshold, temp.scalar(0),
                              stream),

@@ -256,3 +256,66 @@ def estimate_normals_rb(intensity: np.ndarray, light, smoothness: float, max_ite
     n = np.sqrt((x * x).sum(0))
     out = np.stack([x[0] / n, x[1] / n, np.abs(x[2]) / n]).reshape(3, -1)
     return out, it
+
+
+def reference_shift(points: np.ndarray, c_old: np.ndarray, c_new: np.ndarray,
+                    counts: np.ndarray) -> float:
+    """The centroid shift as the reference's cluster() measures it, in FP32
+    (split/src/split/device/kmeans/cluster.cu:40-50, :73-87).  Its previous
+    centroids sit at float offset 2N of the workspace, which label_points
+    (label.cu:80-88: N x K distances, entry i * K + c) and calculate_centroids
+    (centroids.cu:40-63: K reciprocal cluster sizes at offset 2N) overwrite in
+    the same iteration.  The new centroids (planar 3 x K, entry j = d * K + k)
+    are therefore compared with 1 / n_j for j < K and with the distance of
+    point (2N + j) // K to input centroid (2N + j) % K (Norm2, label.cu:23-32)
+    for j >= K; the squares are summed in j order."""
+    f32 = np.float32
+    p = np.asarray(points, f32)
+    n = p.shape[1]
+    k = c_new.shape[1]
+    acc = f32(0.0)
+    for j in range(3 * k):
+        if j < k:
+            word = f32(1.0) / f32(counts[j])
+        else:
+            e = 2 * n + j
+            px, c = e // k, e % k
+            a = [f32(p[d, px]) - f32(c_old[d, c]) for d in range(3)]
+            word = (a[0] * a[0] + a[1] * a[1]) + a[2] * a[2]
+        t = f32(c_new[j // k, j % k]) - f32(word)
+        acc = f32(acc + t * t)
+    return float(np.sqrt(acc, dtype=f32))
+
+
+def kmeans_cluster_threshold(points: np.ndarray, c0: np.ndarray, max_iter: int,
+                             threshold: float, reference_shift_rule: bool = True):
+    """cluster(points, c0, max_iter, threshold) (cluster.cu:27-93): FP32-exact
+    assignments and FP64 updates (rounded to FP32) until max_iter iterations
+    or |delta - old_delta| <= threshold, delta = 0 and old_delta = threshold
+    + 1 at the start (:65-71).  With reference_shift_rule the shift is
+    reference_shift(); otherwise the L2 change of the centroid matrix.
+    Returns (labels, centroids, iterations, shifts)."""
+    p = np.asarray(points, np.float32)
+    c = np.asarray(c0, np.float32).copy()
+    delta, old_delta = np.float32(0.0), np.float32(threshold) + np.float32(1.0)
+    it, shifts, lab = 0, [], None
+    while it < max_iter and abs(float(delta) - float(old_delta)) > threshold:
+        it += 1
+        lab = kmeans_assign_f32(p, c)
+        c64, cnt = kmeans_update_f64(lab, p, c)
+        cn = c64.astype(np.float32)
+        old_delta = delta
+        if reference_shift_rule:
+            delta = np.float32(reference_shift(p, c, cn, cnt))
+        else:
+            delta = np.float32(np.sqrt(np.sum((cn - c).astype(np.float64) ** 2)))
+        shifts.append(float(delta))
+        c = cn
+    return lab, c, it, shifts
+
+
+def propagate_centroids(labels: np.ndarray, centroids: np.ndarray) -> np.ndarray:
+    """out[:, i] = centroids[:, labels[i]] (propagation.cu:9-24: a gather of
+    the centroid columns by label).  Returns (D, N) float32."""
+    c = np.asarray(centroids, np.float32)
+    return np.ascontiguousarray(c[:, np.asarray(labels).reshape(-1)])

@@ -34,6 +34,8 @@
 ORC_API void orc_kmeans_assign_f32(const float* pts, int dim, int64_t n,
                                    const float* cent, int k,
                                    int32_t* labels) {
+  /* pixels are independent: threads change nothing in the result */
+#pragma omp parallel for schedule(static)
   for (int64_t i = 0; i < n; ++i) {
     float best = INFINITY;
     int bk = 0;
@@ -57,6 +59,7 @@ ORC_API void orc_kmeans_assign_f32(const float* pts, int dim, int64_t n,
 ORC_API void orc_kmeans_assign_f64(const float* pts, int dim, int64_t n,
                                    const float* cent, int k, int32_t* labels,
                                    double* d1, double* d2) {
+#pragma omp parallel for schedule(static)
   for (int64_t i = 0; i < n; ++i) {
     double b1 = INFINITY, b2 = INFINITY;
     int bk = 0;

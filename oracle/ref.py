@@ -57,6 +57,33 @@ def kmeans_cluster(points, centroids, iters):
     return lab, c
 
 
+def kmeans_cluster_threshold(points, centroids, max_iter, threshold):
+    """cluster(..., max_iter, threshold) (cluster.cu:27-93).  Returns (labels,
+    centroids, iterations, shifts): the reference prints each iteration's
+    centroid shift and, at the end, its iteration count (cluster.cu:88-92);
+    both are read back from its stdout."""
+    import re
+    import tempfile
+    p = np.ascontiguousarray(points, np.float32)
+    c = np.ascontiguousarray(centroids, np.float32).copy()
+    lab = np.empty(p.shape[1], np.int32)
+    lib = load()
+    lib.ref_kmeans_cluster_threshold.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_void_p,
+                                                 C.c_int, C.c_void_p, C.c_int, C.c_float]
+    lib.ref_kmeans_cluster_threshold.restype = C.c_int
+    with tempfile.TemporaryFile(mode="w+") as f:
+        with capture(f.fileno()):
+            lib.ref_kmeans_cluster_threshold(_p(p), p.shape[0], p.shape[1], _p(c), c.shape[1],
+                                             _p(lab), int(max_iter), float(threshold))
+        f.seek(0)
+        text = f.read()
+    m = re.search(r"in (\d+) iterations", text)
+    if not m:
+        raise RuntimeError("the reference did not report its iteration count")
+    shifts = [float(x) for x in re.findall(r"^([-+0-9.eE]+)$", text, re.M)]
+    return lab, c, int(m.group(1)), shifts
+
+
 def label_points(points, centroids):
     p = np.ascontiguousarray(points, np.float32)
     c = np.ascontiguousarray(centroids, np.float32)
@@ -150,6 +177,27 @@ def lab_beta(rgb_planar, mu=1e5):
     lib.ref_lab_beta.restype = C.c_int
     lib.ref_lab_beta(_p(a), n, float(mu), _p(feats), _p(lum))
     return feats, lum
+
+
+class capture:
+    """Sends the process's stdout (file descriptor 1) to another descriptor
+    for the duration of a block: the reference's progress prints."""
+
+    def __init__(self, fd: int):
+        self.fd = fd
+
+    def __enter__(self):
+        import sys
+        sys.stdout.flush()
+        self._saved = os.dup(1)
+        os.dup2(self.fd, 1)
+        return self
+
+    def __exit__(self, *exc):
+        libc = C.CDLL(None)
+        libc.fflush(None)
+        os.dup2(self._saved, 1)
+        os.close(self._saved)
 
 
 class quiet:

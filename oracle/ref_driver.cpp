@@ -71,6 +71,23 @@ int ref_kmeans_cluster(const float* pts, int dim, int n, float* cent, int k, int
   return 0;
 }
 
+// cluster() with a convergence threshold (cluster.cu:71: it stops once the
+// change of the centroid shift between iterations is at most i_threshold).
+// The reference reports its iteration count and every shift on stdout only;
+// oracle/ref.py reads them from there.
+int ref_kmeans_cluster_threshold(const float* pts, int dim, int n, float* cent, int k,
+                                 int32_t* labels, int max_iter, float threshold) {
+  Mat P(dim, n), Cc(dim, k);
+  IVec L(n);
+  to_dev(P, pts, (std::size_t)dim * n);
+  to_dev(Cc, cent, (std::size_t)dim * k);
+  Temp t(split::device::kmeans::cluster_workspace(n, k, dim));
+  split::device::kmeans::cluster(P, Cc, L, t.p, max_iter, threshold);
+  to_host(Cc, cent, (std::size_t)dim * k);
+  thrust::copy(L.begin(), L.end(), labels);
+  return 0;
+}
+
 int ref_label_points(const float* pts, int dim, int n, const float* cent, int k,
                      int32_t* labels) {
   Mat P(dim, n), Cc(dim, k);

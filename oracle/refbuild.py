@@ -6,8 +6,9 @@ erosion, Sobel normals) with g++ against CUDA 13's Thrust using the OpenMP
 device system, through the CUSP container subset in oracle/cusp_shim, and
 links them with oracle/ref_driver.cpp into oracle/_ref/libsplitref.so.
 
-The reference sources are read from REF_ROOT (default /root/reference) and
-copied into the git-ignored oracle/_ref/src, where two mechanical edits are
+The reference sources are read from REF_ROOT (the SPLIT_REF_ROOT environment
+variable, else the "reference_path" recorded in the repository's
+the benchmark spec) and copied into the git-ignored oracle/_ref/src, where two mechanical edits are
 applied to the copies (the reference itself is never modified and nothing of
 it is committed):
   1. member ``x.get<N>()`` becomes ``thrust::get<N>(x)``: CCCL 3's
@@ -28,7 +29,23 @@ import subprocess
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_ROOT = os.environ.get("SPLIT_REF_ROOT", "/root/reference")
+
+
+def _reference_root() -> str:
+    """SPLIT_REF_ROOT, else BASELINE.json's reference_path; "" when neither
+    names one (the staged copies are then compiled as they are)."""
+    env = os.environ.get("SPLIT_REF_ROOT")
+    if env:
+        return env
+    try:
+        import json
+        with open(os.path.join(os.path.dirname(HERE), "BASELINE.json")) as f:
+            return str(json.load(f).get("reference_path", ""))
+    except (OSError, ValueError):
+        return ""
+
+
+REF_ROOT = _reference_root()
 OUT = os.path.join(HERE, "_ref")
 SRC = os.path.join(OUT, "src")
 BUILD = os.path.join(OUT, "build", platform.machine())
@@ -117,8 +134,8 @@ def rewrite_get(text: str) -> str:
 def stage_sources(verbose: bool = False) -> bool:
     """Copy + patch the reference sources into oracle/_ref/src.  Returns False
     when neither the reference nor an earlier copy is available."""
-    ref_split = os.path.join(REF_ROOT, "split")
-    if not os.path.isdir(ref_split):
+    ref_split = os.path.join(REF_ROOT, "split") if REF_ROOT else ""
+    if not ref_split or not os.path.isdir(ref_split):
         return os.path.isdir(os.path.join(SRC, "include"))
     if os.path.isdir(SRC):
         shutil.rmtree(SRC)

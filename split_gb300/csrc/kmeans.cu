@@ -75,6 +75,7 @@ struct Image {
   int height;               // rows (ceil(npoints / width))
   int ntx;                  // tiles per row of tiles
   int unit_rows;            // rows of a unit (kTile or 2 * kTile, from the tuning table)
+  int ref_shift;            // SPLIT_KMEANS_REFERENCE_SHIFT (D = 3, K >= 3)
 };
 
 struct ImageState {
@@ -793,6 +794,49 @@ __device__ __forceinline__ void load_centroids(const float* src, int K,
   }
 }
 
+// The squared "centroid shift" as the reference's cluster() measures it
+// (cluster.cu:40-50, :73-87): it keeps the previous centroids at float
+// offset 2N of its workspace, but within the same iteration label_points
+// writes its N x K distance matrix from offset 0 (label.cu:80-88, entry
+// i * K + c = distance of point i to centroid c, Norm2 at label.cu:23-32) and
+// calculate_centroids writes its K reciprocal cluster sizes at offset 2N
+// (centroids.cu:40-63).  So the words it compares the new centroids with
+// (planar, entry j = d * K + k) are
+//   j < K:  1 / n_j (the reciprocal size of cluster j, FP32 division);
+//   j >= K: the distance of point (2N + j) / K to centroid (2N + j) % K of
+//           the iteration's input, sum of squares in dimension order;
+// and the shift is the FP32 sum of (c_new[j] - word[j])^2 in j order.  Only
+// the reference's 3-D case is defined, and only for K >= 3 (smaller K would
+// read words no call of the iteration wrote).
+template <int LAYOUT, int DIM>
+__device__ float reference_shift(const Image& im, const float* cent, const float* c_old,
+                                 const unsigned* cnt, const float* lut) {
+  constexpr int CS = cstride(DIM);
+  Loader<LAYOUT, DIM> ld{im.points, im.npoints, im.xy_scale, lut};
+  const int64_t base = 2 * im.npoints;
+  float acc = 0.0f;
+  for (int j = 0; j < im.K * 3; ++j) {
+    const int d = j / im.K, k = j % im.K;
+    float word;
+    if (j < im.K) {
+      word = __fdiv_rn(1.0f, (float)__ldcg(cnt + j));
+    } else {
+      const int64_t e = base + j;
+      const int64_t px = e / im.K;
+      const int c = (int)(e % im.K);
+      float f[DIM];
+      ld.load(px, 0, 0, f);
+      const float a0 = __fsub_rn(f[0], __ldcg(c_old + c * 8 + 0));
+      const float a1 = __fsub_rn(f[1], __ldcg(c_old + c * 8 + 1));
+      const float a2 = __fsub_rn(f[2], __ldcg(c_old + c * 8 + 2));
+      word = __fadd_rn(__fadd_rn(__fmul_rn(a0, a0), __fmul_rn(a1, a1)), __fmul_rn(a2, a2));
+    }
+    const float t = __fsub_rn(cent[k * CS + d], word);
+    acc = __fadd_rn(acc, __fmul_rn(t, t));
+  }
+  return acc;
+}
+
 // Centroids of iteration i >= 1 of an image, c(i) = c(i-1) + S(i-1) / n
 // (empty cluster: unchanged; cluster.cu:71-88), formed after the grid barrier
 // that ended iteration i - 1, and the convergence test of that iteration.
@@ -808,9 +852,9 @@ __device__ __forceinline__ void load_centroids(const float* src, int K,
 // iteration i+1), and on convergence the caller's centroids and iteration
 // count.  Returns whether the image runs iteration i (uniform in the block);
 // its centroids are left in `cent` (stride cstride(DIM)).
-template <int DIM, int MODE>
+template <int LAYOUT, int DIM, int MODE>
 __device__ bool form_centroids(const Params& p, int img, const Image& im, int i, float* cent,
-                               bool owner) {
+                               bool owner, const float* lut) {
   constexpr int CS = cstride(DIM);
   __shared__ float sdiff[kMaxK * kMaxDim];
   __shared__ int smore, sstopped;
@@ -867,6 +911,8 @@ __device__ bool form_centroids(const Params& p, int img, const Image& im, int i,
     float acc = 0.0f;
     for (int idx = threadIdx.x; idx < im.K * DIM; idx += 32) acc = __fadd_rn(acc, sdiff[idx]);
     acc = warp_sum(acc);
+    if (DIM == 3 && im.ref_shift && threadIdx.x == 0)
+      acc = reference_shift<LAYOUT, DIM>(im, cent, c_old, cnt, lut);
     if (threadIdx.x == 0) {
       const float delta = sqrtf(acc);
       const float old_delta = __ldcg(&prev->delta);
@@ -914,7 +960,8 @@ __global__ void __launch_bounds__(kThreads, SG_KM_MINBLOCKS) kmeans_kernel(Param
       if (p.nimages == 1) {
         // every block forms the single image's centroids (block 0 publishes),
         // so all of them see it converge together
-        more = form_centroids<DIM, MODE>(p, 0, image_of(p, 0), it, sm.cent, blockIdx.x == 0);
+        more = form_centroids<LAYOUT, DIM, MODE>(p, 0, image_of(p, 0), it, sm.cent,
+                                                 blockIdx.x == 0, sm.lut);
         cached = 0;
         if (!more) {
           stopped = true;
@@ -925,7 +972,8 @@ __global__ void __launch_bounds__(kThreads, SG_KM_MINBLOCKS) kmeans_kernel(Param
         // barrier, so that a block switching images (often, with small
         // images) only loads the published centroids.
         for (int img = (int)blockIdx.x; img < p.nimages; img += gridDim.x)
-          form_centroids<DIM, MODE>(p, img, image_of(p, img), it, sm.cent, true);
+          form_centroids<LAYOUT, DIM, MODE>(p, img, image_of(p, img), it, sm.cent, true,
+                                            sm.lut);
         if (!grid_barrier(p.hdr)) return;
       }
     }
@@ -974,7 +1022,8 @@ __global__ void __launch_bounds__(kThreads, SG_KM_MINBLOCKS) kmeans_kernel(Param
   if (MODE == kAssignOnly || stopped) return;
   // centroids after the last iteration; every image stops here
   for (int img = (int)blockIdx.x; img < p.nimages; img += gridDim.x)
-    form_centroids<DIM, MODE>(p, img, image_of(p, img), p.max_iter, sm.cent, true);
+    form_centroids<LAYOUT, DIM, MODE>(p, img, image_of(p, img), p.max_iter, sm.cent, true,
+                                      sm.lut);
 }
 
 // ---------------------------------------------------------------------------
@@ -1138,7 +1187,7 @@ static int dispatch(int layout, int dim, Params& p, cudaStream_t st) {
 
 static bool valid_features(const void* points, int layout, int dim, int64_t n,
                            int width, int K) {
-  layout &= ~SPLIT_FEATURES_UNIT_RANGE;
+  layout &= ~(SPLIT_FEATURES_UNIT_RANGE | SPLIT_KMEANS_REFERENCE_SHIFT);
   if (!points || n <= 0 || n > 0x7fffffffLL || K < 1 || K > kMaxK) return false;
   if (dim != 3 && dim != 5) return false;
   if (layout < SPLIT_LAYOUT_PLANAR || layout > SPLIT_LAYOUT_RGB8) return false;
@@ -1154,7 +1203,12 @@ static int run(int mode, const void* points, int layout, int dim, int64_t n,
                float threshold, int32_t* d_iter, cudaStream_t st) {
   if (!valid_features(points, layout, dim, n, width, K)) return SPLIT_ERR_INVALID;
   const int unit_range = (layout & SPLIT_FEATURES_UNIT_RANGE) ? 1 : 0;
-  layout &= ~SPLIT_FEATURES_UNIT_RANGE;
+  const int ref_shift = (layout & SPLIT_KMEANS_REFERENCE_SHIFT) ? 1 : 0;
+  layout &= ~(SPLIT_FEATURES_UNIT_RANGE | SPLIT_KMEANS_REFERENCE_SHIFT);
+  // the reference's shift is defined for its own case only: 3-D clustering
+  // with every word it reads inside the N x K distance matrix
+  if (ref_shift && (mode != kCluster || dim != 3 || K < 3 || n * (K - 2) < 3 * (int64_t)K))
+    return SPLIT_ERR_INVALID;
   const split_tune_entry te = tuned(n);
   const int units = units_of(n, width, te.kmeans_unit_rows);
   Layout l = carve(nullptr, 1);
@@ -1180,6 +1234,7 @@ static int run(int mode, const void* points, int layout, int dim, int64_t n,
   im.height = height_of(n, width);
   im.ntx = tiles_x(width);
   im.unit_rows = te.kmeans_unit_rows;
+  im.ref_shift = ref_shift;
   p.blocks_per_sm = te.kmeans_blocks_per_sm;
   p.nimages = 1;
   p.images = nullptr;
@@ -1308,20 +1363,24 @@ extern "C" int split_kmeans_propagate(const int32_t* labels, int64_t npoints,
 
 // ---------------------------------------------------------------------------
 // Allocation-free clustering.  Some callers cannot allocate device memory at
-// the point where they cluster: code running while a CUDA graph is being
-// captured or inside a latency-critical serving loop (cudaMalloc and
-// cudaFree synchronise the device), and host plugins whose device memory is
-// owned by a pool they may not touch.  This variant keeps its scratch in one
-// file-scope device array of fixed size, so a call needs no workspace.
+// the point where they cluster: a latency-critical serving loop (cudaMalloc
+// and cudaFree synchronise the device), and host plugins whose device memory
+// is owned by a pool they may not touch.  This variant keeps its scratch in
+// one file-scope device array of fixed size, so a call needs no workspace.
 //
 // Limits and sharing rules:
-//   - the array holds the state of one image (three accumulator slots,
-//     centroids, state: about 21 KB); the entry point supports images of at most
-//     kStaticTiles 64 x 64 tiles (2048: a 3840 x 2160 frame fits) and rejects
-//     larger ones with SPLIT_ERR_WORKSPACE before anything is launched;
+//   - the array holds the state of one image, whatever its size: three
+//     accumulator slots, two centroid slots and the iteration state for up
+//     to kMaxK (64) clusters of up to kMaxDim (5) dimensions, 20736 bytes.
+//     K above 64, or D other than 3 and 5, is rejected with
+//     SPLIT_ERR_INVALID before anything is queued, as the workspace entry
+//     point does;
 //   - every GPU that loads the library holds the array until the process
 //     exits; its device address is looked up once per device, on the first
-//     call made with that device current;
+//     call made with that device current.  A cudaDeviceReset of that device
+//     unloads the module and may move the array, so the cached address is
+//     stale afterwards: a process that resets a device must not call this
+//     entry point on it again;
 //   - all calls share the array: two calls whose work overlaps on the GPU
 //     (different streams, or different host threads without ordering) race
 //     and corrupt each other's results.  Order them on one stream.
@@ -1330,8 +1389,6 @@ extern "C" int split_kmeans_propagate(const int32_t* labels, int64_t npoints,
 
 namespace sg {
 namespace km {
-
-constexpr int kStaticTiles = 2048;
 
 // Size of carve(ws, 1), evaluated at compile time (every piece starts on a
 // 256-byte boundary).
@@ -1374,8 +1431,9 @@ extern "C" int split_kmeans_cluster_noalloc(const void* points, int layout, int 
                                             void* stream) {
   using namespace sg::km;
   if (!centroids || !labels || npoints <= 0 || width < 1) return SPLIT_ERR_INVALID;
-  // the units run() will use (tuned height, never below 64 rows)
-  if (units_of(npoints, width) > kStaticTiles) return SPLIT_ERR_WORKSPACE;
+  // K, D and the layout first: nothing is queued for a call run() would refuse
+  if (!valid_features(points, layout, dim, npoints, width, nclusters)) return SPLIT_ERR_INVALID;
+  // one image's state, for any image size, always fits the array
   if (carve(nullptr, 1).bytes > kStaticBytes) return SPLIT_ERR_WORKSPACE;
   void* ws = nullptr;
   SG_TRY(static_scratch(&ws));
@@ -1435,6 +1493,7 @@ int kmeans_batch_prepare(const KmBatchImage* imgs, int nimages, int layout, int 
   // kernel attributes now: the batch's launches may be captured into a graph
   SG_TRY(stage_attributes());
   const int unit_range = (layout & SPLIT_FEATURES_UNIT_RANGE) ? 1 : 0;
+  if (layout & SPLIT_KMEANS_REFERENCE_SHIFT) return SPLIT_ERR_INVALID;   // single images only
   layout &= ~SPLIT_FEATURES_UNIT_RANGE;
   const BatchCounts c = batch_counts(imgs, nimages, true);
   const int slots = nimages > 1 ? nimages : 2;

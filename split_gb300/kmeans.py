@@ -11,6 +11,9 @@ from ._util import Workspace, ensure_workspace, ptr, require_cuda, stream_handle
 
 PLANAR, FLOAT4, RGB8 = N.LAYOUT_PLANAR, N.LAYOUT_FLOAT4, N.LAYOUT_RGB8
 UNIT_RANGE = 0x100  # or into FLOAT4: colour features promised in [0, 1]
+# or into the layout of cluster(): the convergence test measures the centroid
+# shift as the reference's cluster() does (3-D, K >= 3; see the C header)
+REFERENCE_SHIFT = 0x200
 
 
 def cluster_workspace(npoints: int, nclusters: int, dim: int) -> int:
@@ -42,7 +45,7 @@ def default_width(n: int) -> int:
 def _features(points: torch.Tensor, layout: int, dim: int | None):
     """Returns (npoints, dim) for a points tensor in the given layout."""
     require_cuda(points, "points")
-    layout &= ~UNIT_RANGE
+    layout &= ~(UNIT_RANGE | REFERENCE_SHIFT)
     if layout == PLANAR:
         if points.dtype != torch.float32 or points.dim() != 2:
             raise ValueError("planar points must be a float32 (dim, npoints) tensor")

@@ -75,6 +75,19 @@ int main(int argc, char** argv) {
     dump(dir, "kmeans_labels.i32", d_km, N);
     dump(dir, "centroids.f32", d_cent, (size_t)3 * K);
 
+    // the sample's own call (main.cu:244-245): up to 100 iterations with a
+    // 1e-3 threshold, which stops where the reference's convergence test does
+    float* d_cent2 = upload(cent);
+    int32_t* d_km2 = nullptr;
+    sd::check_cuda(cudaMalloc((void**)&d_km2, sizeof(int32_t) * N), "alloc");
+    const int done_thr = sd::kmeans::cluster(sd::const_view2d<float>(d_feat, 3, N),
+                                             sd::view2d<float>(d_cent2, 3, K),
+                                             sd::view1d<int>(d_km2, N), temp, 100, 1e-3f, W);
+    dump(dir, "kmeans_thr_labels.i32", d_km2, N);
+    dump(dir, "centroids_thr.f32", d_cent2, (size_t)3 * K);
+    cudaFree(d_cent2);
+    cudaFree(d_km2);
+
     sd::ccl::connected_components(sd::const_view2d<int>(d_km, H, W), temp,
                                   sd::view1d<int>(d_seg, N), 100);
     dump(dir, "ccl.i32", d_seg, N);
@@ -93,7 +106,8 @@ int main(int argc, char** argv) {
     dump(dir, "normals.f32", d_nrm, (size_t)3 * N);
     sd::check_cuda(cudaDeviceSynchronize(), "sync");
     temp.check();
-    std::printf("{\"iterations\": %d, \"segments\": %d}\n", done, nseg);
+    std::printf("{\"iterations\": %d, \"segments\": %d, \"iterations_thr\": %d}\n", done,
+                nseg, done_thr);
     cudaFree(d_feat); cudaFree(d_cent); cudaFree(d_km); cudaFree(d_seg); cudaFree(d_tmp);
     cudaFree(d_nrm);
   } catch (const sd::error& e) {

@@ -9,6 +9,7 @@ so a generator change is caught.
     python tests/golden/make_golden.py            # reference_golden.npz
     python tests/golden/make_golden.py lab_beta   # lab_beta_golden.npz
     python tests/golden/make_golden.py ic         # ic_golden.npz
+    python tests/golden/make_golden.py threshold  # kmeans_threshold_golden.npz
 
 Known limit of the CPU build: CCCL 3.0.1's host sort orders negative int keys
 after non-negative ones, so compress_labels is only recorded on non-negative
@@ -29,6 +30,8 @@ sys.path.insert(0, ROOT)
 OUT = os.path.join(HERE, "reference_golden.npz")
 OUT_LAB = os.path.join(HERE, "lab_beta_golden.npz")
 OUT_IC = os.path.join(HERE, "ic_golden.npz")
+OUT_THR = os.path.join(HERE, "kmeans_threshold_golden.npz")
+THRESHOLDS = (1e-3, 1e-2, 0.0145)
 
 
 def sha(a: np.ndarray) -> str:
@@ -90,6 +93,27 @@ def main_ic():
     print(f"wrote {OUT_IC}")
 
 
+def main_threshold():
+    """cluster(points, c0, 100, threshold) on the 512 x 512 k-means input, for
+    a few thresholds: the reference's iteration count (cluster.cu:71), the
+    shifts it printed, its labels and centroids; and the SHA-256 of its
+    propagate_centroids render of the final labels (propagation.cu:9-24)."""
+    from oracle import ref
+    d = inputs()
+    g = {"sha_km_rgb": np.array(sha(d["km_rgb"])), "thresholds": np.array(THRESHOLDS)}
+    for i, thr in enumerate(THRESHOLDS):
+        lab, c, iters, shifts = ref.kmeans_cluster_threshold(d["km_points"], d["km_c0"], 100, thr)
+        g[f"iters_{i}"] = np.array(iters)
+        g[f"shifts_{i}"] = np.array(shifts, np.float64)
+        g[f"labels_{i}"] = lab.astype(np.uint8)
+        g[f"centroids_{i}"] = c
+        if i == 0:
+            out = ref.propagate_centroids(lab, c)
+            g["propagate_sha"] = np.array(sha(out))
+    np.savez_compressed(OUT_THR, **g)
+    print(f"wrote {OUT_THR} ({os.path.getsize(OUT_THR) / 1024:.0f} KiB)")
+
+
 def main():
     from oracle import ref
     d = inputs()
@@ -129,5 +153,7 @@ if __name__ == "__main__" and sys.argv[1:] == ["lab_beta"]:
     main_lab_beta()
 elif __name__ == "__main__" and sys.argv[1:] == ["ic"]:
     main_ic()
+elif __name__ == "__main__" and sys.argv[1:] == ["threshold"]:
+    main_threshold()
 elif __name__ == "__main__":
     main()

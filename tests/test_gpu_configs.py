@@ -1,0 +1,183 @@
+"""Parity at the sizes the path is measured on, through the C ABI.
+
+* The 3840 x 2160 frame the benchmark times (256 Voronoi cells from a
+  16-colour palette, illumination gradient, noise sigma 3; K = 16 over 5-D
+  float4 features with xy recomputed in the kernel, 20 iterations, 8-connected
+  labelling, merge < 256 px by most shared boundary, 3 x 3 erosion, L*
+  normals).  The k-means stage is checked in lockstep: twenty single-iteration
+  calls on the packed features, each one's labels against the FP32-exact
+  assignment of its input centroids (and against the FP64 assignment except
+  at near-ties), each one's centroids against the FP64 update of its labels.
+  Chained, the twenty calls must reproduce the pipeline's one-launch
+  clustering bit for bit, so the checks cover the benchmarked launch.  The
+  integer stages are then compared with the oracle's CCL -> merge -> erosion
+  of the GPU's cluster labels, bit for bit, and the normals with the FP64
+  Sobel normals of the FP64 luminance.
+* The 512 x 512 case the reference's own CPU build runs (32 cells, sigma 4,
+  K = 8 over RGB, 10 iterations, 4-connected labelling, merge < 64 px) under
+  both merge rules, with the same lockstep and the same integer checks; its
+  k-means labels are also compared with the compiled reference's recorded
+  ten-iteration labels on the identical input.
+
+Tolerances (from the path's specification): labels may differ from the FP64
+assignment only where the best-vs-second distance gap is below 1e-5 relative;
+centroids within 1e-5 relative of the FP64 update; normals within 1e-4 rad;
+labelling, merge and erosion bit-exact.
+"""
+import os
+import sys
+
+import numpy as np
+import pytest
+
+import oracle
+from split_gb300 import synth
+
+pytestmark = pytest.mark.gpu
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+NEAR_TIE = 1e-5
+CENT_REL = 1e-5
+NORMAL_RAD = 1e-4
+
+
+def _t(a, dev):
+    import torch
+    return torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+
+
+def _lockstep(cuda, pts_dev, layout, dim, width, planar, c0, iters):
+    """`iters` single-iteration k-means calls, each checked against the
+    oracle.  Returns the device labels and centroids after the last call."""
+    import torch
+    from split_gb300 import kmeans
+    n = planar.shape[1]
+    cent = _t(c0, cuda)
+    labels = torch.empty(n, dtype=torch.int32, device=cuda)
+    ws = None
+    c = c0.copy()
+    for it in range(iters):
+        ws = kmeans.cluster(pts_dev, cent, labels, ws, max_iter=1, threshold=-1.0,
+                            layout=layout, dim=dim, width=width)
+        gl = labels.cpu().numpy()
+        gc = cent.cpu().numpy()
+        # the device's distance formula in FP32: identical labels
+        exact = oracle.kmeans_assign_f32(planar, c)
+        bad = np.flatnonzero(gl != exact)
+        assert bad.size == 0, f"iteration {it}: {bad.size} labels differ from the FP32 oracle"
+        # the FP64 assignment: any difference must be a near-tie
+        lab64, d1, d2 = oracle.kmeans_assign_f64(planar, c)
+        diff = np.flatnonzero(gl != lab64)
+        if diff.size:
+            gap = (d2[diff] - d1[diff]) / np.maximum(d2[diff], 1e-300)
+            assert (gap < NEAR_TIE).all(), \
+                f"iteration {it}: {int((gap >= NEAR_TIE).sum())} labels differ beyond near-ties"
+        ref, cnt = oracle.kmeans_update_f64(gl, planar, c)
+        assert (cnt > 0).all(), f"iteration {it}: empty cluster"
+        rel = np.abs(gc - ref) / np.maximum(np.abs(ref), 1e-30)
+        assert rel.max() <= CENT_REL, f"iteration {it}: centroid rel err {rel.max():.3g}"
+        c = gc
+    ws.check("k-means lockstep")
+    return labels, cent
+
+
+def _normals_angle(got, ref):
+    got = got.astype(np.float64)
+    cross = np.linalg.norm(np.cross(got.T, ref.T), axis=1)
+    return np.arctan2(cross, (got * ref).sum(0))
+
+
+def test_4k_frame_pipeline_parity(cuda):
+    import torch
+    import bench
+    from split_gb300 import color, kmeans, pipeline
+    w, h = bench.W4K, bench.H4K
+    rgb, c0 = bench.make_image(w, h)
+    params = pipeline.Params()
+    assert (params.nclusters, params.dim, params.kmeans_iters, params.connectivity,
+            params.merge_P, params.erode_radius) == (16, 5, 20, 8, 256, 1)
+    d_rgb = _t(rgb, cuda)
+    pipe = pipeline.Pipeline(w, h, params, cuda)
+    pipe.run(d_rgb, _t(c0, cuda))
+    torch.cuda.synchronize()
+    pipe.ws.check("pipeline")
+
+    # k-means in lockstep on the packed features the pipeline clusters
+    n = w * h
+    f4 = torch.empty((n, 4), dtype=torch.float32, device=cuda)
+    color.pack_rgb8(d_rgb, f4)
+    planar = synth.features(rgb, 5)
+    assert np.array_equal(f4[:, :3].cpu().numpy(), planar[:3].T)
+    labels, cent = _lockstep(cuda, f4, kmeans.FLOAT4 | kmeans.UNIT_RANGE, 5, w, planar, c0,
+                             params.kmeans_iters)
+    # the one-launch clustering of the pipeline is the same computation
+    assert torch.equal(labels, pipe.cluster_labels)
+    assert torch.equal(cent, pipe.centroids)
+
+    # integer stages: bit-exact against the oracle given the device's labels
+    cl = pipe.cluster_labels.cpu().numpy().reshape(h, w)
+    seg = oracle.ccl(cl, 8, 0)
+    merged = oracle.merge_small(seg, 256, 0)
+    assert len(np.unique(merged)) < len(np.unique(seg))        # the merge did something
+    want = oracle.erode(merged, 1)
+    got = pipe.segment_labels.cpu().numpy()
+    assert np.array_equal(got, want), f"{int((got != want).sum())} segment labels differ"
+
+    # normals of the luminance plane
+    lum = oracle.luminance_f64(rgb).reshape(h, w).astype(np.float32)
+    ref_n = oracle.sobel_normals_f64(lum, params.depth)
+    ang = _normals_angle(pipe.normals.view(3, -1).cpu().numpy(), ref_n)
+    assert ang.max() <= NORMAL_RAD, f"normals: {ang.max():.3g} rad"
+
+
+def _golden():
+    sys.path.insert(0, os.path.join(HERE, "golden"))
+    import make_golden
+    return make_golden, np.load(os.path.join(HERE, "golden", "reference_golden.npz"))
+
+
+@pytest.mark.parametrize("policy", [0, 1])
+def test_512_reference_case_pipeline_parity(cuda, policy):
+    import torch
+    from split_gb300 import _native, color, kmeans, pipeline
+    make_golden, g = _golden()
+    d = make_golden.inputs()
+    rgb, c0 = d["km_rgb"], d["km_c0"]
+    h, w = rgb.shape[:2]
+    assert (w, h, c0.shape) == (512, 512, (3, 8))
+    params = pipeline.Params(nclusters=8, dim=3, kmeans_iters=10, connectivity=4, merge_P=64,
+                             merge_policy=(_native.MERGE_MOST_BOUNDARY, _native.MERGE_REF_CHROMA)[policy],
+                             erode_radius=0, compute_normals=False)
+    d_rgb = _t(rgb, cuda)
+    pipe = pipeline.Pipeline(w, h, params, cuda)
+    pipe.run(d_rgb, _t(c0, cuda))
+    torch.cuda.synchronize()
+    pipe.ws.check("pipeline")
+
+    n = w * h
+    f4 = torch.empty((n, 4), dtype=torch.float32, device=cuda)
+    color.pack_rgb8(d_rgb, f4)
+    planar = d["km_points"]
+    labels, cent = _lockstep(cuda, f4, kmeans.FLOAT4 | kmeans.UNIT_RANGE, 3, w, planar, c0,
+                             params.kmeans_iters)
+    assert torch.equal(labels, pipe.cluster_labels)
+    assert torch.equal(cent, pipe.centroids)
+
+    # against the compiled reference's own 10 iterations on this input: its
+    # FP32 sums drift from FP64 (about 4e-4 relative after 10 iterations), so
+    # at most a handful of near-tie pixels may end on another label
+    gl = pipe.cluster_labels.cpu().numpy()
+    mism = int((gl != g["km_cluster10_labels"]).sum())
+    assert mism <= n // 10000, f"{mism} labels differ from the reference's"
+
+    cl = gl.reshape(h, w)
+    seg = oracle.ccl(cl, 4, 0)
+    chroma = oracle.rgb_to_ic_f32(rgb)[1:] if policy == 1 else None
+    want = oracle.merge_small(seg, 64, policy, chroma)
+    got = pipe.segment_labels.cpu().numpy()
+    assert np.array_equal(got, want), f"{int((got != want).sum())} segment labels differ"
+    if mism == 0:
+        # the same cluster labels as the reference: the same partition as its
+        # 4-connected max-index labelling
+        assert np.array_equal(oracle.canonical(oracle.ccl(cl, 4, 1)),
+                              oracle.canonical(g["ccl_km"]))

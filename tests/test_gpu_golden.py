@@ -156,3 +156,75 @@ def test_rgb_to_ic(cuda):
     color.rgb_to_ic(torch.from_numpy(big).to(cuda), ic2)
     ref = oracle.rgb_to_ic_f32(big)
     assert np.array_equal(ic2.cpu().numpy().view(np.uint32), ref.view(np.uint32))
+
+
+THR = np.load(os.path.join(HERE, "golden", "kmeans_threshold_golden.npz"))
+
+
+@pytest.mark.parametrize("i", range(len(THR["thresholds"])))
+def test_cluster_threshold_stops_where_the_reference_stops(cuda, inp, i):
+    """cluster(..., 100, threshold) with the reference's shift rule
+    (SPLIT_KMEANS_REFERENCE_SHIFT): the device's convergence test stops at
+    the compiled reference's iteration, and the result equals the oracle's
+    run of the same rule (FP32-exact assignments, FP64 updates)."""
+    import torch
+    from split_gb300 import kmeans
+    pts, c0 = inp["km_points"], inp["km_c0"]
+    thr = float(THR["thresholds"][i])
+    cent = _t(c0, cuda)
+    lab = torch.empty(pts.shape[1], dtype=torch.int32, device=cuda)
+    its = torch.full((1,), -1, dtype=torch.int32, device=cuda)
+    ws = kmeans.cluster(_t(pts, cuda), cent, lab, None, max_iter=100, threshold=thr,
+                        layout=kmeans.PLANAR | kmeans.REFERENCE_SHIFT, width=512,
+                        iterations_out=its)
+    torch.cuda.synchronize()
+    ws.check("kmeans")
+    assert int(its.item()) == int(THR[f"iters_{i}"])
+    olab, oc, oit, _ = oracle.kmeans_cluster_threshold(pts, c0, 100, thr)
+    assert oit == int(its.item())
+    gl = lab.cpu().numpy()
+    assert (gl != olab).sum() <= 8            # near-ties after ulp-level centroid differences
+    rel = np.abs(cent.cpu().numpy() - oc) / np.maximum(np.abs(oc), 1e-30)
+    assert rel.max() <= 1e-4
+    # the same rule written by the reference itself: within its FP32 drift
+    assert (gl != THR[f"labels_{i}"]).mean() <= 2e-3
+
+
+def test_cluster_threshold_rule_limits(cuda, inp):
+    """The reference's shift is defined for 3-D features and K >= 3 only."""
+    import torch
+    from split_gb300 import _native, kmeans
+    pts = _t(inp["km_points"], cuda)
+    lab = torch.empty(pts.shape[1], dtype=torch.int32, device=cuda)
+    for k in (1, 2):
+        cent = _t(inp["km_c0"][:, :k], cuda)
+        with pytest.raises(_native.SplitError):
+            kmeans.cluster(pts, cent, lab, None, max_iter=5, threshold=1e-3,
+                           layout=kmeans.PLANAR | kmeans.REFERENCE_SHIFT, width=512)
+    f5 = _t(np.concatenate([inp["km_points"], inp["km_points"][:2]]), cuda)
+    with pytest.raises(_native.SplitError):
+        kmeans.cluster(f5, _t(np.zeros((5, 8), np.float32), cuda), lab, None, max_iter=5,
+                       threshold=1e-3, layout=kmeans.PLANAR | kmeans.REFERENCE_SHIFT, width=512)
+
+
+def test_propagate_centroids(cuda):
+    """propagate_centroids (propagation.cu:9-24) on the reference's final
+    labels and centroids: bit-exact against the oracle's gather and against
+    the SHA-256 of the reference's own render."""
+    import torch
+    from split_gb300 import kmeans
+    labels = THR["labels_0"].astype(np.int32)
+    cent = THR["centroids_0"]
+    out = torch.empty((3, labels.size), dtype=torch.float32, device=cuda)
+    kmeans.propagate_centroids(_t(labels, cuda), _t(cent, cuda), out)
+    got = out.cpu().numpy()
+    assert np.array_equal(got, oracle.propagate_centroids(labels, cent))
+    assert make_golden.sha(got) == str(THR["propagate_sha"])
+    # labels outside [0, K) render as zeros
+    bad = labels.copy()
+    bad[::97] = -1
+    bad[1::101] = cent.shape[1]
+    kmeans.propagate_centroids(_t(bad, cuda), _t(cent, cuda), out)
+    want = oracle.propagate_centroids(np.clip(bad, 0, cent.shape[1] - 1), cent)
+    want[:, (bad < 0) | (bad >= cent.shape[1])] = 0.0
+    assert np.array_equal(out.cpu().numpy(), want)

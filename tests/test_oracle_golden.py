@@ -133,3 +133,43 @@ def test_ic_restatement_against_reference():
     # FP32 rounding of (3 / 255) * (1 / 3) and its reciprocal
     black = oracle.rgb_to_ic_f32(np.zeros((1, 3), np.uint8))
     np.testing.assert_allclose(black[:, 0], [1 / 255, 1.0, 1.0], rtol=1e-6)
+
+
+THR = np.load(os.path.join(HERE, "golden", "kmeans_threshold_golden.npz"))
+
+
+def test_threshold_golden_input_unchanged(inp):
+    assert make_golden.sha(inp["km_rgb"]) == str(THR["sha_km_rgb"])
+
+
+@pytest.mark.parametrize("i", range(len(THR["thresholds"])))
+def test_kmeans_threshold_stops_where_the_reference_stops(inp, i):
+    """cluster(points, c0, 100, threshold): the oracle's restatement of the
+    reference's shift (which reads overwritten workspace words) stops at the
+    reference's iteration; its shifts follow the printed ones within the FP32
+    drift of the reference's centroid sums; the labels agree except on a few
+    tenths of a percent of pixels while the clustering is still moving."""
+    thr = float(THR["thresholds"][i])
+    lab, c, iters, shifts = oracle.kmeans_cluster_threshold(inp["km_points"], inp["km_c0"], 100,
+                                                            thr)
+    assert iters == int(THR[f"iters_{i}"])
+    ref_shifts = THR[f"shifts_{i}"]
+    assert len(shifts) == len(ref_shifts)
+    assert np.abs(np.array(shifts) - ref_shifts).max() <= 1e-3
+    assert (lab != THR[f"labels_{i}"]).mean() <= 2e-3
+    assert np.abs(c - THR[f"centroids_{i}"]).max() <= 5e-3
+
+
+def test_kmeans_threshold_intended_rule_differs():
+    """The L2 change of the centroid matrix stops elsewhere on this input:
+    the reference's rule is what pins its iteration counts."""
+    d = make_golden.inputs()
+    counts = [oracle.kmeans_cluster_threshold(d["km_points"], d["km_c0"], 100, float(t),
+                                              reference_shift_rule=False)[2]
+              for t in THR["thresholds"]]
+    assert counts != [int(THR[f"iters_{i}"]) for i in range(len(counts))]
+
+
+def test_propagate_centroids():
+    out = oracle.propagate_centroids(THR["labels_0"].astype(np.int32), THR["centroids_0"])
+    assert make_golden.sha(out) == str(THR["propagate_sha"])

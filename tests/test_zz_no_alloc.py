@@ -1,13 +1,14 @@
 """The allocation-free k-means entry point (split_kmeans_cluster_noalloc).
 
 It exists for callers that cannot allocate device memory where they cluster
-(graph capture, a latency-critical serving loop, plugins whose device memory
-is owned by someone else); its scratch is a fixed device array inside the
-library instead of a caller workspace.  These checks call it through the C ABI
-and compare it with the workspace entry point (split_kmeans_cluster) on the
-same inputs, twice in a row, since the second call reuses the array the first
-call left behind.  The file is collected last so that a failure here comes
-after every other test has run; it also passes on its own in a fresh process.
+(a latency-critical serving loop, where cudaMalloc would synchronise the
+device; plugins whose device memory is owned by someone else); its scratch is
+a fixed device array inside the library instead of a caller workspace.  These
+checks call it through the C ABI and compare it with the workspace entry point
+(split_kmeans_cluster) on the same inputs, twice in a row, since the second
+call reuses the array the first call left behind.  The file is collected last
+so that a failure here comes after every other test has run; it also passes on
+its own in a fresh process.
 """
 import ctypes as C
 
@@ -76,15 +77,35 @@ def test_noalloc_matches_workspace_entry_point(layout, dim):
         assert torch.equal(cent, ref_c)
 
 
-def test_noalloc_rejects_images_beyond_its_capacity():
+def test_noalloc_any_image_size():
+    """The array holds per-image state only, so an image larger than a 4K
+    frame (4096 x 2304, 2304 tiles of 64 x 64) clusters like the workspace
+    entry point does, bit for bit."""
+    torch = pytest.importorskip("torch")
+    dev = torch.device("cuda", 0)
+    w, h = 4096, 2304
+    rgb = synth.voronoi_rgb8(33, w, h, 128, npalette=16, illum_gradient=True, sigma=3.0)
+    c0 = torch.from_numpy(synth.pick_centroids(33, rgb, 16, 5)).to(dev)
+    pts = torch.from_numpy(rgb.reshape(-1, 3).copy()).to(dev)
+    n = w * h
+    ref_lab, ref_c = _workspace_run(torch, pts, _native.LAYOUT_RGB8, 5, n, w, c0, (n,), 6)
+    lab, cent = _noalloc_run(torch, pts, _native.LAYOUT_RGB8, 5, n, w, c0, (n,), 6)
+    assert torch.equal(lab, ref_lab)
+    assert torch.equal(cent, ref_c)
+
+
+def test_noalloc_rejects_what_its_array_cannot_hold():
+    """More than 64 clusters (or a dimension other than 3 and 5) would need
+    more state than the array holds: refused before any work is queued."""
     torch = pytest.importorskip("torch")
     lib = _native.load()
     dev = torch.device("cuda", 0)
-    # 4096 x 4096 needs 4096 tiles of 64 x 64: more than the 2048 it holds
-    w = h = 4096
-    pts = torch.zeros((1, 3), dtype=torch.uint8, device=dev)
-    cent = torch.zeros((3, 4), dtype=torch.float32, device=dev)
-    lab = torch.zeros(1, dtype=torch.int32, device=dev)
-    st = lib.split_kmeans_cluster_noalloc(_ptr(pts), _native.LAYOUT_RGB8, 3, w * h, w, 0.1,
-                                          _ptr(cent), 4, _ptr(lab), 1, -1.0, None, None, None)
-    assert st == _native.ERR_WORKSPACE
+    w = h = 64
+    pts = torch.zeros((w * h, 3), dtype=torch.uint8, device=dev)
+    lab = torch.zeros(w * h, dtype=torch.int32, device=dev)
+    for k, dim in ((65, 3), (8, 4)):
+        cent = torch.zeros((dim, k), dtype=torch.float32, device=dev)
+        st = lib.split_kmeans_cluster_noalloc(_ptr(pts), _native.LAYOUT_RGB8, dim, w * h, w,
+                                              0.1, _ptr(cent), k, _ptr(lab), 1, -1.0, None,
+                                              None, None)
+        assert st == _native.ERR_INVALID, (k, dim)
