@@ -42,7 +42,7 @@ PROFILE_TRAFFIC = os.path.join(ROOT, "profiles", "kmeans_cluster_4k.txt")
 
 
 def make_image(width, height, seed=SEED):
-    from split_gb300 import synth
+    import split_synth as synth
     rgb = synth.voronoi_rgb8(seed, width, height, 256, npalette=16, illum_gradient=True,
                              sigma=3.0)
     c0 = synth.pick_centroids(seed, rgb, 16, 5, 0.1)
@@ -127,14 +127,40 @@ class ClockSampler:
 
 
 # ------------------------------------------------------------------------ CPU
-def cpu_pipeline_oracle(rgb, c0, iters):
+WORKLOAD = ("3840x2160 RGB8 frame per step (256 Voronoi cells, 16-colour palette, "
+            "illumination gradient x0.6..x1.0, noise sigma 3): K=16 k-means x20, connected "
+            "components, merge of segments <256 px, 3x3 erosion, Sobel normals of the "
+            "luminance plane")
+PATH_NATIVE = "5-D float32 features (RGB / 255, 0.1 x, 0.1 y), 8-connected labelling, " \
+              "merge into the neighbour sharing most boundary"
+PATH_REFERENCE = ("the reference's own entry points on the same frame: 3-D RGB features, "
+                  "4-connected labelling + compress_labels, nearest-chroma merge (chroma = "
+                  "r, g rows), erode n=1, sobel_normals of its rgb_to_lab L* plane; it "
+                  "implements no 5-D features, 8-connectivity or boundary merge")
+
+
+def cpu_inputs(width, height, seed):
+    """Everything the CPU runs read, made before any timing starts: the RGB8
+    frame, the reference's 3-D features (and the copy clamped to >= 1/255 that
+    its colour conversion reads, main.cu:170-173), its initial centroids, and
+    the 5-D features and centroids of the oracle restatement."""
+    import numpy as np
+    import split_synth as synth
+    rgb = synth.voronoi_rgb8(seed, width, height, 256, npalette=16, illum_gradient=True,
+                             sigma=3.0)
+    f3 = synth.features(rgb, 3)
+    return {"rgb": rgb, "width": width, "height": height, "f3": f3,
+            "f3_clamped": np.maximum(f3, np.float32(1.0 / 255.0)),
+            "c3": synth.pick_centroids(seed, rgb, 16, 3),
+            "f5": synth.features(rgb, 5), "c5": synth.pick_centroids(seed, rgb, 16, 5, 0.1)}
+
+
+def cpu_pipeline_oracle(d, iters):
     """The path on the host with the oracle restatement (single thread)."""
     import numpy as np
     import oracle
-    from split_gb300 import synth
-    h, w = rgb.shape[:2]
-    feats = synth.features(rgb, 5)
-    c = c0.copy()
+    h, w = d["height"], d["width"]
+    feats, c = d["f5"], d["c5"].copy()
     lab = None
     for _ in range(iters):
         lab = oracle.kmeans_assign_f32(feats, c)
@@ -143,31 +169,25 @@ def cpu_pipeline_oracle(rgb, c0, iters):
     seg = oracle.ccl(lab.reshape(h, w), 8, 0)
     seg = oracle.merge_small(seg, 256, 0)
     oracle.erode(seg, 1)
-    lum = oracle.luminance_f64(rgb).reshape(h, w).astype(np.float32)
+    lum = oracle.luminance_f64(d["rgb"]).reshape(h, w).astype(np.float32)
     oracle.sobel_normals_f64(lum, 1.0)
 
 
-def cpu_pipeline_reference(rgb, iters):
+def cpu_pipeline_reference(d, iters):
     """The path through the reference's own code built for the CPU (Thrust
-    OMP, all host threads).  The reference implements 3-D features,
-    4-connectivity and the nearest-chroma merge only, so it runs the recipe
-    that way: RGB features, K=16, `iters` iterations, 4-CCL, compression,
-    chroma merge < 256 px (chroma = r, g), erosion n=1, and normals of its
-    own L* plane."""
+    OMP, all host threads): only the reference's calls run here, on inputs
+    prepared by cpu_inputs()."""
     import numpy as np
     from oracle import ref
-    from split_gb300 import synth
-    h, w = rgb.shape[:2]
-    feats = synth.features(rgb, 3)
-    c0 = synth.pick_centroids(SEED, rgb, 16, 3)
+    h, w = d["height"], d["width"]
     with ref.quiet():
-        lab, _ = ref.kmeans_cluster(feats, c0, iters)
+        lab, _ = ref.kmeans_cluster(d["f3"], d["c3"], iters)
         seg = ref.connected_components(lab.reshape(h, w))
         seg, _ = ref.compress_labels(seg)
-        seg = ref.merge_small_segments(feats[:2], seg, 256)
+        seg = ref.merge_small_segments(d["f3"][:2], seg, 256)
         ref.erode(seg, 1)
-        lum = ref.rgb_to_lab(np.maximum(feats, np.float32(1.0 / 255.0)))[0].reshape(h, w) / 100.0
-        ref.sobel_normals(lum.astype(np.float32), 1.0)
+        lum = ref.rgb_to_lab(d["f3_clamped"])[0].reshape(h, w) / np.float32(100.0)
+        ref.sobel_normals(lum, 1.0)
 
 
 def reference_available():
@@ -185,50 +205,63 @@ def cpu_threads():
         return os.cpu_count()
 
 
-def cpu_run(side, seed, iters=20):
-    """(seconds, kind, cores) of one bounded CPU sample."""
-    rgb, c0 = make_image(side, side, seed)
+def cpu_run(d, iters=20):
+    """(seconds, kind, cores) of one pass over the prepared inputs `d`: the
+    reference's own code when it is built, else the oracle restatement."""
     if reference_available():
         t0 = time.perf_counter()
-        cpu_pipeline_reference(rgb, iters)
+        cpu_pipeline_reference(d, iters)
         return time.perf_counter() - t0, "reference", cpu_threads()
     t0 = time.perf_counter()
-    cpu_pipeline_oracle(rgb, c0, iters)
+    cpu_pipeline_oracle(d, iters)
     return time.perf_counter() - t0, "port", 1
 
 
-def cpu_baseline_sample(side=512, iters=20):
-    dt, kind, cores = cpu_run(side, SEED + 1, iters)
-    what = ("the reference's own code (Thrust OMP build): K=16 RGB k-means x20, 4-CCL, "
-            "compression, chroma merge<256, erosion, normals" if kind == "reference" else
-            "the oracle restatement (K=16 5-D k-means x20, 8-CCL, merge<256, erosion, normals)")
-    return {"value": round(side * side / dt / 1e6, 4), "unit": "Mpix/s", "cores": cores,
-            "kind": kind, "sample": f"one {side}x{side} image of the 4K recipe through {what}, "
-                                    f"{dt:.2f} s"}
+def cpu_baseline_sample(width=W4K, height=H4K, iters=20):
+    """One frame of the benchmark's workload on the host cores (about 10-30 s
+    for the reference's code on the full frame)."""
+    d = cpu_inputs(width, height, SEED)
+    dt, kind, cores = cpu_run(d, iters)
+    what = PATH_REFERENCE if kind == "reference" else \
+        "the oracle restatement of the same path (one thread)"
+    return {"value": round(width * height / dt / 1e6, 4), "unit": "Mpix/s", "cores": cores,
+            "kind": kind, "sample": f"one {width}x{height} frame of the benchmark workload "
+                                    f"through {what}, {dt:.2f} s"}
 
 
 def run_reference(args, rank):
+    """The reference arm: its own CPU implementation of the path, timed on the
+    benchmark's frame.  Warm-up steps run a 512 x 512 crop of the recipe (they
+    start the thread pool and fault in the code); every timed step is the
+    full frame, its inputs prepared outside the timing."""
     if rank != 0:
         return
-    vals = []
+    W, H = args.width, args.height
+    warm = cpu_inputs(min(W, 512), min(H, 512), SEED)
     kind, cores = "port", 1
-    for i in range(args.warmup + args.steps):
-        dt, kind, cores = cpu_run(args.ref_side, SEED + 7 + i)
-        if i >= args.warmup:
-            vals.append(args.ref_side * args.ref_side / dt / 1e6)
-    v = statistics.median(vals)
-    sample = f"{args.ref_side}x{args.ref_side} image of the 4K recipe per step"
+    for _ in range(args.warmup):
+        _, kind, cores = cpu_run(warm)
+    d = cpu_inputs(W, H, SEED)
+    times = []
+    for _ in range(args.steps):
+        dt, kind, cores = cpu_run(d)
+        times.append(dt)
+    ms = 1e3 * sum(times) / len(times)
+    v = W * H / (ms * 1e-3) / 1e6
+    sample = f"the full {W}x{H} frame every timed step ({len(times)} steps, " \
+             f"{min(times):.2f}-{max(times):.2f} s each)"
     line = {
         "impl": "reference", "metric": "Mpix/s segment pipeline (4K)", "value": round(v, 4),
         "unit": "Mpix/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": round(args.ref_side ** 2 / v / 1e3, 3), "higher_is_better": True,
+        "ms_per_step": round(ms, 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": "4K recipe on a bounded CPU sample; the reference runs 3-D "
-                               "RGB k-means (K=16, 20 iterations), 4-CCL and its chroma merge "
-                               "(it implements no 5-D features, 8-CCL or most-boundary merge), "
-                               "erosion n=1, normals of its L* plane",
-                   "sample": sample, "host": "Thrust OMP build of the reference" if
-                   kind == "reference" else "oracle restatement (reference not built)"},
+        "config": {"workload": WORKLOAD.replace(f"{W4K}x{H4K}", f"{W}x{H}"),
+                   "path": PATH_REFERENCE if kind == "reference" else
+                   "oracle restatement of " + PATH_NATIVE,
+                   "host": "Thrust OMP build of the reference, all host threads" if
+                   kind == "reference" else "oracle restatement, one thread (reference "
+                                            "not built)",
+                   "warmup": "512x512 crop of the recipe per warm-up step"},
         "cpu_baseline": {"value": round(v, 4), "unit": "Mpix/s", "cores": cores, "kind": kind,
                          "sample": sample},
         "e2e": {"value": round(v, 4), "unit": "Mpix/s", "h2d_bytes_per_step": 0,
@@ -248,7 +281,7 @@ def batch_shapes(n, seed):
 
 
 def batch_images(shapes, seed):
-    from split_gb300 import synth
+    import split_synth as synth
     imgs, cents = [], []
     for i, (w, h, k, _) in enumerate(shapes):
         rgb = synth.voronoi_rgb8(seed + i, w, h, 32, sigma=4.0)
@@ -470,7 +503,8 @@ def run_stress(dev, side=8192, steps=10, seed=2024):
     The oracle's union-find on one host thread is timed once beside it."""
     import numpy as np
     import torch
-    from split_gb300 import ccl, synth
+    import split_synth as synth
+    from split_gb300 import ccl
     lab = synth.maze_labels(seed, side, side)
     d_lab = torch.from_numpy(lab).to(dev)
     out = torch.empty_like(d_lab)
@@ -588,8 +622,6 @@ def main():
     ap.add_argument("--width", type=int, default=W4K)
     ap.add_argument("--height", type=int, default=H4K)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--ref-side", type=int, default=512)
-    ap.add_argument("--cpu-side", type=int, default=512)
     ap.add_argument("--batch-images", type=int, default=256)
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--serve-requests", type=int, default=1024)
@@ -754,15 +786,15 @@ def main():
     if rank == 0:
         cpu = None
         if not args.no_cpu_baseline:
-            cpu = cpu_baseline_sample(args.cpu_side)
+            cpu = cpu_baseline_sample(W, H)
         line = {
             "metric": "Mpix/s segment pipeline (4K)", "value": round(value, 2),
             "unit": "Mpix/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": round(step_ms, 4), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": f"{W}x{H} single image per GPU per step: K=16 5-D float32 "
-                                   "features, 20 k-means iterations, 8-CCL, merge <256 px "
-                                   "(most boundary), 3x3 erosion, luminance normals",
+            "config": {"workload": WORKLOAD if (W, H) == (W4K, H4K) else
+                       WORKLOAD.replace(f"{W4K}x{H4K}", f"{W}x{H}"),
+                       "path": PATH_NATIVE,
                        "mode": "CUDA graph replay of the single-image launch sequence "
                                "(stages_ms and plain_sequence_ms: the same sequence launched "
                                "call by call)",

@@ -3,9 +3,11 @@
  *
  * The reference has no fixtures or datasets (its sample loads a user image,
  * samples/src/main.cu:157-158), so every workload of this library is generated
- * from a seed.  These host functions are exported by libsplit_gb300.so and are
- * also compiled into the CPU reference driver, so both sides see identical
- * bytes.  All return 0 on success, 1 on a bad argument, 2 on host OOM.
+ * from a seed.  These host functions are exported by libsplit_synth.so
+ * (split_synth/synth.c), a library of their own: the GPU path and the timed
+ * CPU run of the reference's code see identical bytes, and a process that only
+ * generates inputs loads nothing of the segmentation library.  All return 0 on
+ * success, 1 on a bad argument, 2 on host OOM.
  */
 #ifndef SPLIT_SYNTH_H
 #define SPLIT_SYNTH_H

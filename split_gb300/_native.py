@@ -1,5 +1,4 @@
-"""ctypes bindings of libsplit_gb300.so (the C ABI declared in include/split_gb300.h
-and include/split_synth.h).
+"""ctypes bindings of libsplit_gb300.so (the C ABI declared in include/split_gb300.h).
 
 The library is built in-tree by ``split_gb300.build``.  Loading fails loudly when
 it is missing: there is no fallback implementation of any entry point.
@@ -76,10 +75,6 @@ _SIGS = {
     "split_batch_centroid_offset": (_i64, [_vp, _i32]),
     "split_batch_bind": (_i32, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _sz, _vp]),
     "split_batch_run": (_i32, [_vp, _vp]),
-    "split_synth_voronoi_rgb8": (_i32, [_u64, _i32, _i32, _i32, _i32, _i32, C.c_double, _vp]),
-    "split_synth_pick_centroids": (_i32, [_u64, _vp, _i32, _i32, _i32, _i32, _f32, _vp]),
-    "split_synth_feature_u8": (_f32, [C.c_uint8]),
-    "split_synth_maze_labels": (_i32, [_u64, _i32, _i32, _vp]),
 }
 
 

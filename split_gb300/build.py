@@ -1,10 +1,10 @@
 """In-tree build of the native library (and the CPU oracle used by the tests).
 
 libsplit_gb300.so: every CUDA translation unit under csrc/ compiled for
-sm_103a only (``-gencode arch=compute_103a,code=sm_103a``), plus the host-side
-synthetic-input generators, linked with the static CUDA runtime.  Objects are
-compiled in parallel; a unit is rebuilt only when it or a header is newer
-than its object.
+sm_103a only (``-gencode arch=compute_103a,code=sm_103a``), linked with the
+static CUDA runtime.  Objects are compiled in parallel; a unit is rebuilt only
+when it or a header is newer than its object.  (The seeded input generators
+are a separate library, split_synth.)
 """
 from __future__ import annotations
 
@@ -29,7 +29,6 @@ ORACLE_LIB = os.path.join(ORACLE_BUILD, "liboracle.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
               "--expt-relaxed-constexpr", "-Xptxas", "-O3"]
-CC_FLAGS = ["-O2", "-fPIC", "-std=c11", "-ffp-contract=off", "-fopenmp"]
 
 
 def _nvcc() -> str:
@@ -73,19 +72,13 @@ def build_library(verbose: bool = False, jobs: int | None = None) -> str:
         objs.append(obj)
         if _stale(obj, [src] + headers):
             steps.append([nvcc, *ARCH, *NVCC_FLAGS, "-c", "-o", obj, src])
-    csrc = os.path.join(CSRC, "synth.c")
-    cobj = os.path.join(BUILD, "synth.o")
-    objs.append(cobj)
-    if _stale(cobj, [csrc] + headers):
-        steps.append(["gcc", *CC_FLAGS, "-c", "-o", cobj, csrc])
     if steps:
         with cf.ThreadPoolExecutor(max_workers=jobs or min(8, os.cpu_count() or 4)) as ex:
             list(ex.map(_run, steps))
     # the stamp lives in the per-machine build directory, so a library built
     # on another architecture is always relinked here
     if steps or _stale(STAMP, objs) or not os.path.exists(LIB):
-        _run([nvcc, *ARCH, "-shared", "-cudart", "static", "-o", LIB, *objs,
-              "-Xcompiler", "-fopenmp", "-lm"])
+        _run([nvcc, *ARCH, "-shared", "-cudart", "static", "-o", LIB, *objs, "-lm"])
         with open(STAMP, "w") as f:
             f.write(platform.machine() + "\n")
     if verbose:
@@ -97,8 +90,8 @@ def build_oracle(verbose: bool = False) -> str:
     os.makedirs(ORACLE_BUILD, exist_ok=True)
     src = os.path.join(ORACLE_DIR, "oracle.c")
     if _stale(ORACLE_LIB, [src]):
-        _run(["gcc", "-O2", "-fPIC", "-shared", "-std=c11", "-ffp-contract=off", "-o",
-              ORACLE_LIB, src, "-lm"])
+        _run(["gcc", "-O2", "-fPIC", "-shared", "-std=c11", "-ffp-contract=off", "-fopenmp",
+              "-o", ORACLE_LIB, src, "-lm"])
     if verbose:
         print(f"built {ORACLE_LIB}")
     return ORACLE_LIB

@@ -20,7 +20,7 @@
 #include <stdlib.h>
 #include <string.h>
 
-#include "../../include/split_synth.h"
+#include "../include/split_synth.h"
 
 typedef struct {
   uint64_t state;

@@ -7,18 +7,16 @@ import re
 import numpy as np
 import pytest
 
-from split_gb300 import _native, synth
+import split_synth as synth
+from split_gb300 import _native
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
-def declared_functions():
-    names = []
-    for h in ("split_gb300.h", "split_synth.h"):
-        text = open(os.path.join(ROOT, "include", h)).read()
-        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
-        names += re.findall(r"\b(split_[a-z0-9_]+)\s*\(", text)
-    return sorted(set(names))
+def declared_functions(header="split_gb300.h"):
+    text = open(os.path.join(ROOT, "include", header)).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(split_[a-z0-9_]+)\s*\(", text)))
 
 
 def test_every_declared_symbol_is_exported():
@@ -28,6 +26,12 @@ def test_every_declared_symbol_is_exported():
     for n in names:
         assert hasattr(lib, n), n
         assert n in _native.exported_symbols(), f"{n} has no ctypes signature"
+    # the input generators live in their own library, not in the product's
+    slib = synth.load()
+    for n in declared_functions("split_synth.h"):
+        assert hasattr(slib, n), n
+        assert n in synth.exported_symbols(), n
+        assert not hasattr(lib, n), f"{n} is linked into libsplit_gb300.so"
 
 
 def test_version_and_status_strings():

@@ -10,7 +10,7 @@ import numpy as np
 import pytest
 
 import oracle
-from split_gb300 import synth
+import split_synth as synth
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 SRC = os.path.join(ROOT, "tests", "cpp", "sample_pipeline.cpp")
@@ -24,8 +24,10 @@ def _compile(out_dir):
     lib = build.build_library()
     exe = os.path.join(str(out_dir), "sample_pipeline")
     libdir = os.path.dirname(lib)
+    sdir = os.path.dirname(synth.build())
     cmd = [nvcc, "-std=c++17", "-O2", "-x", "c++", SRC, "-I", os.path.join(ROOT, "include"),
-           "-L", libdir, "-lsplit_gb300", "-Xlinker", f"-rpath={libdir}", "-o", exe]
+           "-L", libdir, "-lsplit_gb300", "-Xlinker", f"-rpath={libdir}",
+           "-L", sdir, "-lsplit_synth", "-Xlinker", f"-rpath={sdir}", "-o", exe]
     r = subprocess.run(cmd, capture_output=True, text=True)
     assert r.returncode == 0, r.stdout + r.stderr
     return exe
@@ -70,6 +72,18 @@ def test_cpp_sample_pipeline_matches_oracle(tmp_path, cuda):
                    threshold=-1.0, layout=0, dim=3, width=w)
     assert np.array_equal(lab.cpu().numpy(), km)
     assert np.array_equal(cd.cpu().numpy(), cen)
+    # cluster(..., 100, 1e-3) through the C++ layer uses the reference's
+    # convergence rule: the same stop as the binding with that rule, and as
+    # the oracle's restatement of it
+    its = torch.zeros(1, dtype=torch.int32, device=cuda)
+    cd2 = torch.from_numpy(c_in.copy()).to(cuda)
+    kmeans.cluster(torch.from_numpy(feats).to(cuda), cd2, lab, None, max_iter=100,
+                   threshold=1e-3, layout=kmeans.PLANAR | kmeans.REFERENCE_SHIFT, dim=3,
+                   width=w, iterations_out=its)
+    assert info["iterations_thr"] == int(its.item())
+    assert oracle.kmeans_cluster_threshold(feats, c_in, 100, 1e-3)[2] == info["iterations_thr"]
+    assert np.array_equal(_read(out, "kmeans_thr_labels.i32", np.int32, (n,)), lab.cpu().numpy())
+    assert np.array_equal(_read(out, "centroids_thr.f32", np.float32, (3, k)), cd2.cpu().numpy())
     # every stage after k-means is bit-exact given its input
     seg = _read(out, "ccl.i32", np.int32, (h, w))
     assert np.array_equal(seg, oracle.ccl(km.reshape(h, w), 4, 1))
