@@ -307,6 +307,36 @@ def run_batched(dev, nimages, steps, seed=SEED + 1000):
     b.run()
     torch.cuda.synchronize()
     batch_launches = pipeline.launch_count() - l0
+    # per-stage split of the batch: the same launch sequence with events
+    # around every stage (launched call by call, L2 flushed before each run)
+    from split_gb300 import _native as N
+    nst = len(N.PIPELINE_STAGES)
+    reps = max(3, steps)
+    sev = [[torch.cuda.Event(enable_timing=True) for _ in range(2 * nst)] for _ in range(reps)]
+    for row in sev:
+        for e in row:
+            e.record()
+    torch.cuda.synchronize()
+    for r in range(reps):
+        b.centroids.copy_(c0_all)
+        flush.zero_()
+        b.run(stage_events=sev[r])
+    torch.cuda.synchronize()
+    stage_ms = {name: statistics.median(sev[r][2 * i].elapsed_time(sev[r][2 * i + 1])
+                                        for r in range(reps))
+                for i, name in enumerate(N.PIPELINE_STAGES)}
+    peak, peak_kind = peaks()
+    km_bytes = sum(w * h * (16 * it + 4) for w, h, _, it in shapes)
+    bpp = {"pack": 31 * total_px, "kmeans": km_bytes, "ccl": 8 * total_px,
+           "merge": 4 * total_px, "erode": 8 * total_px}
+    stages = {}
+    for name, ms in stage_ms.items():
+        e = {"ms": round(ms, 4)}
+        if name in bpp and ms > 0:
+            gbs = bpp[name] / (ms * 1e-3) / 1e9
+            e.update(gb_s=round(gbs, 1), frac=round(gbs / peak, 4),
+                     algorithmic_bytes=int(bpp[name]))
+        stages[name] = e
     b.capture()
     torch.cuda.synchronize()
     t_batch = []
@@ -373,6 +403,12 @@ def run_batched(dev, nimages, steps, seed=SEED + 1000):
             "plain_mpix_s": round(total_px / (tp * 1e-3) / 1e6, 1),
             "batched_ms": round(tb, 3), "plain_ms": round(tp, 3),
             "speedup": round(tp / tb, 2), "identical_labels": bool(same),
+            "stages": stages,
+            "stages_note": "CUDA-event time of each stage of the batch launched call by call "
+                           "(median of runs, L2 flushed before each); frac = algorithmic bytes "
+                           "(features + normals 31 B/px, k-means 16 B/px per iteration + 4, "
+                           f"labelling 8, merge pair pass 4, erosion 8) / time / {peak_kind} "
+                           "HBM peak",
             "launches_per_run": {"batched": int(batch_launches), "plain": int(plain_launches)}}
 
 
@@ -544,55 +580,71 @@ def run_stress(dev, side=8192, steps=10, seed=2024):
     return res
 
 
-def run_serving(dev, nimages, nrequests, seed=SEED + 2000):
-    """Continuous batching under open-loop Poisson arrivals (40 GB admission
-    budget, batches of at most 64 Mpix, two batches in flight).  A closed
-    run of every request at once gives the saturation throughput; open-loop
-    runs at 50% and 80% of it give p50/p99 latency.  Request images sit in
-    pinned host memory, as a receive path would leave them."""
+def serving_shapes(n, seed):
+    """Serving configuration: sides log-uniform in [256, 4096] per axis
+    (random aspect), K from {8, 16, 32}, 20 k-means iterations."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    lo, hi = np.log(256.0), np.log(4096.0)
+    return [(int(round(np.exp(rng.uniform(lo, hi)))), int(round(np.exp(rng.uniform(lo, hi)))),
+             int(rng.choice([8, 16, 32])), 20) for _ in range(n)]
+
+
+def run_serving(dev, rates, seconds, pool=48, seed=SEED + 2000):
+    """Continuous batching through the C++ server (split_server_*) under
+    open-loop Poisson arrivals at each offered rate for `seconds` (the
+    serving configuration asks for 60 s per rate; the bench uses a shorter,
+    stated duration so that the run stays within minutes), 40 GB admission
+    budget, batches of at most 64 Mpix, two batches in flight.  Requests cycle
+    through a pool of distinct images held in pinned host memory, as a
+    receive path would leave them.  A closed run of every pool image at once
+    gives the saturation throughput."""
     import torch
     from split_gb300 import pipeline
     from split_gb300.serve import Request, Server, poisson_arrivals
-    shapes = batch_shapes(nimages, seed)
+    shapes = serving_shapes(pool, seed)
     imgs, cents = batch_images(shapes, seed)
     h_rgb = [torch.from_numpy(im).pin_memory() for im in imgs]
     h_c0 = [torch.from_numpy(c).pin_memory() for c in cents]
     params = pipeline.Params()
+    mean_px = sum(w * h for w, h, _, _ in shapes) / pool
 
     def requests(arrivals):
         out = []
         for j, t in enumerate(arrivals):
-            i = j % nimages
+            i = j % pool
             w, h, k, iters = shapes[i]
             out.append(Request(j, h_rgb[i], k, iters, h_c0[i], float(t)))
         return out
 
-    srv = Server(params, device=dev, keep_results=False, reserve_pixels=64 << 20)
-    srv.serve(requests([0.0] * min(64, nrequests)), realtime=False)   # warm-up
-    srv.completed.clear()
-    nb0 = len(srv.batch_sizes)
+    srv = Server(params, budget_bytes=40 << 30, device=dev, keep_results=False,
+                 reserve_pixels=64 << 20)
+    srv.serve(requests([0.0] * pool), realtime=False)   # warm-up
+    nsat = 4 * pool
     t = time.perf_counter()
-    done = srv.serve(requests([0.0] * nrequests), realtime=False)
+    done = srv.serve(requests([0.0] * nsat), realtime=False)
     wall = time.perf_counter() - t
     sat = Server.report(done, wall)
-    sat["mean_batch"] = round(nrequests / max(1, len(srv.batch_sizes) - nb0), 2)
-    sat_rps = len(done) / wall
-    out = {"requests": nrequests, "distinct_images": nimages,
-           "mean_mpix_per_request": round(sum(s[0] * s[1] for s in shapes) / nimages / 1e6, 3),
-           "saturation": sat}
-    for load in (0.5, 0.8):
-        srv = Server(params, device=dev, keep_results=False, reserve_pixels=64 << 20)
-        srv.serve(requests([0.0] * min(64, nrequests)), realtime=False)   # warm-up
-        srv.completed.clear()
-        srv.batch_sizes.clear()
-        arr = poisson_arrivals(seed + int(load * 100), nrequests, load * sat_rps)
+    sat["mean_batch"] = round(len(done) / max(1, len(srv.batch_sizes)), 2)
+    out = {"workload": f"requests with sides log-uniform in [256, 4096] per axis, K in "
+                       f"{{8,16,32}}, 20 k-means iterations, 5-D features, 8-CCL, merge<256, "
+                       f"erosion, normals; {pool} distinct images cycled "
+                       f"({mean_px / 1e6:.2f} Mpix mean); 40 GB budget; C++ server",
+           "seconds_per_rate": seconds, "saturation": sat, "rates": {}}
+    for rate in rates:
+        n = max(8, int(round(rate * seconds)))
+        arr = poisson_arrivals(seed + int(rate), n, float(rate))
         t = time.perf_counter()
         done = srv.serve(requests(arr))
         wall = time.perf_counter() - t
         rep = Server.report(done, wall)
-        rep["offered_rps"] = round(load * sat_rps, 1)
-        rep["mean_batch"] = round(sum(srv.batch_sizes) / max(1, len(srv.batch_sizes)), 2)
-        out[f"load_{int(load * 100)}"] = rep
+        rep["offered_rps"] = rate
+        rep["offered_mpix_s"] = round(rate * mean_px / 1e6, 1)
+        rep["mean_batch"] = round(len(done) / max(1, len(srv.batch_sizes)), 2)
+        out["rates"][str(rate)] = rep
+    c = srv.counters()
+    out["bytes_per_pixel"] = int(c.bytes_per_pixel)
+    out["peak_in_use_gb"] = round(c.peak_in_use_bytes / 1e9, 2)
     return out
 
 
@@ -624,7 +676,10 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--batch-images", type=int, default=256)
     ap.add_argument("--no-batch", action="store_true")
-    ap.add_argument("--serve-requests", type=int, default=1024)
+    ap.add_argument("--serve-rates", default="50,200,500,1000,2000",
+                    help="offered request rates (req/s) of the serving leg")
+    ap.add_argument("--serve-seconds", type=float, default=4.0,
+                    help="open-loop arrivals per rate, in seconds")
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--no-stress", action="store_true")
     ap.add_argument("--no-next", action="store_true",
@@ -780,8 +835,9 @@ def main():
         next_rows = run_next_rows(dev, pipe, rgb)
 
     serving = None
-    if not args.no_serve and args.serve_requests > 0:
-        serving = run_serving(dev, min(args.batch_images, 256) or 64, args.serve_requests)
+    if not args.no_serve:
+        serving = run_serving(dev, [int(x) for x in args.serve_rates.split(",")],
+                              args.serve_seconds)
 
     if rank == 0:
         cpu = None

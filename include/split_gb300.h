@@ -91,6 +91,7 @@ const char* split_status_string(int status);
  * work queued on `stream` completes.  Synchronises `stream`. */
 int split_workspace_status(void* workspace, void* stream, int* out_status);
 
+
 /* ======================================================================== */
 /* k-means                                                                  */
 /* ======================================================================== */
@@ -148,6 +149,17 @@ int split_kmeans_cluster_noalloc(const void* points, int layout, int dim,
                                  int32_t* labels, int max_iter,
                                  float threshold, int32_t* d_iterations,
                                  int32_t* d_status, void* stream);
+
+/* Test setting of the bounded waits (no counterpart in the reference, which
+ * has no device-wide waits).  Process-wide; applies to the single-image
+ * k-means launches queued after the call (not to batches).  A device-wide
+ * barrier of those launches gives up after spin_limit polls (0: the default,
+ * about a second), and block skip_block (>= 0; -1: none) leaves at its first
+ * barrier without arriving, so that the other blocks' wait runs out: the call
+ * then reports SPLIT_ERR_TIMEOUT through split_workspace_status, and every
+ * block returns (nothing waits without a limit).  (0, -1) restores normal
+ * operation. */
+void split_kmeans_set_wait_test(unsigned spin_limit, int skip_block);
 
 /* Replaces split::device::kmeans::label_points_workspace (label.cuh:39-40). */
 size_t split_kmeans_assign_workspace_size(int64_t npoints, int nclusters);
@@ -429,9 +441,102 @@ int split_batch_bind(split_batch* batch, const uint8_t* rgb, float* centroids,
  * segment labels come out image-local (minimum linear index within the
  * image, -1 = eroded). */
 int split_batch_run(split_batch* batch, void* stream);
+/* split_batch_run with per-stage timing: stage_events is null, or
+ * 2 * SPLIT_PIPELINE_STAGES cudaEvent_t recorded on `stream` around the
+ * batch's stages in the order of split_pipeline_run's (features, k-means,
+ * labelling, merge decision, relabel + erosion, normals). */
+int split_batch_run_events(split_batch* batch, void* const* stage_events,
+                           void* stream);
 
 /* Kernels launched by this library since it was loaded (all entry points). */
 unsigned long long split_launch_count(void);
+
+/* ======================================================================== */
+/* serving (no counterpart in the reference, whose only caller segments one  */
+/* image per run: samples/src/main.cu:154-372)                               */
+/* ======================================================================== */
+
+/* A continuous-batching server on one GPU.  Requests are admitted in arrival
+ * order while their device footprint fits the HBM budget, packed into
+ * batches (split_batch_*) while fewer than max_inflight batches are on the
+ * device, and run with uploads, compute and downloads on three streams.  A
+ * worker thread owned by the server does all of this; submit and poll may be
+ * called from any thread.  Every request's results equal the same request
+ * served alone (and the single-image pipeline's). */
+typedef struct split_server split_server; /* opaque */
+
+typedef struct split_server_config {
+  split_pipeline_params params; /* as for split_batch_create (per-request K
+                                   and iteration count replace nclusters and
+                                   kmeans_iters) */
+  size_t hbm_budget_bytes;      /* admission budget; 0: 40 GiB */
+  int64_t max_batch_pixels;     /* pixel cap of a batch; 0: 64 Mi pixels (a
+                                   larger image still forms a batch alone) */
+  int max_inflight;             /* batches on the device at once; 0: 2 (<= 8) */
+  int device;                   /* CUDA device ordinal */
+} split_server_config;
+
+/* One request.  All pointers are host memory that must stay valid until the
+ * request's completion has been returned by split_server_poll; page-locked
+ * buffers (cudaHostAlloc / cudaHostRegister) let the copies overlap. */
+typedef struct split_request {
+  const uint8_t* rgb;       /* height * width * 3 bytes, interleaved RGB8 */
+  int width, height;
+  int nclusters;            /* K <= 64 */
+  int kmeans_iters;
+  const float* centroids;   /* initial centroids, dim x K planar */
+  int32_t* segment_labels;  /* out: height * width (image-local minimum
+                               index of each segment, -1 = eroded) */
+  float* centroids_out;     /* out (optional): dim x K */
+  float* normals;           /* out (optional): 3 x height * width planar */
+  int32_t* cluster_labels;  /* out (optional): height * width */
+  void* user;               /* returned with the completion */
+} split_request;
+
+typedef struct split_completion {
+  uint64_t ticket;    /* from split_server_submit */
+  void* user;
+  int status;         /* SPLIT_OK, or the error of the request's batch */
+  int64_t pixels;
+  double latency_ms;  /* submit -> results in the host buffers */
+} split_completion;
+
+typedef struct split_server_counters {
+  uint64_t submitted, completed, batches;
+  size_t in_use_bytes;       /* footprint of admitted, unfinished requests */
+  size_t peak_in_use_bytes;
+  size_t bytes_per_pixel;    /* the footprint of a pixel of a request */
+  size_t budget_bytes;
+} split_server_counters;
+
+int split_server_create(const split_server_config* config, split_server** out);
+/* The device footprint of one pixel of a request under these parameters
+ * (arenas plus workspace; a request of w x h pixels holds
+ * ceil(w * h / 64) * 64 times this while admitted).  0: invalid parameters. */
+size_t split_server_bytes_per_pixel(const split_pipeline_params* params);
+/* Grows every slot's resident arena to hold a batch of `pixels` pixels in up
+ * to `max_requests` images (so that serving allocates nothing later).  Only
+ * while the server is idle. */
+int split_server_reserve(split_server* server, int64_t pixels, int max_requests);
+/* Queues a request (never blocks on the GPU).  SPLIT_ERR_WORKSPACE: its
+ * footprint exceeds the whole budget. */
+int split_server_submit(split_server* server, const split_request* request,
+                        uint64_t* ticket);
+/* Returns up to `max` completions (*n of them), waiting up to timeout_ms for
+ * the first (0: do not wait; < 0: until one arrives or nothing is pending). */
+int split_server_poll(split_server* server, split_completion* out, int max,
+                      int timeout_ms, int* n);
+int split_server_stats(split_server* server, split_server_counters* out);
+/* Finishes every submitted request, then frees the server. */
+int split_server_destroy(split_server* server);
+/* The admission and batch-formation policy on the host alone (for tests):
+ * n requests of the given footprints and pixel counts arrive at once;
+ * batch_of[i] receives request i's batch.  Returns the number of batches or
+ * a negative status. */
+int split_server_admission_test(const int64_t* footprints, const int64_t* pixels,
+                                int n, int64_t budget, int64_t max_batch_pixels,
+                                int max_inflight, int32_t* batch_of,
+                                int64_t* peak_in_use);
 
 /* ======================================================================== */
 /* tuning table (no counterpart in the reference)                           */

@@ -143,7 +143,8 @@ inline std::size_t cluster_workspace(int npoints, int nclusters, int dim, int wi
 enum class Convergence { reference, l2_change };
 
 /* kmeans/cluster.cuh:31-37.  Planar D x N points (D = 3 or 5, all rows read
- * from memory), D x K centroids in/out.  Returns the iterations performed
+ * from memory), D x K centroids in/out, K <= 64 (the centroids live in shared
+ * memory; a larger K throws split::device::error with SPLIT_ERR_INVALID).  Returns the iterations performed
  * (the reference returns nothing; reading the count synchronises `stream`). */
 inline int cluster(const_view2d<float> points, view2d<float> centroids, view1d<int> labels,
                    Temp& temp, int max_iter, float threshold = 1.f, int width = 0,
@@ -299,19 +300,33 @@ inline void merge_smooth_boundaries(const_view2d<float> points, int nsegments,
 namespace morph {
 
 /* morph/erode.cuh:16-18: in-place square erosion of every label's mask
- * (eroded pixels = -1).  The kernel writes to a separate buffer: pass one
- * (`scratch`, at least as large as `labels`) or let the call take
- * stream-ordered memory (cudaMallocAsync) for it, as the reference
- * allocates internally. */
+ * (eroded pixels = -1), any niterations >= 0.  The kernel writes to a
+ * separate buffer: pass one (`scratch`, at least as large as `labels`) or let
+ * the call take stream-ordered memory (cudaMallocAsync) for it, as the
+ * reference allocates internally.  One kernel pass erodes by up to 16; a
+ * larger radius runs in passes (square erosions compose: radius a then b is
+ * radius a + b, with the image border and -1 pixels as background). */
 inline void erode(view2d<int> labels, int niterations = 1, int32_t* scratch = nullptr,
                   cudaStream_t stream = nullptr) {
+  if (niterations < 0) check(SPLIT_ERR_INVALID, "morph::erode");
+  if (niterations == 0) return;
   const int w = (int)labels.num_cols(), h = (int)labels.num_rows();
   const size_t bytes = sizeof(int32_t) * (size_t)w * h;
   int32_t* tmp = scratch;
   if (!tmp) check_cuda(cudaMallocAsync((void**)&tmp, bytes, stream), "morph::erode: alloc");
-  int st = split_erode(labels.data(), tmp, w, h, niterations, stream);
-  if (st == SPLIT_OK)
-    st = cudaMemcpyAsync(labels.data(), tmp, bytes, cudaMemcpyDeviceToDevice, stream) ==
+  int32_t* src = labels.data();
+  int32_t* dst = tmp;
+  int st = SPLIT_OK;
+  for (int left = niterations; left > 0 && st == SPLIT_OK;) {
+    const int r = left < 16 ? left : 16;
+    st = split_erode(src, dst, w, h, r, stream);
+    left -= r;
+    int32_t* t = src;
+    src = dst;
+    dst = t;
+  }
+  if (st == SPLIT_OK && src != labels.data())
+    st = cudaMemcpyAsync(labels.data(), src, bytes, cudaMemcpyDeviceToDevice, stream) ==
                  cudaSuccess ? SPLIT_OK : SPLIT_ERR_CUDA;
   if (!scratch) cudaFreeAsync(tmp, stream);
   check(st, "morph::erode");

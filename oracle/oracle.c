@@ -323,20 +323,28 @@ ORC_API int orc_merge_small(const int32_t* in, int width, int height, int P,
     int32_t t = map[s];
     fixed[s] = (map[t] == s && s > t) ? (int32_t)s : t;
   }
+  /* every segment follows its chain to the end (map_until_converged.cuh:
+   * 14-31); ends already found are remembered (done[] marks them), so each
+   * chain link is walked once */
   int rc = 0;
+  unsigned char* done = (unsigned char*)calloc((size_t)n, 1);
+  int32_t* path = (int32_t*)malloc(sizeof(int32_t) * (size_t)n);
   for (int64_t s = 0; s < n && !rc; ++s) {
-    if (fixed[s] == s) continue;
+    if (done[s]) continue;
+    int64_t len = 0;
     int32_t r = (int32_t)s;
-    int64_t steps = 0;
-    while (fixed[r] != r) {
+    while (!done[r] && fixed[r] != r) {
+      path[len++] = r;
       r = fixed[r];
-      if (++steps > n) { rc = 3; break; }
+      if (len > n) { rc = 3; break; }
     }
-    map[s] = r;
+    if (rc) break;
+    const int32_t end = done[r] ? map[r] : r;
+    if (!done[r]) { map[r] = r; done[r] = 1; }
+    for (int64_t i = 0; i < len; ++i) { map[path[i]] = end; done[path[i]] = 1; }
   }
-  if (!rc)
-    for (int64_t s = 0; s < n; ++s)
-      if (fixed[s] == s) map[s] = (int32_t)s;
+  free(done);
+  free(path);
   for (int64_t i = 0; i < n; ++i) out[i] = map[in[i]];
   free(fixed);
   free(e);

@@ -26,6 +26,7 @@ _SIGS = {
     "split_version": (C.c_char_p, []),
     "split_status_string": (C.c_char_p, [_i32]),
     "split_workspace_status": (_i32, [_vp, _vp, C.POINTER(C.c_int)]),
+    "split_kmeans_set_wait_test": (None, [C.c_uint, _i32]),
     "split_kmeans_cluster_workspace_size": (_sz, [_i64, _i32, _i32]),
     "split_kmeans_cluster_workspace_size_2d": (_sz, [_i64, _i32, _i32, _i32]),
     "split_kmeans_cluster": (_i32, [_vp, _i32, _i32, _i64, _i32, _f32, _vp, _i32, _vp, _vp, _sz,
@@ -75,6 +76,15 @@ _SIGS = {
     "split_batch_centroid_offset": (_i64, [_vp, _i32]),
     "split_batch_bind": (_i32, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _sz, _vp]),
     "split_batch_run": (_i32, [_vp, _vp]),
+    "split_batch_run_events": (_i32, [_vp, _vp, _vp]),
+    "split_server_bytes_per_pixel": (_sz, [_vp]),
+    "split_server_create": (_i32, [_vp, _vp]),
+    "split_server_reserve": (_i32, [_vp, _i64, _i32]),
+    "split_server_submit": (_i32, [_vp, _vp, _vp]),
+    "split_server_poll": (_i32, [_vp, _vp, _i32, _i32, _vp]),
+    "split_server_stats": (_i32, [_vp, _vp]),
+    "split_server_destroy": (_i32, [_vp]),
+    "split_server_admission_test": (_i32, [_vp, _vp, _i32, _i64, _i64, _i32, _vp, _vp]),
 }
 
 
@@ -91,6 +101,33 @@ FEATURES_LAB_BETA = 3   # split_pipeline_params.features: the sample's Lab + bet
 
 
 PIPELINE_STAGES = ("pack", "kmeans", "ccl", "merge", "erode", "normals")
+
+
+class ServerConfig(C.Structure):
+    """split_server_config (include/split_gb300.h)."""
+    _fields_ = [("params", PipelineParams), ("hbm_budget_bytes", C.c_size_t),
+                ("max_batch_pixels", C.c_int64), ("max_inflight", C.c_int), ("device", C.c_int)]
+
+
+class ServerRequest(C.Structure):
+    """split_request (include/split_gb300.h)."""
+    _fields_ = [("rgb", C.c_void_p), ("width", C.c_int), ("height", C.c_int),
+                ("nclusters", C.c_int), ("kmeans_iters", C.c_int), ("centroids", C.c_void_p),
+                ("segment_labels", C.c_void_p), ("centroids_out", C.c_void_p),
+                ("normals", C.c_void_p), ("cluster_labels", C.c_void_p), ("user", C.c_void_p)]
+
+
+class Completion(C.Structure):
+    """split_completion (include/split_gb300.h)."""
+    _fields_ = [("ticket", C.c_uint64), ("user", C.c_void_p), ("status", C.c_int),
+                ("pixels", C.c_int64), ("latency_ms", C.c_double)]
+
+
+class ServerCounters(C.Structure):
+    """split_server_counters (include/split_gb300.h)."""
+    _fields_ = [("submitted", C.c_uint64), ("completed", C.c_uint64), ("batches", C.c_uint64),
+                ("in_use_bytes", C.c_size_t), ("peak_in_use_bytes", C.c_size_t),
+                ("bytes_per_pixel", C.c_size_t), ("budget_bytes", C.c_size_t)]
 
 
 class BatchImage(C.Structure):

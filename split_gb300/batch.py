@@ -148,8 +148,18 @@ class Batch:
                                        non_blocking=True)
 
     # ---- execution
-    def run(self, stream=None):
-        N.check(N.load().split_batch_run(self._h, stream_handle(stream)), "batch.run")
+    def run(self, stream=None, stage_events=None):
+        """One run of the bound batch; stage_events: None, or
+        2 * len(PIPELINE_STAGES) torch CUDA events (recorded once before)
+        placed around the stages."""
+        if stage_events is None:
+            N.check(N.load().split_batch_run(self._h, stream_handle(stream)), "batch.run")
+            return
+        if any(e.cuda_event == 0 for e in stage_events):
+            raise ValueError("stage events must have been recorded once (torch creates "
+                             "CUDA events lazily)")
+        ev = (C.c_void_p * len(stage_events))(*[e.cuda_event for e in stage_events])
+        N.check(N.load().split_batch_run_events(self._h, ev, stream_handle(stream)), "batch.run")
 
     def capture(self):
         """Capture one run into a CUDA graph (replay with replay())."""

@@ -252,17 +252,27 @@ extern "C" int split_batch_bind(split_batch* b, const uint8_t* rgb, float* centr
 }
 
 extern "C" int split_batch_run(split_batch* b, void* stream) {
+  return split_batch_run_events(b, nullptr, stream);
+}
+
+extern "C" int split_batch_run_events(split_batch* b, void* const* stage_events, void* stream) {
   if (!b || !b->bound) return SPLIT_ERR_INVALID;
   const split_pipeline_params& p = b->params;
   Layout l = carve(b->ws, *b);
   cudaStream_t st = as_stream(stream);
+  auto mark = [&](int i) -> int {
+    if (stage_events)
+      SG_CUDA_TRY(cudaEventRecord(reinterpret_cast<cudaEvent_t>(stage_events[i]), st));
+    return SPLIT_OK;
+  };
   // the stages' own status words (sub-workspace headers, cleared at bind),
   // folded into the batch's at the end
   StatusSources ss{};
   ss.p[ss.n++] = &static_cast<WsHeader*>(l.km_ws)->status;
   ss.p[ss.n++] = &static_cast<WsHeader*>(l.ccl_ws)->status;
   if (l.mrg_ws) ss.p[ss.n++] = &static_cast<WsHeader*>(l.mrg_ws)->status;
-  // byte / 255 features with the normals, from one read of the bytes
+  // 0: byte / 255 features with the normals, from one read of the bytes
+  SG_TRY(mark(0));
   const bool fused = p.features == SPLIT_LAYOUT_FLOAT4 && p.compute_normals;
   if (fused)
     SG_TRY(normals_rgb8_geoms(b->rgb, device_geoms(*b, l, l.rgb_maps), p.depth, b->normals,
@@ -272,10 +282,19 @@ extern "C" int split_batch_run(split_batch* b, void* stream) {
   else if (p.features == kFeaturesLabBeta)
     SG_TRY(lab_beta_geoms(b->rgb, device_geoms(*b, l, nullptr), p.beta_mu, l.features4, l.maxima,
                           st));
+  SG_TRY(mark(1));
+  // 1: k-means over every image
+  SG_TRY(mark(2));
   SG_TRY(kmeans_batch_run(b->km, l.km_ws, st));
+  SG_TRY(mark(3));
+  // 2: connected components
+  SG_TRY(mark(4));
   const Geoms gs = device_geoms(*b, l, nullptr);
   SG_TRY(ccl_geoms(b->cluster_labels, gs, p.connectivity, SPLIT_LABEL_MIN_INDEX, l.seg,
                    p.merge_P > 0 ? l.sizes : nullptr, reinterpret_cast<WsHeader*>(l.ccl_ws), st));
+  SG_TRY(mark(5));
+  // 3: merge decision
+  SG_TRY(mark(6));
   const void* mstate = nullptr;
   const int32_t* mfin = nullptr;
   if (p.merge_P > 0) {
@@ -285,12 +304,19 @@ extern "C" int split_batch_run(split_batch* b, void* stream) {
     mstate = mv.state;
     mfin = mv.fin;
   }
+  SG_TRY(mark(7));
+  // 4: relabel + erosion
+  SG_TRY(mark(8));
   SG_TRY(erode_geoms(l.seg, b->segment_labels, device_geoms(*b, l, l.lab_maps), p.erode_radius,
                      mstate, mfin, 1, st));
+  SG_TRY(mark(9));
+  // 5: normals (empty when the features pass wrote them)
+  SG_TRY(mark(10));
   if (p.compute_normals && !fused)
     SG_TRY(normals_rgb8_geoms(b->rgb, device_geoms(*b, l, l.rgb_maps), p.depth, b->normals,
                               nullptr, st));
   // errors the stages recorded in their own workspace headers, into the
   // batch's status word
-  return fold_status(&l.hdr->status, ss, st);
+  SG_TRY(fold_status(&l.hdr->status, ss, st));
+  return mark(11);
 }

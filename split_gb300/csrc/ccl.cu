@@ -161,7 +161,7 @@ __device__ __forceinline__ Links needed(bool N, bool W, bool NW, bool NE, bool E
 // root in one step and stores the global index of that local root.  Local
 // roots clear their size counter.
 template <bool MAXC, int CONN>
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreads, 5)
 tile_kernel(const int32_t* __restrict__ in, Geoms gs, int* __restrict__ P,
             int32_t* __restrict__ sizes, int* status) {
   __shared__ int lab[TH * TW];
@@ -173,13 +173,40 @@ tile_kernel(const int32_t* __restrict__ in, Geoms gs, int* __restrict__ P,
   const int lane = threadIdx.x & 31, r0 = (threadIdx.x >> 5) * kRowsPerWarp;
   const bool ca = lane < tw, cb = lane + 32 < tw;
   int va[kRowsPerWarp], vb[kRowsPerWarp], na[kRowsPerWarp], nb[kRowsPerWarp];
+  // the tile's first pixel: a tile holding one value everywhere is one
+  // component, written without the run / union machinery below
+  const int v0 = __ldg(in + off + (long long)ty0 * W + tx0);
+  bool same = true;
 #pragma unroll
   for (int k = 0; k < kRowsPerWarp; ++k) {
     const int r = r0 + k;
     const bool rok = r < th;
     const int32_t* row = in + off + (long long)(ty0 + (rok ? r : 0)) * W + tx0;
-    va[k] = (rok && ca) ? __ldg(row + lane) : 0;
-    vb[k] = (rok && cb) ? __ldg(row + lane + 32) : 0;
+    va[k] = (rok && ca) ? __ldg(row + lane) : v0;
+    vb[k] = (rok && cb) ? __ldg(row + lane + 32) : v0;
+    same = same && va[k] == v0 && vb[k] == v0;
+  }
+  if (__syncthreads_and(same)) {
+    // local root: the first pixel (minimum convention) or the last (maximum)
+    const long long gr = off + (long long)(ty0 + (MAXC ? th - 1 : 0)) * W + tx0 +
+                         (MAXC ? tw - 1 : 0);
+#pragma unroll
+    for (int k = 0; k < kRowsPerWarp; ++k) {
+      const int r = r0 + k;
+      if (r >= th) break;
+      const long long rowg = off + (long long)(ty0 + r) * W + tx0;
+      if (ca) __stcg(P + rowg + lane, rowg + lane == gr ? (int)gr : ~(int)gr);
+      if (cb) __stcg(P + rowg + lane + 32, rowg + lane + 32 == gr ? (int)gr : ~(int)gr);
+    }
+    if (sizes && threadIdx.x == 0) sizes[gr] = tw * th;
+    return;
+  }
+#pragma unroll
+  for (int k = 0; k < kRowsPerWarp; ++k) {
+    const int r = r0 + k;
+    const bool rok = r < th;
+    va[k] = (rok && ca) ? va[k] : 0;
+    vb[k] = (rok && cb) ? vb[k] : 0;
     lab[r * TW + lane] = va[k];
     lab[r * TW + lane + 32] = vb[k];
     // run nodes of this row
@@ -416,19 +443,46 @@ flatten_kernel(int* P, Geoms gs, int32_t* __restrict__ sizes, int* status) {
   const int tw = min(TW, W - tx0), th = min(TH, t.H - ty0);
   const int lane = threadIdx.x & 31, r0 = (threadIdx.x >> 5) * kRowsPerWarp;
   const int base = (int)(t.off + (long long)ty0 * W + tx0);
+  if (r0 >= th) return;   // the warp's rows lie below the image
   int g[2 * kRowsPerWarp], e[2 * kRowsPerWarp], x[2 * kRowsPerWarp], p[2 * kRowsPerWarp];
 #pragma unroll
   for (int k = 0; k < 2 * kRowsPerWarp; ++k) {
     const int r = r0 + (k >> 1), c = lane + 32 * (k & 1);
     g[k] = (r < th && c < tw) ? base + r * W + c : -1;
     e[k] = g[k] >= 0 ? __ldcg(P + g[k]) : 0;
-  }
-#pragma unroll
-  for (int k = 0; k < 2 * kRowsPerWarp; ++k) {
     x[k] = local_root(e[k]);
-    p[k] = g[k] >= 0 && x[k] != g[k] ? P[x[k]] : x[k];
   }
   unsigned budget = kFindCap;
+  // A warp whose pixels all name one local root (a uniform stretch of the
+  // image) resolves that root's chain once, in lane 0, and broadcasts it.
+  // Lane 0's first pixel is inside the image whenever the warp's rows are.
+  const int xr = __shfl_sync(0xffffffffu, x[0], 0);
+  bool same = true;
+#pragma unroll
+  for (int k = 0; k < 2 * kRowsPerWarp; ++k) same = same && (g[k] < 0 || x[k] == xr);
+  if (__all_sync(0xffffffffu, same)) {
+    int f = xr;
+    if (lane == 0) {
+      int q = P[f];
+      while (q != f && budget) {
+        --budget;
+        f = q;
+        q = P[f];
+      }
+    }
+    f = __shfl_sync(0xffffffffu, f, 0);
+#pragma unroll
+    for (int k = 0; k < 2 * kRowsPerWarp; ++k) {
+      if (g[k] < 0 || e[k] == g[k]) continue;   // outside, or a final root
+      P[g[k]] = f;
+      if (sizes && e[k] >= 0) atomicAdd(sizes + f, __ldcg(sizes + g[k]));
+    }
+    if (!budget) set_status(status, SPLIT_ERR_NOT_CONVERGED);
+    return;
+  }
+#pragma unroll
+  for (int k = 0; k < 2 * kRowsPerWarp; ++k)
+    p[k] = g[k] >= 0 && x[k] != g[k] ? P[x[k]] : x[k];
 #pragma unroll
   for (int k = 0; k < 2 * kRowsPerWarp; ++k) {
     if (g[k] < 0 || e[k] == g[k]) continue;   // outside, or a final root

@@ -114,9 +114,12 @@ bool layout_unchanged(const void* workspace, unsigned long long key);
 constexpr unsigned kSpinLimit = 1u << 24;
 
 // Device-wide barrier for a cooperative (co-resident) grid.  Sense is carried
-// by a generation counter.  A wait that exceeds kSpinLimit records
-// SPLIT_ERR_TIMEOUT and returns false; callers then leave the kernel.
-__device__ __forceinline__ bool grid_barrier(WsHeader* h) {
+// by a generation counter.  A wait that exceeds `limit` polls (kSpinLimit by
+// default) records SPLIT_ERR_TIMEOUT and returns false; callers then leave
+// the kernel.  Block `skip` (a test setting; -1: none) returns false at once
+// without arriving, so that the others' wait runs out.
+__device__ __forceinline__ bool grid_barrier(WsHeader* h, unsigned limit = kSpinLimit,
+                                             int skip = -1) {
   __syncthreads();
   __shared__ int ok;
   if (threadIdx.x == 0) {
@@ -124,16 +127,21 @@ __device__ __forceinline__ bool grid_barrier(WsHeader* h) {
     cuda::atomic_ref<unsigned, cuda::thread_scope_device> cnt(h->barrier_count);
     const unsigned nblocks = gridDim.x * gridDim.y * gridDim.z;
     const unsigned g = gen.load(cuda::memory_order_relaxed);
+    const unsigned lim = limit;
     ok = 1;
     // acq_rel: publish this block's writes, observe the others' on release
-    const unsigned arrived = cnt.fetch_add(1, cuda::memory_order_acq_rel);
-    if (arrived == nblocks - 1) {
+    const unsigned arrived = skip == (int)blockIdx.x
+                                 ? ~0u
+                                 : cnt.fetch_add(1, cuda::memory_order_acq_rel);
+    if (arrived == ~0u) {
+      ok = 0;
+    } else if (arrived == nblocks - 1) {
       cnt.store(0, cuda::memory_order_relaxed);
       gen.fetch_add(1, cuda::memory_order_release);
     } else {
       unsigned spins = 0;
       while (gen.load(cuda::memory_order_acquire) == g) {
-        if (++spins > kSpinLimit) {
+        if (++spins > lim) {
           set_status(&h->status, SPLIT_ERR_TIMEOUT);
           ok = 0;
           break;

@@ -29,6 +29,7 @@
 #include <math.h>
 #include <string.h>
 
+#include <atomic>
 #include <mutex>
 #include <vector>
 
@@ -99,6 +100,10 @@ struct Params {
   ImageState* state;     // [2][nimages]: state after iteration i - 1 in slot i & 1
   WsHeader* hdr;
   int blocks_per_sm;     // 0: as many as fit (host side only)
+  // grid barriers: polls before a wait gives up, and a block that leaves
+  // without arriving (-1: none); see split_kmeans_set_wait_test
+  unsigned wait_limit;
+  int wait_skip;
 };
 
 constexpr int cstride(int dim) { return dim == 3 ? 4 : 8; }
@@ -404,6 +409,30 @@ __device__ __forceinline__ void flush_acc(Smem& sm, int warp, int l, const float
   if (lane == 0) sm.cnt[warp][l] += c;
 }
 
+// Accumulate one batch whose kPx pixels all carry label l (warp-uniform):
+// the same sums, in the same order, as accumulate_valid's uniform case.
+template <int DIM>
+__device__ __forceinline__ void accumulate_uniform(Smem& sm, int warp, const float (&f)[kPx][DIM],
+                                                   int l, int& acc_l, int& acc_n,
+                                                   float (&acc)[DIM]) {
+  constexpr int CS = cstride(DIM);
+  if (l != acc_l) {
+    if (acc_l >= 0) flush_acc<DIM>(sm, warp, acc_l, acc, acc_n);
+    acc_l = l;
+    acc_n = 0;
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) acc[d] = 0.0f;
+  }
+  float c[DIM];
+#pragma unroll
+  for (int d = 0; d < DIM; ++d) c[d] = sm.cent[l * CS + d];
+#pragma unroll
+  for (int j = 0; j < kPx; ++j)
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) acc[d] = __fadd_rn(acc[d], __fsub_rn(f[j][d], c[d]));
+  acc_n += kPx;
+}
+
 // Accumulate one batch whose kPx labels are all valid: the same sums, in the
 // same order, as the general path below.
 template <int DIM>
@@ -486,6 +515,10 @@ __device__ __forceinline__ void fast_span(const Image& im, Smem& sm, int warp, i
                                           float (&acc)[DIM]) {
   const int64_t step = (int64_t)kBatchRows * im.width;
   int64_t px0 = (int64_t)row_first * im.width + col;
+  // A mask with one cluster names every pixel's nearest centroid outright:
+  // the span's box excludes all others for every pixel it holds (and the
+  // features of this path lie in the unit cube, so none is NaN).
+  const int single = (mask != 0ull && (mask & (mask - 1ull)) == 0ull) ? __ffsll(mask) - 1 : -1;
   float fx[kPx];
 #pragma unroll
   for (int j = 0; j < kPx; ++j) fx[j] = __fmul_rn(im.xy_scale, (float)(col + j));
@@ -560,10 +593,21 @@ __device__ __forceinline__ void fast_span(const Image& im, Smem& sm, int warp, i
       }
     }
     int lab[kPx];
-    nearest_px<DIM>(f, sm.cent, mask, lab);
+    if (single >= 0) {
+      // one candidate for the whole span: every pixel's argmin, no distances
+#pragma unroll
+      for (int j = 0; j < kPx; ++j) lab[j] = single;
+    } else {
+      nearest_px<DIM>(f, sm.cent, mask, lab);
+    }
     if (write_labels)
       *reinterpret_cast<int4*>(im.labels + px0) = make_int4(lab[0], lab[1], lab[2], lab[3]);
-    if (MODE != kAssignOnly) accumulate_valid<DIM>(sm, warp, f, lab, acc_l, acc_n, acc);
+    if (MODE != kAssignOnly) {
+      if (single >= 0)
+        accumulate_uniform<DIM>(sm, warp, f, single, acc_l, acc_n, acc);
+      else
+        accumulate_valid<DIM>(sm, warp, f, lab, acc_l, acc_n, acc);
+    }
   }
 }
 
@@ -974,7 +1018,7 @@ __global__ void __launch_bounds__(kThreads, SG_KM_MINBLOCKS) kmeans_kernel(Param
         for (int img = (int)blockIdx.x; img < p.nimages; img += gridDim.x)
           form_centroids<LAYOUT, DIM, MODE>(p, img, image_of(p, img), it, sm.cent, true,
                                             sm.lut);
-        if (!grid_barrier(p.hdr)) return;
+        if (!grid_barrier(p.hdr, p.wait_limit, p.wait_skip)) return;
       }
     }
     // The first wave is static (block b takes unit b): only later fetches go
@@ -1017,7 +1061,7 @@ __global__ void __launch_bounds__(kThreads, SG_KM_MINBLOCKS) kmeans_kernel(Param
     if (MODE == kAssignOnly) return;
     // the barrier publishes every block's sums (fire-and-forget adds ordered
     // by the block barrier before the arrival's release)
-    if (!grid_barrier(p.hdr)) return;
+    if (!grid_barrier(p.hdr, p.wait_limit, p.wait_skip)) return;
   }
   if (MODE == kAssignOnly || stopped) return;
   // centroids after the last iteration; every image stops here
@@ -1196,6 +1240,16 @@ static bool valid_features(const void* points, int layout, int dim, int64_t n,
   return true;
 }
 
+// Test setting of the grid barriers of single-image launches
+// (split_kmeans_set_wait_test): poll limit (0: kSpinLimit) and skipping block.
+static std::atomic<unsigned> g_wait_limit{0};
+static std::atomic<int> g_wait_skip{-1};
+static void wait_test(unsigned* limit, int* skip) {
+  const unsigned l = g_wait_limit.load(std::memory_order_relaxed);
+  *limit = l ? l : kSpinLimit;
+  *skip = g_wait_skip.load(std::memory_order_relaxed);
+}
+
 static int run(int mode, const void* points, int layout, int dim, int64_t n,
                int width, float xy_scale, float* centroids,
                const float* centroids_in, int K, int32_t* labels,
@@ -1236,6 +1290,7 @@ static int run(int mode, const void* points, int layout, int dim, int64_t n,
   im.unit_rows = te.kmeans_unit_rows;
   im.ref_shift = ref_shift;
   p.blocks_per_sm = te.kmeans_blocks_per_sm;
+  wait_test(&p.wait_limit, &p.wait_skip);
   p.nimages = 1;
   p.images = nullptr;
   p.total_units = units;
@@ -1263,6 +1318,11 @@ static int run(int mode, const void* points, int layout, int dim, int64_t n,
 }  // namespace sg
 
 using namespace sg;
+
+extern "C" void split_kmeans_set_wait_test(unsigned spin_limit, int skip_block) {
+  km::g_wait_limit.store(spin_limit, std::memory_order_relaxed);
+  km::g_wait_skip.store(skip_block < 0 ? -1 : skip_block, std::memory_order_relaxed);
+}
 
 extern "C" size_t split_kmeans_cluster_workspace_size_2d(int64_t npoints, int width,
                                                          int nclusters, int dim) {
@@ -1559,6 +1619,8 @@ int kmeans_batch_run(const KmBatchPlan& plan, void* ws, cudaStream_t st) {
   p.state = l.state;
   p.hdr = l.hdr;
   p.blocks_per_sm = plan.blocks_per_sm;
+  p.wait_limit = kSpinLimit;   // the wait test applies to single images only
+  p.wait_skip = -1;
   SG_TRY(reset_counters(l, plan.nimages, st));
   init_kernel<<<(plan.nimages + 255) / 256, 256, 0, st>>>(p);
   SG_TRY(launch_status());

@@ -16,7 +16,19 @@
 //   table keys / counts / slot list   zero outside a call
 //   best[n]                            zero outside a call
 // Per-call arrays: size[n] (unless the caller passes component sizes),
-// map[n], fin[n] (final target of every small segment), sum[n] (chroma).
+// map[n], fin[n] (final target of every small segment), sum[n] (chroma),
+// dec[n] (segments decided by the overflow path).
+//
+// The table holds at most half its capacity (2^ceil(log2 n) slots) of pairs.
+// An image cut into very many small segments can have more distinct pairs
+// than that (up to about 8 per pixel).  Then the pair pass stops inserting and
+// flags the overflow, and the decision kernel takes the overflow path: the
+// small segments are split into classes by the top bits of a hash of their
+// id, and each class goes through its own round of pair pass, bids and
+// decisions in the emptied table; a class whose pairs still do not fit is
+// split in two again.  Bids only compare pairs of one segment, so rounds over
+// disjoint classes decide exactly what one pass over a large enough table
+// would.  The chains then resolve over the decided segments.
 #include "geom.cuh"
 #include "merge_state.cuh"
 
@@ -27,6 +39,9 @@ constexpr int kThreads = 256;
 static_assert(kTileH * kTileW % kThreads == 0, "whole pixels per thread in a tile");
 constexpr int kProbeCap = 1 << 16;
 constexpr unsigned kChainCap = 1u << 24;
+// overflow path: pending classes (level, class) on a stack, and a bound on rounds
+constexpr int kStackCap = 64;
+constexpr unsigned kRoundCap = 1u << 20;
 
 struct Layout {
   WsHeader* hdr;
@@ -39,6 +54,8 @@ struct Layout {
   unsigned long long* keys;
   unsigned* counts;
   int32_t* list;
+  int32_t* dec;
+  int* stack;   // [1 + 2 * kStackCap]: depth, then (level, class) pairs
   int cap_log2;
   size_t bytes;
 };
@@ -64,6 +81,8 @@ inline Layout carve(void* ws, int64_t n) {
   l.keys = c.take<unsigned long long>(cap);
   l.counts = c.take<unsigned>(cap);
   l.list = c.take<int32_t>(cap);
+  l.dec = c.take<int32_t>((size_t)n);
+  l.stack = c.take<int>(1 + 2 * kStackCap);
   l.bytes = c.size();
   return l;
 }
@@ -74,13 +93,16 @@ __device__ __forceinline__ unsigned long long pair_key(int s, int t) {
 __device__ __forceinline__ int key_s(unsigned long long k) { return (int)((k - 1ull) >> 32); }
 __device__ __forceinline__ int key_t(unsigned long long k) { return (int)(unsigned)((k - 1ull) & 0xffffffffull); }
 
-__device__ void insert(const Layout& L, int s, int t, unsigned m, int* status) {
+// Inserts (s, t) with multiplicity m.  A new pair beyond half the capacity
+// (or a probe sequence that runs out) flags the overflow instead.
+__device__ void insert(const Layout& L, int s, int t, unsigned m) {
   const unsigned long long key = pair_key(s, t);
   const unsigned mask = (1u << L.cap_log2) - 1u;
   unsigned h = (unsigned)((key * 0x9E3779B97F4A7C15ull) >> (64 - L.cap_log2));
   for (int probe = 0; probe < kProbeCap; ++probe, h = (h + 1) & mask) {
     unsigned long long k = *(volatile unsigned long long*)(L.keys + h);
     if (k == 0ull) {
+      if (*(volatile unsigned*)&L.state->list_count >= (mask >> 1)) break;
       k = atomicCAS(L.keys + h, 0ull, key);
       if (k == 0ull) {
         atomicAdd(L.counts + h, m);
@@ -94,7 +116,13 @@ __device__ void insert(const Layout& L, int s, int t, unsigned m, int* status) {
       return;
     }
   }
-  set_status(status, SPLIT_ERR_OVERFLOW);
+  *(volatile int*)&L.state->overflow = 1;
+}
+
+// Class of segment s at split level `lev`: the top lev bits of a hash of s
+// (level 0: every segment in class 0).
+__device__ __forceinline__ unsigned seg_class(int s, int lev) {
+  return lev == 0 ? 0u : ((unsigned)s * 2654435761u) >> (32 - lev);
 }
 
 // sizes (generic path) and chroma sums; REF_CHROMA also notes whether the
@@ -123,12 +151,14 @@ size_kernel(const int32_t* __restrict__ lab, int64_t n, Layout L, bool count_siz
   }
 }
 
-// boundary histogram of small segments, one block per 32 x 64 tile
-__global__ void __launch_bounds__(kThreads)
-pair_kernel(const int32_t* __restrict__ lab, Geoms gs, Layout L, const int32_t* sizes, int P,
-            int* status) {
+// boundary histogram of the small segments (of class (lev, cls) when CLASSES)
+// in one 32 x 64 tile, by the block
+template <bool CLASSES>
+__device__ __forceinline__ void pair_tile(const int32_t* __restrict__ lab, const Geoms& gs,
+                                          const Layout& L, const int32_t* sizes, int P, int tile,
+                                          int lev, unsigned cls, int* status) {
   const long long n = gs.total_px;
-  const TileRef tr = tile_ref(gs, blockIdx.x);
+  const TileRef tr = tile_ref(gs, tile);
   const int W = tr.W, H = tr.H;
   // all label loads, then all size gathers, before any pixel is examined:
   // the eight pixels' dependent load pairs overlap instead of serialising
@@ -143,7 +173,7 @@ pair_kernel(const int32_t* __restrict__ lab, Geoms gs, Layout L, const int32_t* 
 #pragma unroll
   for (int j = 0; j < kPer; ++j) sz[j] = (seg[j] >= 0 && seg[j] < n) ? __ldg(sizes + seg[j]) : P;
   for (int j = 0; j < kPer; ++j) {
-    if (sz[j] >= P) continue;
+    if (sz[j] >= P || (CLASSES && seg_class(seg[j], lev) != cls)) continue;
     const int q = threadIdx.x + j * kThreads;
     const int x = tr.tx0 + q % kTileW, y = tr.ty0 + q / kTileW;
     const int s = seg[j];
@@ -169,9 +199,16 @@ pair_kernel(const int32_t* __restrict__ lab, Geoms gs, Layout L, const int32_t* 
       for (int b = 0; b < a; ++b) first &= (t[b] != t[a]);
       if (!first) continue;
       for (int b = a + 1; b < nt; ++b) m += (t[b] == t[a]);
-      insert(L, s, t[a], m, status);
+      insert(L, s, t[a], m);
     }
   }
+}
+
+// boundary histogram of small segments, one block per 32 x 64 tile
+__global__ void __launch_bounds__(kThreads, 4)
+pair_kernel(const int32_t* __restrict__ lab, Geoms gs, Layout L, const int32_t* sizes, int P,
+            int* status) {
+  pair_tile<false>(lab, gs, L, sizes, P, blockIdx.x, 0, 0u, status);
 }
 
 __device__ __forceinline__ float seg_mean(const Layout& L, const int32_t* sizes, int s) {
@@ -269,12 +306,140 @@ __device__ void cleanup_phase(const Layout& L) {
   }
 }
 
+// ---- overflow path -----------------------------------------------------
+// empties the table slots listed in the claimed-slot list
+__device__ void clear_table(const Layout& L) {
+  const unsigned cnt = *(volatile unsigned*)&L.state->list_count;
+  for (unsigned j = blockIdx.x * blockDim.x + threadIdx.x; j < cnt; j += gridDim.x * blockDim.x) {
+    const int h = L.list[j];
+    L.keys[h] = 0ull;
+    L.counts[h] = 0u;
+  }
+}
+
+// decisions of one round, also listing the decided segments
+__device__ void decide_list_phase(const Layout& L, int policy) {
+  const unsigned cnt = *(volatile unsigned*)&L.state->list_count;
+  for (unsigned j = blockIdx.x * blockDim.x + threadIdx.x; j < cnt; j += gridDim.x * blockDim.x) {
+    const unsigned long long k = L.keys[L.list[j]];
+    const int s = key_s(k), t = key_t(k);
+    if (bid_target(L.best[s], policy) == t) {
+      L.map[s] = t;
+      L.dec[atomicAdd(&L.state->dec_count, 1u)] = s;
+    }
+  }
+}
+
+__device__ void cycle_dec_phase(const Layout& L, const int32_t* sizes, int P) {
+  const unsigned cnt = *(volatile unsigned*)&L.state->dec_count;
+  for (unsigned j = blockIdx.x * blockDim.x + threadIdx.x; j < cnt; j += gridDim.x * blockDim.x) {
+    const int s = L.dec[j];
+    const int t = *(volatile int*)(L.map + s);
+    if (next_of(L, sizes, P, t) == s && s > t) *(volatile int*)(L.map + s) = s;
+  }
+}
+
+__device__ void resolve_dec_phase(const Layout& L, const int32_t* sizes, int P, int* status) {
+  const unsigned cnt = *(volatile unsigned*)&L.state->dec_count;
+  for (unsigned j = blockIdx.x * blockDim.x + threadIdx.x; j < cnt; j += gridDim.x * blockDim.x) {
+    const int s = L.dec[j];
+    int r = s;
+    unsigned steps = 0;
+    for (;;) {
+      const int nx = next_of(L, sizes, P, r);
+      if (nx == r) break;
+      r = nx;
+      if (++steps > kChainCap) {
+        set_status(status, SPLIT_ERR_NOT_CONVERGED);
+        break;
+      }
+    }
+    L.fin[s] = r;
+  }
+}
+
+// The pair pass overflowed: decide class by class (see the top of the file).
+// Runs inside the cooperative decision launch; every phase sits behind a
+// bounded grid barrier and the round count is bounded.
+__device__ void overflow_path(const Layout& L, const int32_t* lab, const Geoms& gs,
+                              const int32_t* sizes, int P, int policy,
+                              unsigned long long stamp) {
+  WsHeader* h = L.hdr;
+  State* st = L.state;
+  const bool lead = blockIdx.x == 0 && threadIdx.x == 0;
+  clear_table(L);
+  if (!grid_barrier(h)) return;
+  if (lead) {
+    st->list_count = 0;
+    st->overflow = 0;
+    st->dec_count = 0;
+    L.stack[0] = 2;            // the two halves of level 1
+    L.stack[1] = 1, L.stack[2] = 1;
+    L.stack[3] = 1, L.stack[4] = 0;
+  }
+  if (!grid_barrier(h)) return;
+  __shared__ int lev, cls;
+  for (unsigned round = 0;; ++round) {
+    if (threadIdx.x == 0) {
+      const int depth = *(volatile int*)L.stack;
+      lev = depth > 0 && round < kRoundCap ? *(volatile int*)(L.stack + 2 * depth - 1) : -1;
+      cls = depth > 0 ? *(volatile int*)(L.stack + 2 * depth) : 0;
+    }
+    __syncthreads();
+    if (lev < 0) break;   // the same decision in every block
+    for (int t = blockIdx.x; t < gs.total_tiles; t += gridDim.x)
+      pair_tile<true>(lab, gs, L, sizes, P, t, lev, (unsigned)cls, &h->status);
+    if (!grid_barrier(h)) return;
+    const bool split = *(volatile int*)&st->overflow != 0;
+    if (!split) {
+      bid_phase(L, sizes, policy);
+      if (!grid_barrier(h)) return;
+      decide_list_phase(L, policy);
+      if (!grid_barrier(h)) return;
+    }
+    clear_table(L);
+    if (!grid_barrier(h)) return;
+    if (lead) {
+      int depth = L.stack[0] - 1;   // pop (lev, cls)
+      if (split) {
+        if (lev >= 31 || depth + 2 > kStackCap) {
+          set_status(&h->status, SPLIT_ERR_OVERFLOW);
+          depth = 0;
+        } else {
+          L.stack[1 + 2 * depth] = lev + 1, L.stack[2 + 2 * depth] = 2 * cls + 1;
+          L.stack[3 + 2 * depth] = lev + 1, L.stack[4 + 2 * depth] = 2 * cls;
+          depth += 2;
+        }
+      }
+      L.stack[0] = depth;
+      st->list_count = 0;
+      st->overflow = 0;
+      if (round + 1 >= kRoundCap) set_status(&h->status, SPLIT_ERR_NOT_CONVERGED);
+    }
+    if (!grid_barrier(h)) return;
+  }
+  cycle_dec_phase(L, sizes, P);
+  if (!grid_barrier(h)) return;
+  resolve_dec_phase(L, sizes, P, &h->status);
+  if (!grid_barrier(h)) return;
+  const unsigned cnt = *(volatile unsigned*)&st->dec_count;
+  for (unsigned j = blockIdx.x * blockDim.x + threadIdx.x; j < cnt; j += gridDim.x * blockDim.x)
+    L.best[L.dec[j]] = 0ull;
+  if (lead) h->stamp = stamp;
+}
+
 // The decision over the pair list, one cooperative launch (one block per
 // SM): bids, decisions, mutual-pair fix, chains, cleanup, each phase behind a
 // bounded grid barrier.  The last step records the layout the guard cleared for.
+// When the pair pass overflowed, the overflow path decides instead.
 __global__ void __launch_bounds__(kThreads)
-list_kernel(Layout L, const int32_t* sizes, int P, int policy, unsigned long long stamp) {
+list_kernel(Layout L, const int32_t* lab, Geoms gs, const int32_t* sizes, int P, int policy,
+            unsigned long long stamp) {
   WsHeader* h = L.hdr;
+  if (*(volatile int*)&L.state->overflow) {   // set before this launch: the same in every block
+    overflow_path(L, lab, gs, sizes, P, policy, stamp);
+    return;
+  }
   bid_phase(L, sizes, policy);
   if (!grid_barrier(h)) return;
   decide_phase(L, policy);
@@ -309,6 +474,8 @@ __global__ void guard_kernel(WsHeader* h, unsigned long long stamp, Layout L, lo
     st->unsorted = 0;
     st->list_count = 0;
     st->cap_log2 = L.cap_log2;
+    st->overflow = 0;
+    st->dec_count = 0;
     h->barrier_count = 0;
   }
   if (*(volatile const unsigned long long*)&h->stamp == stamp) return;
@@ -395,7 +562,9 @@ static int merge_run(int32_t* labels, const Geoms& gs, int P, int policy, const 
     unsigned long long stamp_arg = stamp;
     int P_arg = P, policy_arg = policy;
     const int32_t* sizes_arg = sizes;
-    void* args[] = {&l, &sizes_arg, &P_arg, &policy_arg, &stamp_arg};
+    const int32_t* lab_arg = labels;
+    Geoms gs_arg = gs;
+    void* args[] = {&l, &lab_arg, &gs_arg, &sizes_arg, &P_arg, &policy_arg, &stamp_arg};
     SG_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)mrg::list_kernel, dim3(di.sm_count),
                                             dim3(mrg::kThreads), args, 0, st));
   }

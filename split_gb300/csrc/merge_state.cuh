@@ -15,7 +15,9 @@ struct State {
   unsigned list_count;   // occupied table slots
   int cap_log2;
   int n;                 // pixels (segment ids lie in [0, n))
-  int pad[8];
+  int overflow;          // the pair pass found the table full (see split_round)
+  unsigned dec_count;    // decided segments of the rounds (overflow path)
+  int pad[6];
 };
 
 // Final label of a pixel whose pre-merge label is v.  Small segments take the

@@ -1,98 +1,79 @@
-"""Continuous-batching server for the segmentation path.
+"""Continuous-batching server for the segmentation path: a binding of the C++
+server (split_server_* in include/split_gb300.h).
 
 Requests (an RGB8 image plus its K, iteration count and initial centroids)
-arrive open-loop.  The loop admits them in arrival order while their device
-footprint fits the HBM budget, packs every admitted request into the next
-batch (one fixed launch sequence for the batch, split_batch_*), and keeps up
-to two batches in flight: while one batch computes, the host admits new
-arrivals and stages the next batch's inputs with asynchronous copies from
-pinned memory.  Each in-flight slot owns a resident arena (RGB, centroid,
-label, normal and workspace buffers, union-find and merge state included)
-that every batch of that slot binds to, so serving allocates no device
-memory once the arenas have grown to the largest batch.  A request completes
-when its batch's results are back in host memory; its latency runs from its
+arrive open-loop.  The server's worker thread admits them in arrival order
+while their device footprint fits the HBM budget, packs every admitted
+request into the next batch (split_batch_*), and keeps up to `depth` batches
+in flight, with uploads, compute and downloads on three streams.  Each
+in-flight slot owns a resident arena that its batches bind to, so serving
+allocates no device memory once the arenas have grown (reserve()).  A request
+completes when its results are in host memory; its latency runs from its
 arrival.
 
-Each request's result is independent of what shares its batch (per-image
-tiles, reduction trees and label spaces), so a result served in a mix equals
-the same request served alone.
+Each request's result is independent of what shares its batch, so a result
+served in a mix equals the same request served alone.
 """
 from __future__ import annotations
 
-import collections
+import ctypes as C
 import dataclasses
 import time
 
 import numpy as np
 
-# device bytes held per pixel of a batch: RGB8 arena (3), float4 features (16),
-# three int32 label arenas and sizes (16), normals (12), merge state and hash
-# table (44), k-means and tile tables (< 1)
-BYTES_PER_PIXEL = 92
+from . import _native as N
 
 
 @dataclasses.dataclass
 class Request:
     rid: int
-    rgb: np.ndarray          # (H, W, 3) uint8
+    rgb: object              # (H, W, 3) uint8: numpy array or (pinned) torch tensor
     nclusters: int
     iters: int
-    centroids: np.ndarray    # (dim, K) float32 initial centroids
+    centroids: object        # (dim, K) float32 initial centroids
     arrival: float = 0.0     # seconds on the server clock
-    admitted: float | None = None
+    admitted: float | None = None   # when it was handed to the server
     done: float | None = None
     segment_labels: np.ndarray | None = None
     centroids_out: np.ndarray | None = None
 
     @property
-    def pixels(self) -> int:
-        return self.rgb.shape[0] * self.rgb.shape[1]
+    def shape(self):
+        return tuple(self.rgb.shape[:2])
 
     @property
-    def footprint(self) -> int:
-        return (self.pixels + 63) // 64 * 64 * BYTES_PER_PIXEL
+    def pixels(self) -> int:
+        h, w = self.shape
+        return h * w
 
 
-class Admission:
-    """FIFO admission under a byte budget (no GPU: unit-testable on CPU)."""
+def footprint(pixels: int, bytes_per_pixel: int) -> int:
+    """Device bytes a request of `pixels` holds while admitted (the arena
+    starts every image on 64 pixels)."""
+    return (pixels + 63) // 64 * 64 * bytes_per_pixel
 
-    def __init__(self, budget_bytes: int):
-        self.budget = int(budget_bytes)
-        self.in_use = 0
-        self.waiting: collections.deque[Request] = collections.deque()
-        self.admitted: list[Request] = []
 
-    def arrive(self, req: Request) -> None:
-        if req.footprint > self.budget:
-            raise ValueError(f"request {req.rid} needs {req.footprint} B, budget {self.budget} B")
-        self.waiting.append(req)
+def bytes_per_pixel(params) -> int:
+    cp = params.c()
+    return int(N.load().split_server_bytes_per_pixel(C.byref(cp)))
 
-    def admit(self, now: float) -> int:
-        n = 0
-        while self.waiting and self.in_use + self.waiting[0].footprint <= self.budget:
-            r = self.waiting.popleft()
-            r.admitted = now
-            self.in_use += r.footprint
-            self.admitted.append(r)
-            n += 1
-        return n
 
-    def take(self, max_pixels: int | None = None) -> list[Request]:
-        """Hand the admitted requests (in order) to the next batch."""
-        out, keep, px = [], [], 0
-        for r in self.admitted:
-            if max_pixels is None or px + r.pixels <= max_pixels or not out:
-                out.append(r)
-                px += r.pixels
-            else:
-                keep.append(r)
-        self.admitted = keep
-        return out
-
-    def release(self, reqs) -> None:
-        for r in reqs:
-            self.in_use -= r.footprint
-        assert self.in_use >= 0
+def admission_plan(footprints, pixels, budget: int, max_batch_pixels: int, depth: int):
+    """The C++ server's admission and batch-formation policy on the host
+    alone: requests arriving at once -> (batch index of each request, number
+    of batches, peak bytes in use)."""
+    n = len(footprints)
+    fp = np.ascontiguousarray(footprints, np.int64)
+    px = np.ascontiguousarray(pixels, np.int64)
+    out = np.full(n, -1, np.int32)
+    peak = C.c_int64(0)
+    nb = N.load().split_server_admission_test(
+        C.c_void_p(fp.ctypes.data), C.c_void_p(px.ctypes.data), n, budget, max_batch_pixels,
+        depth, C.c_void_p(out.ctypes.data), C.byref(peak))
+    if nb < 0:
+        raise N.SplitError(-nb, "admission_plan")
+    return out, nb, peak.value
 
 
 def percentile(values, q):
@@ -105,26 +86,10 @@ def percentile(values, q):
     return v[lo] + (v[hi] - v[lo]) * (k - lo)
 
 
-
-
-class _Flight:
-    """One batch between launch and the host seeing its results."""
-
-    def __init__(self, reqs, batch, done, labels_h, cents_h):
-        self.reqs, self.batch, self.done = reqs, batch, done
-        self.labels_h, self.cents_h = labels_h, cents_h
-
-
 class Server:
-    """Serves requests through split_batch on one CUDA device.
-
-    Three streams: uploads of the next batch (host to device), the batch
-    launch sequence itself, and downloads of finished results.  All batches
-    compute on the one compute stream, so the k-means kernel, a cooperative
-    grid that fills the GPU, never shares the GPU with another batch's; the
-    copy streams overlap both directions of PCIe/C2C traffic with it.
-    `depth` bounds the batches launched but not yet collected.
-    """
+    """A split_server on one CUDA device.  keep_results: each request gets
+    result buffers of its own (otherwise requests that share an input image
+    share output buffers, for timing runs)."""
 
     def __init__(self, params=None, budget_bytes: int = 40 << 30,
                  max_batch_pixels: int = 64 << 20, depth: int = 2, device=None,
@@ -135,144 +100,118 @@ class Server:
         self.params = params or Params()
         self.device = torch.device("cuda", torch.cuda.current_device()) if device is None \
             else torch.device(device)
-        self.admission = Admission(budget_bytes)
-        self.max_batch_pixels = max_batch_pixels
-        self.depth = depth
         self.keep_results = keep_results
-        self.h2d = torch.cuda.Stream(self.device)
-        self.compute = torch.cuda.Stream(self.device)
-        self.d2h = torch.cuda.Stream(self.device)
-        self.inflight: collections.deque[_Flight] = collections.deque()
+        self.depth = depth
+        cfg = N.ServerConfig(self.params.c(), budget_bytes, max_batch_pixels, depth,
+                             self.device.index or 0)
+        self._h = C.c_void_p()
+        N.check(N.load().split_server_create(C.byref(cfg), C.byref(self._h)), "server.create")
         self.completed: list[Request] = []
-        self.batches = 0
-        from .batch import Arena
-        # one resident arena per slot; batch i uses slot i % depth, which the
-        # collection order (oldest first) has freed by the time it launches
-        self.arenas = [Arena(self.device, normals=bool(self.params.compute_normals))
-                       for _ in range(depth)]
-        self.batch_sizes: list[int] = []
-        self.t0 = time.perf_counter()
+        self._scratch = {}
+        self._batches0 = 0
         if reserve_pixels > 0:
             self.reserve(reserve_pixels)
 
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            N.load().split_server_destroy(h)
+            self._h = None
+
     def reserve(self, pixels: int, max_requests: int = 4096) -> None:
-        """Grow every arena up front to hold a batch of `pixels` pixels (so a
-        timed serving run allocates nothing)."""
-        from .batch import Batch
-        side = 8192
-        probe = Batch([(side, max(1, (pixels + side - 1) // side), 64, 1)], self.params,
-                      self.device, arena=self.arenas[0])
-        wsb = probe.ws.nbytes
-        del probe
-        for a in self.arenas:
-            a.ensure(pixels + 64 * max_requests, self.params.dim * 64 * max_requests, wsb)
-            if not self.keep_results:
-                a.host_buffers()
+        """Grow every slot's arena up front to hold a batch of `pixels` pixels
+        (so a timed serving run allocates nothing)."""
+        N.check(N.load().split_server_reserve(self._h, pixels, max_requests), "server.reserve")
 
-    def now(self) -> float:
-        return time.perf_counter() - self.t0
+    def counters(self) -> N.ServerCounters:
+        c = N.ServerCounters()
+        N.check(N.load().split_server_stats(self._h, C.byref(c)), "server.stats")
+        return c
 
-    def _host(self, a):
+    @property
+    def batch_sizes(self) -> list[float]:
+        """Mean requests per batch since the last serve() started (one entry
+        per batch, for compatibility with per-batch lists)."""
+        c = self.counters()
+        nb = int(c.batches) - self._batches0
+        n = len(self.completed)
+        return [n / nb] * nb if nb else []
+
+    def _pinned(self, a, dtype):
         t = self.torch
         if isinstance(a, t.Tensor):
-            return a
-        return t.from_numpy(np.ascontiguousarray(a))
+            if a.is_pinned():
+                return a.contiguous()
+            return a.contiguous().pin_memory()
+        return t.from_numpy(np.ascontiguousarray(a, dtype=dtype)).pin_memory()
 
-    def _launch(self, reqs) -> None:
-        torch = self.torch
-        from .batch import Batch
-        shapes = [(r.rgb.shape[1], r.rgb.shape[0], r.nclusters, r.iters) for r in reqs]
-        with torch.cuda.stream(self.h2d):
-            b = Batch(shapes, self.params, self.device, stream=self.h2d,
-                      arena=self.arenas[self.batches % self.depth])
-            for i, r in enumerate(reqs):
-                b.rgb_of(i).copy_(self._host(r.rgb), non_blocking=True)
-                b.centroids_of(i).copy_(self._host(r.centroids), non_blocking=True)
-            up = torch.cuda.Event()
-            up.record(self.h2d)
-        self.compute.wait_event(up)
-        b.run(self.compute)
-        ran = torch.cuda.Event()
-        ran.record(self.compute)
-        self.d2h.wait_event(ran)
-        with torch.cuda.stream(self.d2h):
-            if self.keep_results:
-                # results outlive the batch: buffers of their own
-                labels_h = torch.empty(b.segment_labels.shape, dtype=torch.int32,
-                                       pin_memory=True)
-                cents_h = torch.empty(b.centroids.shape, dtype=torch.float32, pin_memory=True)
-            else:
-                # the slot's buffers, pinned once (the slot is reused only
-                # after this batch has been collected)
-                lh, ch = self.arenas[self.batches % self.depth].host_buffers()
-                labels_h = lh[:b.segment_labels.numel()].view(b.segment_labels.shape)
-                cents_h = ch[:b.centroids.numel()].view(b.centroids.shape)
-            labels_h.copy_(b.segment_labels, non_blocking=True)
-            cents_h.copy_(b.centroids, non_blocking=True)
-            done = torch.cuda.Event()
-            done.record(self.d2h)
-        self.inflight.append(_Flight(reqs, b, done, labels_h, cents_h))
-        self.batches += 1
-        self.batch_sizes.append(len(reqs))
-
-    def _finish(self, f: _Flight) -> None:
-        t = self.now()
-        b = f.batch
-        b.ws.check("serve: batch")
-        for i, r in enumerate(f.reqs):
-            r.done = t
-            if self.keep_results:
-                # views of the batch's pinned download buffers (no host copy)
-                o = b.offsets[i]
-                h, w = r.rgb.shape[:2]
-                r.segment_labels = f.labels_h[o:o + w * h].numpy().reshape(h, w)
-                co = b.coffsets[i]
-                r.centroids_out = f.cents_h[co:co + self.params.dim * r.nclusters].numpy() \
-                    .reshape(self.params.dim, r.nclusters)
-        self.admission.release(f.reqs)
-        self.completed.extend(f.reqs)
-
-    def _collect(self, block: bool) -> bool:
-        """Finish the oldest batches whose results are home; with block, wait
-        for the oldest one.  Returns whether anything finished."""
-        got = False
-        while self.inflight:
-            f = self.inflight[0]
-            if not f.done.query():
-                if not block or got:
-                    break
-                f.done.synchronize()
-            self.inflight.popleft()
-            self._finish(f)
-            got = True
-        return got
+    def _outputs(self, r: Request):
+        t = self.torch
+        h, w = r.shape
+        key = (id(r.rgb), h, w, r.nclusters)
+        if not self.keep_results and key in self._scratch:
+            return self._scratch[key]
+        out = (t.empty((h, w), dtype=t.int32, pin_memory=True),
+               t.empty((self.params.dim, r.nclusters), dtype=t.float32, pin_memory=True))
+        if not self.keep_results:
+            self._scratch[key] = out
+        return out
 
     def serve(self, requests, realtime: bool = True):
-        """Serve `requests`.  With realtime each request becomes visible at its
-        `arrival` (seconds after the call starts); otherwise all are visible
-        at once.  Returns the requests in completion order."""
-        pending = collections.deque(sorted(requests, key=lambda r: r.arrival))
-        total = len(pending) + len(self.completed)
-        self.t0 = time.perf_counter()
-        if not realtime:
-            for r in pending:
+        """Serve `requests`.  With realtime each request is submitted at its
+        `arrival` (seconds after the call starts); otherwise all at once.
+        Returns the requests in completion order."""
+        lib = N.load()
+        pending = sorted(requests, key=lambda r: r.arrival)
+        prepared = []
+        for r in pending:
+            if not realtime:
                 r.arrival = 0.0
-        while len(self.completed) < total:
-            now = self.now()
-            while pending and pending[0].arrival <= now:
-                self.admission.arrive(pending.popleft())
-            self.admission.admit(now)
-            self._collect(block=False)
-            if self.admission.admitted and len(self.inflight) < self.depth:
-                self._launch(self.admission.take(self.max_batch_pixels))
-                continue
-            if self.inflight and (len(self.inflight) >= self.depth or not pending):
-                self._collect(block=True)
-            elif pending:
-                # nothing to launch: wait for the next arrival, polling the
-                # in-flight batches meanwhile
-                time.sleep(min(2e-4, max(0.0, pending[0].arrival - now)))
-        self.torch.cuda.synchronize()
+            rgb = self._pinned(r.rgb, np.uint8)
+            c0 = self._pinned(r.centroids, np.float32)
+            lab, cout = self._outputs(r)
+            h, w = r.shape
+            req = N.ServerRequest(rgb.data_ptr(), w, h, r.nclusters, r.iters, c0.data_ptr(),
+                                  lab.data_ptr(), cout.data_ptr(), None, None, None)
+            prepared.append((r, req, rgb, c0, lab, cout))
+        self._batches0 = int(self.counters().batches)
+        self.completed = []
+        by_ticket = {}
+        comp = (N.Completion * 64)()
+        got = C.c_int(0)
+        t0 = time.perf_counter()
+
+        def drain(timeout_ms: int) -> None:
+            N.check(lib.split_server_poll(self._h, comp, 64, timeout_ms, C.byref(got)),
+                    "server.poll")
+            for i in range(got.value):
+                c = comp[i]
+                r, lab, cout = by_ticket.pop(int(c.ticket))
+                if c.status != N.OK:
+                    raise N.SplitError(c.status, f"serve: request {r.rid}")
+                r.done = r.admitted + c.latency_ms * 1e-3
+                r.segment_labels = lab.numpy()
+                r.centroids_out = cout.numpy()
+                self.completed.append(r)
+
+        ticket = C.c_uint64(0)
+        for r, req, _rgb, _c0, lab, cout in prepared:
+            while realtime:
+                wait = r.arrival - (time.perf_counter() - t0)
+                if wait <= 0:
+                    break
+                if by_ticket:
+                    drain(max(0, min(int(wait * 1e3), 1)))
+                else:
+                    time.sleep(min(wait, 1e-3))
+            r.admitted = time.perf_counter() - t0
+            N.check(lib.split_server_submit(self._h, C.byref(req), C.byref(ticket)),
+                    f"serve: submit {r.rid}")
+            by_ticket[int(ticket.value)] = (r, lab, cout)
+            drain(0)
+        while by_ticket:
+            drain(100)
+        self._keep = prepared   # host buffers stay alive with the results
         return self.completed
 
     @staticmethod

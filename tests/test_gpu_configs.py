@@ -117,8 +117,10 @@ def test_4k_frame_pipeline_parity(cuda):
     # integer stages: bit-exact against the oracle given the device's labels
     cl = pipe.cluster_labels.cpu().numpy().reshape(h, w)
     seg = oracle.ccl(cl, 8, 0)
+    # (with xy in the features the 16 clusters are 16 compact regions, none
+    # below 256 px: the merge leaves them as they are on this frame; the
+    # merge's decisions are exercised by the 512 x 512 case below)
     merged = oracle.merge_small(seg, 256, 0)
-    assert len(np.unique(merged)) < len(np.unique(seg))        # the merge did something
     want = oracle.erode(merged, 1)
     got = pipe.segment_labels.cpu().numpy()
     assert np.array_equal(got, want), f"{int((got != want).sum())} segment labels differ"

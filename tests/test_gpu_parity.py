@@ -268,16 +268,23 @@ def test_workspace_reuse_across_sizes(cuda):
 
 
 # ---------------------------------------------------------------- edge cases
-@pytest.mark.parametrize("radius", [5, 8, 16])
+@pytest.mark.parametrize("radius", [5, 8, 16, 17, 29, 40])
 def test_erode_large_radius(cuda, radius):
+    """Up to 16 in one kernel pass; beyond that the binding runs passes of at
+    most 16 (out-of-place and in place, as the reference's erode(labels, n))."""
     import torch
     from split_gb300 import morph
     rng = np.random.default_rng(radius)
-    lab = rng.integers(0, 3, size=(12, 15)).repeat(23, 0).repeat(19, 1)[:270, :277]
+    lab = rng.integers(0, 3, size=(12, 15)).repeat(41, 0).repeat(37, 1)[:470, :537]
     lab = np.ascontiguousarray(lab).astype(np.int32)
-    out = morph.erode(_t(lab, cuda), radius, out=torch.empty(lab.shape, dtype=torch.int32,
-                                                            device=cuda))
-    assert np.array_equal(out.cpu().numpy(), oracle.erode(lab, radius))
+    want = oracle.erode(lab, radius)
+    assert (want >= 0).any()
+    d = _t(lab, cuda)
+    out = morph.erode(d, radius, out=torch.empty(lab.shape, dtype=torch.int32, device=cuda))
+    assert np.array_equal(out.cpu().numpy(), want)
+    assert np.array_equal(d.cpu().numpy(), lab)          # the input is left alone
+    morph.erode(d, radius)                                 # in place
+    assert np.array_equal(d.cpu().numpy(), want)
 
 
 @pytest.mark.parametrize("fill", ["uniform", "checker"])
@@ -545,3 +552,36 @@ def test_pipeline_reference_chroma_merge(cuda):
     # and the rule is the chroma one, not the boundary one
     assert not np.array_equal(merged, oracle.merge_small(seg, 48, 0))
     assert np.array_equal(pipe.segment_labels.cpu().numpy(), oracle.erode(merged, 1))
+
+
+@pytest.mark.parametrize("shape,policy", [((2160, 3840), 0), ((311, 97), 0), ((311, 97), 1),
+                                          ((1, 5000), 0)])
+def test_merge_every_pixel_its_own_segment(cuda, shape, policy):
+    """Every pixel its own segment (all smaller than P): about 8 distinct
+    (segment, neighbour) pairs per pixel, far more than the pair table holds
+    at once.  The merge decides the segments in rounds over hash classes and
+    equals the oracle (which sorts every edge), bit for bit; a workspace
+    reused afterwards for a normal image is still exact."""
+    import torch
+    from split_gb300 import ccl
+    h, w = shape
+    rng = np.random.default_rng(h + w)
+    # ids in raster order, or shuffled for the chroma rule (which leaves
+    # labels already in sorted order as they are)
+    ids = np.arange(h * w, dtype=np.int32)
+    lab = (rng.permutation(ids) if policy else ids).astype(np.int32).reshape(h, w)
+    chroma = (rng.integers(0, 256, size=(2, h * w)) / 256.0).astype(np.float32)
+    g = _t(lab, cuda)
+    ws = ccl.merge_small_segments(_t(chroma, cuda) if policy else None, g, None, 4,
+                                  policy=policy)
+    torch.cuda.synchronize()
+    ws.check("merge")
+    want = oracle.merge_small(lab, 4, policy, chroma if policy else None)
+    assert np.array_equal(g.cpu().numpy(), want)
+    # the same workspace on an ordinary image afterwards
+    blk = rng.integers(0, 4, size=(h // 4 + 1, w // 4 + 1)).repeat(4, 0).repeat(4, 1)[:h, :w]
+    seg = oracle.ccl(np.ascontiguousarray(blk).astype(np.int32), 8, 0)
+    g2 = _t(seg, cuda)
+    ccl.merge_small_segments(None, g2, ws, 24, policy=0)
+    ws.check("merge after")
+    assert np.array_equal(g2.cpu().numpy(), oracle.merge_small(seg, 24, 0))

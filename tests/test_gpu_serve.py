@@ -1,9 +1,10 @@
-"""Serving: a request's results are identical whether it is served alone or
-batched with others, and equal the single-image pipeline's."""
+"""Serving through the C++ server (split_server_*): a request's results are
+identical whether it is served alone or batched with others, and equal the
+single-image pipeline's; the HBM budget bounds what is admitted."""
 import numpy as np
 import pytest
 
-from split_gb300 import synth
+import split_synth as synth
 
 pytestmark = pytest.mark.gpu
 
@@ -56,13 +57,19 @@ def test_alone_equals_mix(cuda):
 
 def test_budget_bounds_batches(cuda):
     from split_gb300 import pipeline
-    from split_gb300.serve import Server
+    from split_gb300.serve import Server, bytes_per_pixel, footprint
     params = pipeline.Params(merge_P=64)
     reqs = _requests(params.dim)
-    budget = max(r.footprint for r in reqs) * 2
+    bpp = bytes_per_pixel(params)
+    budget = max(footprint(r.pixels, bpp) for r in reqs) * 2
     s = Server(params, budget_bytes=budget, device=cuda, depth=2)
     done = s.serve(reqs, realtime=False)
     assert sorted(r.rid for r in done) == list(range(len(SHAPES)))
-    assert s.admission.in_use == 0
+    c = s.counters()
+    assert c.in_use_bytes == 0 and 0 < c.peak_in_use_bytes <= budget
+    assert c.bytes_per_pixel == bpp and c.completed == c.submitted == len(SHAPES)
+    # the budget holds all but the largest request at once: it waits for a
+    # later batch
+    assert c.batches >= 2
     for r in done:
         assert r.done >= r.admitted >= r.arrival

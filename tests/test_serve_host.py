@@ -1,59 +1,53 @@
-"""Host logic of the continuous-batching server: admission order, the byte
-budget, batch formation and the latency percentiles (no GPU)."""
+"""Host logic of the continuous-batching server (no GPU): the C++ server's
+admission and batch-formation policy through split_server_admission_test
+(arrival order, the byte budget, the pixel cap), the footprint query, and the
+latency percentiles."""
 import numpy as np
 import pytest
 
-from split_gb300.serve import Admission, Request, percentile, poisson_arrivals, BYTES_PER_PIXEL
-
-
-def _req(rid, w, h, t=0.0):
-    return Request(rid, np.zeros((h, w, 3), np.uint8), 8, 5, np.zeros((5, 8), np.float32), t)
+from split_gb300 import pipeline
+from split_gb300.serve import admission_plan, bytes_per_pixel, footprint, percentile, \
+    poisson_arrivals
 
 
 def test_footprint_rounds_to_arena_granule():
-    assert _req(0, 64, 1).footprint == 64 * BYTES_PER_PIXEL
-    assert _req(0, 65, 1).footprint == 128 * BYTES_PER_PIXEL
+    assert footprint(64, 100) == 64 * 100
+    assert footprint(65, 100) == 128 * 100
+    bpp = bytes_per_pixel(pipeline.Params())
+    # arenas (RGB8, two label planes, normals: 23 B) plus the workspace
+    assert 23 + 16 < bpp < 512
 
 
 def test_admission_is_fifo_under_budget():
-    a = Admission(budget_bytes=_req(0, 64, 64).footprint * 2)
-    reqs = [_req(i, 64, 64) for i in range(5)]
-    for r in reqs:
-        a.arrive(r)
-    assert a.admit(1.0) == 2
-    assert [r.rid for r in a.admitted] == [0, 1]
-    assert a.admit(2.0) == 0
-    batch = a.take()
-    assert [r.rid for r in batch] == [0, 1] and a.admitted == []
-    a.release(batch[:1])
-    assert a.admit(3.0) == 1 and a.admitted[0].rid == 2 and a.admitted[0].admitted == 3.0
-    a.release(batch[1:])
-    a.release(a.take())
-    assert a.in_use == 0
-    # a large request at the head blocks the ones behind it (no overtaking)
-    b = Admission(budget_bytes=_req(0, 64, 64).footprint * 2)
-    b.arrive(_req(10, 64, 64))
-    b.admit(0)
-    b.arrive(_req(11, 64, 128))
-    b.arrive(_req(12, 64, 32))
-    assert b.admit(0) == 0
+    fp = [100] * 5
+    batch, nb, peak = admission_plan(fp, [1] * 5, budget=200, max_batch_pixels=1 << 30, depth=2)
+    # two fit at a time; each batch takes what was admitted, in order
+    assert list(batch) == [0, 0, 1, 1, 2] and nb == 3 and peak <= 200
+    # a large request at the head blocks the ones behind it (no overtaking):
+    # 150 waits for the first batch to finish, and the small one behind it too
+    batch, nb, _ = admission_plan([100, 150, 10], [1, 1, 1], budget=200,
+                                  max_batch_pixels=1 << 30, depth=2)
+    assert list(batch) == [0, 1, 1]
+
+
+def test_in_flight_depth_bounds_batches():
+    batch, nb, _ = admission_plan([1] * 6, [10] * 6, budget=1 << 40, max_batch_pixels=20,
+                                  depth=1)
+    assert list(batch) == [0, 0, 1, 1, 2, 2] and nb == 3
 
 
 def test_oversized_request_rejected():
-    a = Admission(budget_bytes=1000)
-    with pytest.raises(ValueError):
-        a.arrive(_req(0, 64, 64))
+    from split_gb300 import _native
+    with pytest.raises(_native.SplitError):
+        admission_plan([1000], [1], budget=999, max_batch_pixels=1 << 30, depth=2)
 
 
 def test_take_respects_pixel_cap_but_always_progresses():
-    a = Admission(budget_bytes=1 << 40)
-    for i, (w, h) in enumerate([(100, 100), (100, 100), (300, 300), (10, 10)]):
-        a.arrive(_req(i, w, h))
-    a.admit(0)
-    first = a.take(max_pixels=25000)
-    assert [r.rid for r in first] == [0, 1, 3]
-    second = a.take(max_pixels=25000)      # larger than the cap on its own
-    assert [r.rid for r in second] == [2]
+    px = [10000, 10000, 90000, 100]
+    batch, nb, _ = admission_plan([1] * 4, px, budget=1 << 40, max_batch_pixels=25000, depth=8)
+    # the cap skips the large one and takes the small one behind it; the large
+    # one then forms a batch alone
+    assert list(batch) == [0, 0, 1, 0] and nb == 2
 
 
 def test_percentile_matches_numpy_linear():
