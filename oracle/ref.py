@@ -122,6 +122,21 @@ def merge_small_segments(chroma, labels, P):
     return a
 
 
+def merge_smooth_boundaries(points, labels, nsegments, threshold=0.01):
+    """merge_smooth_boundaries (merge_smooth_boundaries.cu:134-243): points
+    planar (3, N) float32, labels (H, W) compressed to [0, nsegments)."""
+    p = np.ascontiguousarray(points, np.float32)
+    a = np.ascontiguousarray(labels, np.int32).copy()
+    h, w = a.shape
+    lib = load()
+    lib.ref_merge_smooth_boundaries.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int,
+                                                C.c_int, C.c_float]
+    lib.ref_merge_smooth_boundaries.restype = C.c_int
+    with quiet():
+        lib.ref_merge_smooth_boundaries(_p(p), _p(a), w, h, int(nsegments), float(threshold))
+    return a
+
+
 def erode(labels, niter=1):
     a = np.ascontiguousarray(labels, np.int32).copy()
     h, w = a.shape

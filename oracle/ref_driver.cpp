@@ -18,6 +18,7 @@
 #include "split/device/detail/unary_functional.cuh"
 #include "split/device/ccl/connected_components.cuh"
 #include "split/device/ccl/merge_small_segments.cuh"
+#include "split/device/ccl/merge_smooth_boundaries.cuh"
 #include "split/device/kmeans/centroids.cuh"
 #include "split/device/kmeans/cluster.cuh"
 #include "split/device/kmeans/label.cuh"
@@ -141,6 +142,24 @@ int ref_merge_small_segments(const float* chroma, int32_t* labels, int w, int h,
   for (std::size_t i = 0; i < n; ++i) mx = std::max(mx, (int)labels[i]);
   Temp t(split::device::ccl::merge_small_segments_workspace((int)n, mx + 1));
   split::device::ccl::merge_small_segments(Ch, L, t.p, P);
+  to_host(L, labels, n);
+  return 0;
+}
+
+// merge_smooth_boundaries (merge_smooth_boundaries.cu:134-243, staged with
+// the one-token reduction fix recorded in refbuild.py).  labels: h x w,
+// compressed to [0, nsegments); points: planar 3 x n features.  Its
+// workspace query takes the edge count, which only the call itself learns:
+// the bound 8 n (every pixel's eight neighbours) is passed.
+int ref_merge_smooth_boundaries(const float* pts, int32_t* labels, int w, int h, int nsegments,
+                                float threshold) {
+  const std::size_t n = (std::size_t)w * h;
+  Mat P(3, n);
+  IMat L(h, w);
+  to_dev(P, pts, 3 * n);
+  to_dev(L, labels, n);
+  Temp t(split::device::ccl::merge_smooth_boundaries_workspace((int)n, nsegments, (int)(8 * n)));
+  split::device::ccl::merge_smooth_boundaries(P, nsegments, L, t.p, threshold);
   to_host(L, labels, n);
   return 0;
 }

@@ -14,7 +14,10 @@ it is committed):
   1. member ``x.get<N>()`` becomes ``thrust::get<N>(x)``: CCCL 3's
      thrust::tuple is cuda::std::tuple, which has no member get;
   2. oracle/ref_prelude.h is force-included (host min/max, stand-ins that let
-     g++ parse the one never-launched kernel).
+     g++ parse the one never-launched kernel);
+  3. merge_smooth_boundaries.cu:216-226 gets thrust::minimum instead of the
+     predicate thrust::less as its reduction (PATCHES below): as written the
+     file does not compile, and its comment says it takes the smallest value.
 When the copied sources are present but the reference is not (another
 machine), the copies are compiled as they are.
 """
@@ -64,11 +67,21 @@ SOURCES = [
     "split/src/split/device/sfs/sobel_normals.cu",
     "split/src/split/device/detail/normalize_vectors.cu",
     "split/src/split/device/color/beta_feature.cu",
+    "split/src/split/device/ccl/merge_smooth_boundaries.cu",
 ]
 
 # Headers a source used through includes of the Thrust / CUSP versions it was
 # written against (added to that file's staged copy only).
 EXTRA_INCLUDES = {"beta_feature.cu": ("thrust/extrema.h",)}
+
+# One-token fixes without which a source does not compile, applied to its
+# staged copy only:
+#   merge_smooth_boundaries.cu:216-226 hands reduce_by_key the predicate
+#   thrust::less as its reduction ("If we are faced with multiple options, we
+#   take the smallest scalar"); the functor that takes the smaller value is
+#   thrust::minimum, which is what the comment describes.
+PATCHES = {"merge_smooth_boundaries.cu": (("thrust::less<thrust::tuple<real, int>>()",
+                                           "thrust::minimum<thrust::tuple<real, int>>()"),)}
 
 _GET = re.compile(r"\.get<(\d+)>\(\)")
 _IDENT = re.compile(r"[A-Za-z0-9_]")
@@ -146,6 +159,10 @@ def stage_sources(verbose: bool = False) -> bool:
         with open(os.path.join(REF_ROOT, rel)) as f:
             text = f.read()
         extra = "".join(f"#include <{h}>\n" for h in EXTRA_INCLUDES.get(os.path.basename(rel), ()))
+        for old, new in PATCHES.get(os.path.basename(rel), ()):
+            if text.count(old) != 1:
+                raise RuntimeError(f"{rel}: the patched expression is not there once")
+            text = text.replace(old, new)
         with open(dst, "w") as f:
             f.write(extra + rewrite_get(text))
     for root, _, files in os.walk(os.path.join(SRC, "include")):

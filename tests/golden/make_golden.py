@@ -10,6 +10,7 @@ so a generator change is caught.
     python tests/golden/make_golden.py lab_beta   # lab_beta_golden.npz
     python tests/golden/make_golden.py ic         # ic_golden.npz
     python tests/golden/make_golden.py threshold  # kmeans_threshold_golden.npz
+    python tests/golden/make_golden.py smooth     # smooth_golden.npz
 
 Known limit of the CPU build: CCCL 3.0.1's host sort orders negative int keys
 after non-negative ones, so compress_labels is only recorded on non-negative
@@ -31,6 +32,8 @@ OUT = os.path.join(HERE, "reference_golden.npz")
 OUT_LAB = os.path.join(HERE, "lab_beta_golden.npz")
 OUT_IC = os.path.join(HERE, "ic_golden.npz")
 OUT_THR = os.path.join(HERE, "kmeans_threshold_golden.npz")
+OUT_SMOOTH = os.path.join(HERE, "smooth_golden.npz")
+SMOOTH_THRESHOLDS = (0.01, 0.03, 0.1)
 THRESHOLDS = (1e-3, 1e-2, 0.0145)
 
 
@@ -91,6 +94,37 @@ def main_ic():
     ic = ref.rgb_to_ic(synth.features(rgb, 3))
     np.savez_compressed(OUT_IC, rgb_sha=sha(rgb), ic=ic)
     print(f"wrote {OUT_IC}")
+
+
+def smooth_inputs():
+    """Segments and features for the smooth-boundary merge: a Voronoi image
+    with gentle noise; segments are the 8-connected components of its colours
+    quantised to 3 bits per channel, compressed to [0, S); features are the
+    colours scaled to [0, 100].  Returns (rgb, labels (H, W), points (3, N),
+    S)."""
+    import oracle
+    from split_gb300 import synth
+    rgb = synth.voronoi_rgb8(0x56, 160, 120, 40, sigma=2.0)
+    q = (rgb // 32).astype(np.int32)
+    cls = q[..., 0] * 64 + q[..., 1] * 8 + q[..., 2]
+    seg = oracle.ccl(cls, 8, 0)
+    lab, s = oracle.compress_labels(seg)
+    pts = synth.features(rgb, 3) * np.float32(100.0)
+    return rgb, lab.reshape(seg.shape), np.ascontiguousarray(pts, np.float32), s
+
+
+def main_smooth():
+    """merge_smooth_boundaries of the reference (merge_smooth_boundaries.cu:
+    134-243, built with the one-token reduction fix recorded in
+    oracle/refbuild.py) at a few thresholds."""
+    from oracle import ref
+    rgb, lab, pts, s = smooth_inputs()
+    g = {"rgb_sha": np.array(sha(rgb)), "labels_sha": np.array(sha(lab)),
+         "nsegments": np.array(s), "thresholds": np.array(SMOOTH_THRESHOLDS)}
+    for i, t in enumerate(SMOOTH_THRESHOLDS):
+        g[f"merged_{i}"] = ref.merge_smooth_boundaries(pts, lab, s, t)
+    np.savez_compressed(OUT_SMOOTH, **g)
+    print(f"wrote {OUT_SMOOTH} ({os.path.getsize(OUT_SMOOTH) / 1024:.0f} KiB)")
 
 
 def main_threshold():
@@ -155,5 +189,7 @@ elif __name__ == "__main__" and sys.argv[1:] == ["ic"]:
     main_ic()
 elif __name__ == "__main__" and sys.argv[1:] == ["threshold"]:
     main_threshold()
+elif __name__ == "__main__" and sys.argv[1:] == ["smooth"]:
+    main_smooth()
 elif __name__ == "__main__":
     main()

@@ -228,3 +228,19 @@ def test_propagate_centroids(cuda):
     want = oracle.propagate_centroids(np.clip(bad, 0, cent.shape[1] - 1), cent)
     want[:, (bad < 0) | (bad >= cent.shape[1])] = 0.0
     assert np.array_equal(out.cpu().numpy(), want)
+
+
+SMOOTH = np.load(os.path.join(HERE, "golden", "smooth_golden.npz"))
+
+
+@pytest.mark.parametrize("i", range(len(SMOOTH["thresholds"])))
+def test_merge_smooth_boundaries(cuda, i):
+    """merge_smooth_boundaries on the device equals the compiled reference's
+    output (built with the one-token reduction fix) bit for bit."""
+    from split_gb300 import ccl
+    rgb, lab, pts, s = make_golden.smooth_inputs()
+    assert make_golden.sha(lab) == str(SMOOTH["labels_sha"])
+    g = _t(lab, cuda)
+    ws = ccl.merge_smooth_boundaries(_t(pts, cuda), s, g, None, float(SMOOTH["thresholds"][i]))
+    ws.check("merge_smooth")
+    assert np.array_equal(g.cpu().numpy(), SMOOTH[f"merged_{i}"])

@@ -173,3 +173,18 @@ def test_kmeans_threshold_intended_rule_differs():
 def test_propagate_centroids():
     out = oracle.propagate_centroids(THR["labels_0"].astype(np.int32), THR["centroids_0"])
     assert make_golden.sha(out) == str(THR["propagate_sha"])
+
+
+SMOOTH = np.load(os.path.join(HERE, "golden", "smooth_golden.npz"))
+
+
+@pytest.mark.parametrize("i", range(len(SMOOTH["thresholds"])))
+def test_merge_smooth_boundaries(i):
+    """The smooth-boundary merge restatement equals the compiled reference
+    (merge_smooth_boundaries.cu:134-243, built with thrust::minimum as the
+    reduction its comment describes) bit for bit."""
+    rgb, lab, pts, s = make_golden.smooth_inputs()
+    assert make_golden.sha(rgb) == str(SMOOTH["rgb_sha"])
+    assert make_golden.sha(lab) == str(SMOOTH["labels_sha"]) and s == int(SMOOTH["nsegments"])
+    got = oracle.merge_smooth(lab, pts, float(SMOOTH["thresholds"][i]))
+    assert np.array_equal(got, SMOOTH[f"merged_{i}"])
