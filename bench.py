@@ -620,7 +620,7 @@ def run_serving(dev, rates, seconds, pool=48, seed=SEED + 2000):
     srv = Server(params, budget_bytes=40 << 30, device=dev, keep_results=False,
                  reserve_pixels=64 << 20)
     srv.serve(requests([0.0] * pool), realtime=False)   # warm-up
-    nsat = 4 * pool
+    nsat = max(1024, 8 * pool)
     t = time.perf_counter()
     done = srv.serve(requests([0.0] * nsat), realtime=False)
     wall = time.perf_counter() - t

@@ -19,6 +19,7 @@
 namespace sg {
 int ccl_geoms(const int32_t* in, const Geoms& gs, int connectivity, int convention, int32_t* out,
               int32_t* sizes, WsHeader* hdr, cudaStream_t st);
+size_t ccl_workspace_bytes(int tiles);
 int erode_geoms(const int32_t* in, int32_t* out, const Geoms& gs, int radius, const void* mstate,
                 const int32_t* mfin, int local_labels, cudaStream_t st);
 int batch_image_maps(const int32_t* labels, const uint8_t* rgb, int W, int H, int radius,
@@ -172,7 +173,7 @@ extern "C" int split_batch_create(const split_batch_image* images, int nimages,
   b->total_tiles = tiles;
   std::vector<KmBatchImage> kmi = km_images(*b, Layout{});
   b->km_bytes = kmeans_batch_workspace(kmi.data(), nimages);
-  b->ccl_bytes = split_ccl_workspace_size(1, 1);
+  b->ccl_bytes = ccl_workspace_bytes(tiles);
   b->mrg_bytes = p.merge_P > 0 ? merge_workspace_bytes(off) : 0;
   *out = b;
   return SPLIT_OK;

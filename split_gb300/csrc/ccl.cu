@@ -15,7 +15,10 @@
 //            union-find on shared parents.  A local root stores its own
 //            global index, every other pixel the bitwise complement of its
 //            local root's (a negative entry), and local roots store their
-//            tile-local pixel count as their size.
+//            tile-local pixel count as their size.  A tile holding one value
+//            everywhere is one component: it stores only its root's entry and
+//            records the root in a per-tile word of the workspace (the other
+//            passes read that word instead of the tile's entries).
 //   border : per tile, edges to earlier tiles (W, NW, N, NE across the tile
 //            edge) are merged with lock-free atomicMin/atomicMax hooking of
 //            local roots (entries read at edge pixels are decoded first).
@@ -163,7 +166,7 @@ __device__ __forceinline__ Links needed(bool N, bool W, bool NW, bool NE, bool E
 template <bool MAXC, int CONN>
 __global__ void __launch_bounds__(kThreads, 5)
 tile_kernel(const int32_t* __restrict__ in, Geoms gs, int* __restrict__ P,
-            int32_t* __restrict__ sizes, int* status) {
+            int32_t* __restrict__ sizes, int* __restrict__ tword, int* status) {
   __shared__ int lab[TH * TW];
   __shared__ int par[TH * TW];
   const TileRef t = tile_ref(gs, blockIdx.x);
@@ -187,20 +190,18 @@ tile_kernel(const int32_t* __restrict__ in, Geoms gs, int* __restrict__ P,
     same = same && va[k] == v0 && vb[k] == v0;
   }
   if (__syncthreads_and(same)) {
-    // local root: the first pixel (minimum convention) or the last (maximum)
-    const long long gr = off + (long long)(ty0 + (MAXC ? th - 1 : 0)) * W + tx0 +
-                         (MAXC ? tw - 1 : 0);
-#pragma unroll
-    for (int k = 0; k < kRowsPerWarp; ++k) {
-      const int r = r0 + k;
-      if (r >= th) break;
-      const long long rowg = off + (long long)(ty0 + r) * W + tx0;
-      if (ca) __stcg(P + rowg + lane, rowg + lane == gr ? (int)gr : ~(int)gr);
-      if (cb) __stcg(P + rowg + lane + 32, rowg + lane + 32 == gr ? (int)gr : ~(int)gr);
+    // local root: the first pixel (minimum convention) or the last (maximum);
+    // only its entry is stored, the tile word names it for the other passes
+    if (threadIdx.x == 0) {
+      const long long gr = off + (long long)(ty0 + (MAXC ? th - 1 : 0)) * W + tx0 +
+                           (MAXC ? tw - 1 : 0);
+      __stcg(P + gr, (int)gr);
+      tword[blockIdx.x] = (int)gr + 1;
+      if (sizes) sizes[gr] = tw * th;
     }
-    if (sizes && threadIdx.x == 0) sizes[gr] = tw * th;
     return;
   }
+  if (threadIdx.x == 0) tword[blockIdx.x] = 0;
 #pragma unroll
   for (int k = 0; k < kRowsPerWarp; ++k) {
     const int r = r0 + k;
@@ -362,10 +363,19 @@ constexpr int kBorderThreads = 128;
 // root's complement; a local root, hooked or not, stores a root index).
 __device__ __forceinline__ int local_root(int e) { return e < 0 ? ~e : e; }
 
+// The local root of pixel g of tile t: the tile word of a one-value tile, the
+// pixel's entry otherwise.
+__device__ __forceinline__ int lroot(const int* P, const int* tword, long long g, int t) {
+  const int w = __ldcg(tword + t);
+  return w ? w - 1 : local_root(__ldcg(P + g));
+}
+
 template <bool MAXC, int CONN>
 __global__ void __launch_bounds__(kBorderThreads)
-border_kernel(const int32_t* __restrict__ in, Geoms gs, int* P, int* status) {
+border_kernel(const int32_t* __restrict__ in, Geoms gs, int* P, const int* __restrict__ tword,
+              int* status) {
   const TileRef t = tile_ref(gs, blockIdx.x);
+  const int me = blockIdx.x, up = me - t.tiles_x;
   const int W = t.W, tx0 = t.tx0, ty0 = t.ty0;
   const long long off = t.off;
   const int tw = min(TW, W - tx0), th = min(TH, t.H - ty0);
@@ -387,10 +397,10 @@ border_kernel(const int32_t* __restrict__ in, Geoms gs, int* P, int* status) {
     // is made by that edge's warp; the rule still holds across tiles
     const Links l = needed<CONN>(N, Wq, NW, NE, E);
     if (l.n || l.nw || l.ne) {
-      const int a = local_root(__ldcg(P + g));
-      if (l.n) gunite<MAXC>(P, a, local_root(__ldcg(P + g - W)), status);
-      if (l.nw) gunite<MAXC>(P, a, local_root(__ldcg(P + g - W - 1)), status);
-      if (l.ne) gunite<MAXC>(P, a, local_root(__ldcg(P + g - W + 1)), status);
+      const int a = lroot(P, tword, g, me);
+      if (l.n) gunite<MAXC>(P, a, lroot(P, tword, g - W, up), status);
+      if (l.nw) gunite<MAXC>(P, a, lroot(P, tword, g - W - 1, c == 0 ? up - 1 : up), status);
+      if (l.ne) gunite<MAXC>(P, a, lroot(P, tword, g - W + 1, c == tw - 1 ? up + 1 : up), status);
     }
   } else if (warp == 2) {
     if (tx0 == 0 || lane >= th) return;
@@ -400,7 +410,7 @@ border_kernel(const int32_t* __restrict__ in, Geoms gs, int* P, int* status) {
     const bool Wq = __ldg(in + g - 1) == v;
     if (lane == 0) {
       // the corner pixel: its N / NW links belong to the top-edge warps
-      if (Wq) gunite<MAXC>(P, local_root(__ldcg(P + g)), local_root(__ldcg(P + g - 1)), status);
+      if (Wq) gunite<MAXC>(P, lroot(P, tword, g, me), lroot(P, tword, g - 1, me - 1), status);
       return;
     }
     const bool N = __ldg(in + g - W) == v;
@@ -410,9 +420,9 @@ border_kernel(const int32_t* __restrict__ in, Geoms gs, int* P, int* status) {
     const bool lw = Wq && !(N && NW);
     const bool lnw = CONN == 8 && NW && !Wq && !N;
     if (lw || lnw) {
-      const int a = local_root(__ldcg(P + g));
-      if (lw) gunite<MAXC>(P, a, local_root(__ldcg(P + g - 1)), status);
-      if (lnw) gunite<MAXC>(P, a, local_root(__ldcg(P + g - W - 1)), status);
+      const int a = lroot(P, tword, g, me);
+      if (lw) gunite<MAXC>(P, a, lroot(P, tword, g - 1, me - 1), status);
+      if (lnw) gunite<MAXC>(P, a, lroot(P, tword, g - W - 1, me - 1), status);
     }
   } else if (CONN == 8) {
     // right column, rows 1 .. th - 1: the NE link into the tile to the right
@@ -422,7 +432,7 @@ border_kernel(const int32_t* __restrict__ in, Geoms gs, int* P, int* status) {
     const int v = __ldg(in + g);
     const bool NE = __ldg(in + g - W + 1) == v;
     if (NE && __ldg(in + g - W) != v && __ldg(in + g + 1) != v)
-      gunite<MAXC>(P, local_root(__ldcg(P + g)), local_root(__ldcg(P + g - W + 1)), status);
+      gunite<MAXC>(P, lroot(P, tword, g, me), lroot(P, tword, g - W + 1, me + 1), status);
   }
 }
 
@@ -437,12 +447,43 @@ border_kernel(const int32_t* __restrict__ in, Geoms gs, int* P, int* status) {
 // local root hooked under another adds its tile-local count to the final
 // root's size (nobody adds to a hooked root, so its count is final).
 __global__ void __launch_bounds__(kThreads)
-flatten_kernel(int* P, Geoms gs, int32_t* __restrict__ sizes, int* status) {
+flatten_kernel(int* P, Geoms gs, int32_t* __restrict__ sizes, const int* __restrict__ tword,
+               int* status) {
   const TileRef t = tile_ref(gs, blockIdx.x);
   const int W = t.W, tx0 = t.tx0, ty0 = t.ty0;
   const int tw = min(TW, W - tx0), th = min(TH, t.H - ty0);
   const int lane = threadIdx.x & 31, r0 = (threadIdx.x >> 5) * kRowsPerWarp;
   const int base = (int)(t.off + (long long)ty0 * W + tx0);
+  // a one-value tile: its root's chain is resolved once and every pixel
+  // stored without reading the (unwritten) entries
+  const int word = __ldcg(tword + blockIdx.x);
+  if (word) {
+    __shared__ int final_root;
+    if (threadIdx.x == 0) {
+      const int root = word - 1;
+      int f = root, q = P[f];
+      unsigned budget = kFindCap;
+      while (q != f && budget) {
+        --budget;
+        f = q;
+        q = P[f];
+      }
+      if (!budget) set_status(status, SPLIT_ERR_NOT_CONVERGED);
+      // a root hooked under another adds its count to the final root
+      if (sizes && f != root) atomicAdd(sizes + f, __ldcg(sizes + root));
+      final_root = f;
+    }
+    __syncthreads();
+    const int f = final_root;
+#pragma unroll
+    for (int k = 0; k < kRowsPerWarp; ++k) {
+      const int r = r0 + k;
+      if (r >= th) break;
+      if (lane < tw) P[base + r * W + lane] = f;
+      if (lane + 32 < tw) P[base + r * W + lane + 32] = f;
+    }
+    return;
+  }
   if (r0 >= th) return;   // the warp's rows lie below the image
   int g[2 * kRowsPerWarp], e[2 * kRowsPerWarp], x[2 * kRowsPerWarp], p[2 * kRowsPerWarp];
 #pragma unroll
@@ -499,13 +540,15 @@ flatten_kernel(int* P, Geoms gs, int32_t* __restrict__ sizes, int* status) {
 
 struct Layout {
   WsHeader* hdr;
+  int* tword;   // [tiles]: root + 1 of a one-value tile, else 0 (written every run)
   size_t bytes;
 };
 
-static Layout carve(void* ws) {
+static Layout carve(void* ws, int tiles) {
   Carver c(ws);
   Layout l;
   l.hdr = c.take<WsHeader>(1);
+  l.tword = c.take<int>((size_t)tiles);
   l.bytes = c.size();
   return l;
 }
@@ -513,12 +556,14 @@ static Layout carve(void* ws) {
 template <bool MAXC, int CONN>
 static int run(const int32_t* in, const Geoms& gs, int32_t* out, int32_t* sizes, WsHeader* hdr,
                cudaStream_t st) {
-  tile_kernel<MAXC, CONN><<<gs.total_tiles, kThreads, 0, st>>>(in, gs, out, sizes, &hdr->status);
+  int* tword = carve(hdr, gs.total_tiles).tword;
+  tile_kernel<MAXC, CONN><<<gs.total_tiles, kThreads, 0, st>>>(in, gs, out, sizes, tword,
+                                                               &hdr->status);
   SG_TRY(launch_status());
-  border_kernel<MAXC, CONN><<<gs.total_tiles, kBorderThreads, 0, st>>>(in, gs, out,
+  border_kernel<MAXC, CONN><<<gs.total_tiles, kBorderThreads, 0, st>>>(in, gs, out, tword,
                                                                       &hdr->status);
   SG_TRY(launch_status());
-  flatten_kernel<<<gs.total_tiles, kThreads, 0, st>>>(out, gs, sizes, &hdr->status);
+  flatten_kernel<<<gs.total_tiles, kThreads, 0, st>>>(out, gs, sizes, tword, &hdr->status);
   return launch_status();
 }
 
@@ -691,10 +736,14 @@ __global__ void gather_kernel(int32_t* labels, int64_t n, const uint32_t* __rest
 using namespace sg;
 
 extern "C" size_t split_ccl_workspace_size(int width, int height) {
-  (void)width;
-  (void)height;
-  return ccl::carve(nullptr).bytes;
+  if (width < 1 || height < 1) return 0;
+  return ccl::carve(nullptr, tiles_of(width, height)).bytes;
 }
+
+namespace sg {
+// the labelling workspace of a geometry table with `tiles` tiles (batches)
+size_t ccl_workspace_bytes(int tiles) { return ccl::carve(nullptr, tiles).bytes; }
+}  // namespace sg
 
 extern "C" int split_ccl(const int32_t* labels_in, int width, int height, int connectivity,
                          int convention, int32_t* labels_out, int32_t* d_sizes, void* workspace,
@@ -705,10 +754,11 @@ extern "C" int split_ccl(const int32_t* labels_in, int width, int height, int co
   if (convention != SPLIT_LABEL_MIN_INDEX && convention != SPLIT_LABEL_MAX_INDEX)
     return SPLIT_ERR_INVALID;
   if (labels_in == labels_out) return SPLIT_ERR_INVALID;
-  ccl::Layout l = ccl::carve(nullptr);
+  const int tiles = tiles_of(width, height);
+  ccl::Layout l = ccl::carve(nullptr, tiles);
   if (!workspace || workspace_bytes < l.bytes || (reinterpret_cast<uintptr_t>(workspace) & 255))
     return SPLIT_ERR_WORKSPACE;
-  l = ccl::carve(workspace);
+  l = ccl::carve(workspace, tiles);
   return ccl_geoms(labels_in, single_geom(width, height), connectivity, convention, labels_out,
                    d_sizes, l.hdr, as_stream(stream));
 }

@@ -59,6 +59,7 @@ struct TileRef {
   long long off;
   int tx0, ty0;   // tile origin (pixels)
   int tma_ok;
+  int tiles_x;    // tiles per tile row of the image (neighbour tiles: +-1, +-tiles_x)
 };
 
 __device__ __forceinline__ TileRef tile_ref(const Geoms& gs, int tile) {
@@ -82,6 +83,7 @@ __device__ __forceinline__ TileRef tile_ref(const Geoms& gs, int tile) {
   r.tx0 = tx * kTileW;
   r.ty0 = ty * kTileH;
   r.tma_ok = g.tma_ok;
+  r.tiles_x = g.tiles_x;
   return r;
 }
 

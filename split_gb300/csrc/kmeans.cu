@@ -278,6 +278,15 @@ __device__ __forceinline__ float2 fsub2(float2 a, float2 b) {
       : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
   return r;
 }
+__device__ __forceinline__ float2 fadd2(float2 a, float2 b) {
+  float2 r;
+  asm("{.reg .b64 a_, b_, r_;\n\t"
+      "mov.b64 a_, {%2, %3};\n\tmov.b64 b_, {%4, %5};\n\t"
+      "add.rn.f32x2 r_, a_, b_;\n\tmov.b64 {%0, %1}, r_;}"
+      : "=f"(r.x), "=f"(r.y)
+      : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+  return r;
+}
 __device__ __forceinline__ float2 fmul2(float2 a, float2 b) {
   float2 r;
   asm("{.reg .b64 a_, b_, r_;\n\t"
@@ -295,6 +304,26 @@ __device__ __forceinline__ float2 ffma2(float2 a, float2 b, float2 c) {
       : "=f"(r.x), "=f"(r.y)
       : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y), "f"(c.x), "f"(c.y));
   return r;
+}
+
+// acc[d] += x[d] - c[d] for every dimension, in IEEE single precision: the
+// pairs (0, 1) and (3, 4) on the packed pipe (per-lane results, the same bits
+// as the scalar operations).
+template <int DIM>
+__device__ __forceinline__ void add_centered(const float (&x)[DIM], const float* c,
+                                             float (&acc)[DIM]) {
+  const float2 a01 = fadd2(make_float2(acc[0], acc[1]),
+                           fsub2(make_float2(x[0], x[1]), make_float2(c[0], c[1])));
+  acc[0] = a01.x;
+  acc[1] = a01.y;
+  acc[2] = __fadd_rn(acc[2], __fsub_rn(x[2], c[2]));
+  if (DIM == 5) {
+    constexpr int X = DIM == 5 ? 3 : 0, Y = DIM == 5 ? 4 : 0;
+    const float2 a34 = fadd2(make_float2(acc[X], acc[Y]),
+                             fsub2(make_float2(x[X], x[Y]), make_float2(c[X], c[Y])));
+    acc[X] = a34.x;
+    acc[Y] = a34.y;
+  }
 }
 
 constexpr int kPx = 4;                 // consecutive pixels per lane
@@ -409,30 +438,6 @@ __device__ __forceinline__ void flush_acc(Smem& sm, int warp, int l, const float
   if (lane == 0) sm.cnt[warp][l] += c;
 }
 
-// Accumulate one batch whose kPx pixels all carry label l (warp-uniform):
-// the same sums, in the same order, as accumulate_valid's uniform case.
-template <int DIM>
-__device__ __forceinline__ void accumulate_uniform(Smem& sm, int warp, const float (&f)[kPx][DIM],
-                                                   int l, int& acc_l, int& acc_n,
-                                                   float (&acc)[DIM]) {
-  constexpr int CS = cstride(DIM);
-  if (l != acc_l) {
-    if (acc_l >= 0) flush_acc<DIM>(sm, warp, acc_l, acc, acc_n);
-    acc_l = l;
-    acc_n = 0;
-#pragma unroll
-    for (int d = 0; d < DIM; ++d) acc[d] = 0.0f;
-  }
-  float c[DIM];
-#pragma unroll
-  for (int d = 0; d < DIM; ++d) c[d] = sm.cent[l * CS + d];
-#pragma unroll
-  for (int j = 0; j < kPx; ++j)
-#pragma unroll
-    for (int d = 0; d < DIM; ++d) acc[d] = __fadd_rn(acc[d], __fsub_rn(f[j][d], c[d]));
-  acc_n += kPx;
-}
-
 // Accumulate one batch whose kPx labels are all valid: the same sums, in the
 // same order, as the general path below.
 template <int DIM>
@@ -457,9 +462,7 @@ __device__ __forceinline__ void accumulate_valid(Smem& sm, int warp, const float
 #pragma unroll
     for (int d = 0; d < DIM; ++d) c[d] = sm.cent[mn * CS + d];
 #pragma unroll
-    for (int j = 0; j < kPx; ++j)
-#pragma unroll
-      for (int d = 0; d < DIM; ++d) acc[d] = __fadd_rn(acc[d], __fsub_rn(f[j][d], c[d]));
+    for (int j = 0; j < kPx; ++j) add_centered<DIM>(f[j], c, acc);
     acc_n += kPx;
     return;
   }
@@ -474,9 +477,7 @@ __device__ __forceinline__ void accumulate_valid(Smem& sm, int warp, const float
 #pragma unroll
     for (int j = 0; j < kPx; ++j) {
       if (lab[j] == l) {
-#pragma unroll
-        for (int d = 0; d < DIM; ++d)
-          sum[d] = __fadd_rn(sum[d], __fsub_rn(f[j][d], sm.cent[l * CS + d]));
+        add_centered<DIM>(f[j], sm.cent + l * CS, sum);
         ++c;
       } else if (lab[j] > l) {
         nxt = min(nxt, lab[j]);
@@ -519,6 +520,15 @@ __device__ __forceinline__ void fast_span(const Image& im, Smem& sm, int warp, i
   // the span's box excludes all others for every pixel it holds (and the
   // features of this path lie in the unit cube, so none is NaN).
   const int single = (mask != 0ull && (mask & (mask - 1ull)) == 0ull) ? __ffsll(mask) - 1 : -1;
+  // with one label for the whole span the running sums switch to it once
+  if (MODE != kAssignOnly && single >= 0 && single != acc_l) {
+    if (acc_l >= 0) flush_acc<DIM>(sm, warp, acc_l, acc, acc_n);
+    acc_l = single;
+    acc_n = 0;
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) acc[d] = 0.0f;
+  }
+
   float fx[kPx];
 #pragma unroll
   for (int j = 0; j < kPx; ++j) fx[j] = __fmul_rn(im.xy_scale, (float)(col + j));
@@ -603,10 +613,15 @@ __device__ __forceinline__ void fast_span(const Image& im, Smem& sm, int warp, i
     if (write_labels)
       *reinterpret_cast<int4*>(im.labels + px0) = make_int4(lab[0], lab[1], lab[2], lab[3]);
     if (MODE != kAssignOnly) {
-      if (single >= 0)
-        accumulate_uniform<DIM>(sm, warp, f, single, acc_l, acc_n, acc);
-      else
+      if (single >= 0) {
+        // the same sums, in the same order, as accumulate_valid's uniform case
+        const float* c = sm.cent + single * cstride(DIM);
+#pragma unroll
+        for (int j = 0; j < kPx; ++j) add_centered<DIM>(f[j], c, acc);
+        acc_n += kPx;
+      } else {
         accumulate_valid<DIM>(sm, warp, f, lab, acc_l, acc_n, acc);
+      }
     }
   }
 }
@@ -764,8 +779,7 @@ __device__ void process_unit(const Image& im, int unit, Smem& sm, bool write_lab
 #pragma unroll
       for (int j = 0; j < kPx; ++j) {
         if (lab[j] >= 0) {
-#pragma unroll
-          for (int d = 0; d < DIM; ++d) acc[d] = __fadd_rn(acc[d], __fsub_rn(f[j][d], c[d]));
+          add_centered<DIM>(f[j], c, acc);
           ++acc_n;
         }
       }
@@ -781,8 +795,7 @@ __device__ void process_unit(const Image& im, int unit, Smem& sm, bool write_lab
 #pragma unroll
         for (int j = 0; j < kPx; ++j) {
           if (lab[j] == l) {
-#pragma unroll
-            for (int d = 0; d < DIM; ++d) s[d] = __fadd_rn(s[d], __fsub_rn(f[j][d], sm.cent[l * CS + d]));
+            add_centered<DIM>(f[j], sm.cent + l * CS, s);
             ++c;
           } else if (lab[j] > l) {
             nxt = min(nxt, lab[j]);
