@@ -505,30 +505,70 @@ __device__ __forceinline__ void cp_async_wait() {
 constexpr int kStageFloat4 = kWarps * 2 * 4 * 32;   // float4 elements per block
 constexpr size_t kStageBytes = (size_t)kStageFloat4 * 16;
 
-// A warp span that lies wholly inside the image, with packed features (float4,
-// or RGB8 read as three 32-bit words per 4 pixels) and a candidate mask known
-// for the whole span: no per-pixel bounds checks, one pointer step per batch,
-// the column feature hoisted.  Results equal the general path's.
-template <int LAYOUT, int DIM, int MODE>
-__device__ __forceinline__ void fast_span(const Image& im, Smem& sm, int warp, int row_first,
-                                          int col, int nbatches, unsigned long long mask,
-                                          bool write_labels, int& acc_l, int& acc_n,
-                                          float (&acc)[DIM]) {
+// Labels of the lane's pixels when the candidates are exactly ka < kb: the
+// same distances, in the same order and with the same comparisons, as
+// nearest_px over a two-bit mask.
+template <int DIM>
+__device__ __forceinline__ void nearest_pair(const float (&f)[kPx][DIM],
+                                             const float* __restrict__ cs, int ka, int kb,
+                                             int (&lab)[kPx]) {
+  constexpr int CS = cstride(DIM);
+  float best[kPx];
+#pragma unroll
+  for (int j = 0; j < kPx; ++j) {
+    best[j] = INFINITY;
+    lab[j] = 0;
+  }
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    const int k = h ? kb : ka;
+    const float4 c0 = *reinterpret_cast<const float4*>(cs + k * CS);
+    const float cc[5] = {c0.x, c0.y, c0.z, c0.w, DIM == 5 ? cs[k * CS + 4] : 0.0f};
+#pragma unroll
+    for (int q = 0; q < kPx / 2; ++q) {
+      const int a = 2 * q, b = 2 * q + 1;
+      float2 t = fsub2(make_float2(f[a][0], f[b][0]), make_float2(cc[0], cc[0]));
+      float2 d = fmul2(t, t);
+#pragma unroll
+      for (int dd = 1; dd < DIM; ++dd) {
+        t = fsub2(make_float2(f[a][dd], f[b][dd]), make_float2(cc[dd], cc[dd]));
+        d = ffma2(t, t, d);
+      }
+      if (d.x < best[a]) {
+        best[a] = d.x;
+        lab[a] = k;
+      }
+      if (d.y < best[b]) {
+        best[b] = d.y;
+        lab[b] = k;
+      }
+    }
+  }
+}
+
+// How a span's candidate mask is used: one cluster (every pixel's label
+// outright), two clusters with finite centroids (two running sums per lane),
+// or any other mask (per-batch reduction by label).
+enum SpanKind { kSpanSingle = 0, kSpanPair = 1, kSpanAny = 2 };
+
+// The batches of a fast span (see fast_span).  For kSpanPair every pixel's
+// label is ka or kb (finite features and centroids), so `acc` runs for ka
+// and a second per-lane sum for kb, reduced once at the end of the span
+// however often the two labels mix within its batches.
+template <int LAYOUT, int DIM, int MODE, int KIND>
+__device__ __forceinline__ void span_batches(const Image& im, Smem& sm, int warp, int row_first,
+                                             int col, int nbatches, unsigned long long mask,
+                                             int ka, int kb, bool write_labels, int& acc_l,
+                                             int& acc_n, float (&acc)[DIM]) {
+  constexpr int CS = cstride(DIM);
   const int64_t step = (int64_t)kBatchRows * im.width;
   int64_t px0 = (int64_t)row_first * im.width + col;
-  // A mask with one cluster names every pixel's nearest centroid outright:
-  // the span's box excludes all others for every pixel it holds (and the
-  // features of this path lie in the unit cube, so none is NaN).
-  const int single = (mask != 0ull && (mask & (mask - 1ull)) == 0ull) ? __ffsll(mask) - 1 : -1;
-  // with one label for the whole span the running sums switch to it once
-  if (MODE != kAssignOnly && single >= 0 && single != acc_l) {
-    if (acc_l >= 0) flush_acc<DIM>(sm, warp, acc_l, acc, acc_n);
-    acc_l = single;
-    acc_n = 0;
+  float acc2[DIM];
+  int acc2_n = 0;
+  if (KIND == kSpanPair) {
 #pragma unroll
-    for (int d = 0; d < DIM; ++d) acc[d] = 0.0f;
+    for (int d = 0; d < DIM; ++d) acc2[d] = 0.0f;
   }
-
   float fx[kPx];
 #pragma unroll
   for (int j = 0; j < kPx; ++j) fx[j] = __fmul_rn(im.xy_scale, (float)(col + j));
@@ -603,27 +643,93 @@ __device__ __forceinline__ void fast_span(const Image& im, Smem& sm, int warp, i
       }
     }
     int lab[kPx];
-    if (single >= 0) {
+    if (KIND == kSpanSingle) {
       // one candidate for the whole span: every pixel's argmin, no distances
 #pragma unroll
-      for (int j = 0; j < kPx; ++j) lab[j] = single;
+      for (int j = 0; j < kPx; ++j) lab[j] = ka;
+    } else if (KIND == kSpanPair) {
+      nearest_pair<DIM>(f, sm.cent, ka, kb, lab);
     } else {
       nearest_px<DIM>(f, sm.cent, mask, lab);
     }
     if (write_labels)
       *reinterpret_cast<int4*>(im.labels + px0) = make_int4(lab[0], lab[1], lab[2], lab[3]);
     if (MODE != kAssignOnly) {
-      if (single >= 0) {
+      if (KIND == kSpanSingle) {
         // the same sums, in the same order, as accumulate_valid's uniform case
-        const float* c = sm.cent + single * cstride(DIM);
+        const float* c = sm.cent + ka * CS;
 #pragma unroll
         for (int j = 0; j < kPx; ++j) add_centered<DIM>(f[j], c, acc);
         acc_n += kPx;
+      } else if (KIND == kSpanPair) {
+        const float* ca = sm.cent + ka * CS;
+        const float* cb = sm.cent + kb * CS;
+#pragma unroll
+        for (int j = 0; j < kPx; ++j) {
+          if (lab[j] == ka) {
+            add_centered<DIM>(f[j], ca, acc);
+            ++acc_n;
+          } else {
+            add_centered<DIM>(f[j], cb, acc2);
+            ++acc2_n;
+          }
+        }
       } else {
         accumulate_valid<DIM>(sm, warp, f, lab, acc_l, acc_n, acc);
       }
     }
   }
+  // the second candidate's sums (the first's stay running)
+  if (MODE != kAssignOnly && KIND == kSpanPair) flush_acc<DIM>(sm, warp, kb, acc2, acc2_n);
+}
+
+// A warp span that lies wholly inside the image, with packed features (float4,
+// or RGB8 read as three 32-bit words per 4 pixels) and a candidate mask known
+// for the whole span: no per-pixel bounds checks, one pointer step per batch,
+// the column feature hoisted.  Results equal the general path's labels; the
+// sums are the same pixels' in a fixed, data-dependent order.
+template <int LAYOUT, int DIM, int MODE>
+__device__ __forceinline__ void fast_span(const Image& im, Smem& sm, int warp, int row_first,
+                                          int col, int nbatches, unsigned long long mask,
+                                          bool write_labels, int& acc_l, int& acc_n,
+                                          float (&acc)[DIM]) {
+  constexpr int CS = cstride(DIM);
+  // A mask with one cluster names every pixel's nearest centroid outright:
+  // the span's box excludes all others for every pixel it holds (and the
+  // features of this path lie in the unit cube, so none is NaN).
+  int kind = kSpanAny, ka = -1, kb = -1;
+  if (mask != 0ull && (mask & (mask - 1ull)) == 0ull) {
+    kind = kSpanSingle;
+    ka = __ffsll((long long)mask) - 1;
+  } else if (MODE != kAssignOnly && __popcll((long long)mask) == 2) {
+    const int a = __ffsll((long long)mask) - 1, b = 63 - __clzll((long long)mask);
+    bool fin = true;
+#pragma unroll
+    for (int d = 0; d < DIM; ++d)
+      fin = fin && isfinite(sm.cent[a * CS + d]) && isfinite(sm.cent[b * CS + d]);
+    if (fin) {
+      kind = kSpanPair;
+      ka = a;
+      kb = b;
+    }
+  }
+  // with one running label for the whole span the sums switch to it once
+  if (MODE != kAssignOnly && ka >= 0 && ka != acc_l) {
+    if (acc_l >= 0) flush_acc<DIM>(sm, warp, acc_l, acc, acc_n);
+    acc_l = ka;
+    acc_n = 0;
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) acc[d] = 0.0f;
+  }
+  if (kind == kSpanSingle)
+    span_batches<LAYOUT, DIM, MODE, kSpanSingle>(im, sm, warp, row_first, col, nbatches, mask, ka,
+                                                 kb, write_labels, acc_l, acc_n, acc);
+  else if (kind == kSpanPair)
+    span_batches<LAYOUT, DIM, MODE, kSpanPair>(im, sm, warp, row_first, col, nbatches, mask, ka,
+                                               kb, write_labels, acc_l, acc_n, acc);
+  else
+    span_batches<LAYOUT, DIM, MODE, kSpanAny>(im, sm, warp, row_first, col, nbatches, mask, ka,
+                                              kb, write_labels, acc_l, acc_n, acc);
 }
 
 // Process one unit (a 64 x 64 tile): assign (unless update-only) and
