@@ -19,7 +19,7 @@
 // order units finish in and whatever else shares the launch.  A unit ends with
 // fire-and-forget adds and one block barrier: no fence, no arrival counter.
 // The grid barrier that ends the iteration publishes the sums; then c_new =
-// c + S / n is formed in FP64, rounded to FP32 (form_centroids): for a single
+// c + S / n is formed in FP32 from the exact sum (form_centroids): for a single
 // image by every block from the same inputs (bit-identical), block 0
 // publishing it; in a batch by one owner block per image, published before a
 // second grid barrier.  The sums are
@@ -1049,11 +1049,14 @@ __device__ bool form_centroids(const Params& p, int img, const Image& im, int i,
     const unsigned n = __ldcg(cnt + k);
     float cn = c;
     if (n > 0) {
-      // S = (hi * 2^32 + lo) * 2^-24, exact up to the final FP64 rounding
-      const double h = (double)(long long)__ldcg(hi + a);
-      const double l = (double)__ldcg(lo + a);
-      const double S = __dmul_rn(__dadd_rn(__dmul_rn(h, 4294967296.0), l), 1.0 / 16777216.0);
-      cn = __double2float_rn(__dadd_rn((double)c, __ddiv_rn(S, (double)n)));
+      // S = (hi * 2^32 + lo) * 2^-24: one FP64 rounding of the exact sum,
+      // one to FP32 (the scaling by 2^-24 is exact); then c + S / n in FP32
+      // (every block forms all K x D values, so the FP64 pipe is kept to the
+      // conversion: a division there costs the iteration about a microsecond)
+      const double S64 = __fma_rn((double)(long long)__ldcg(hi + a), 4294967296.0,
+                                  (double)__ldcg(lo + a));
+      const float S = __fmul_rn(__double2float_rn(S64), 1.0f / 16777216.0f);
+      cn = __fadd_rn(c, __fdiv_rn(S, (float)n));
     }
     cent[k * CS + d] = cn;
     if (owner) __stcg(c_new + k * 8 + d, cn);
