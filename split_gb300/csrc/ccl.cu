@@ -166,7 +166,8 @@ __device__ __forceinline__ Links needed(bool N, bool W, bool NW, bool NE, bool E
 template <bool MAXC, int CONN>
 __global__ void __launch_bounds__(kThreads, 5)
 tile_kernel(const int32_t* __restrict__ in, Geoms gs, int* __restrict__ P,
-            int32_t* __restrict__ sizes, int* __restrict__ tword, int* status) {
+            int32_t* __restrict__ sizes, int* __restrict__ tword, int* __restrict__ tval,
+            int* status) {
   __shared__ int lab[TH * TW];
   __shared__ int par[TH * TW];
   const TileRef t = tile_ref(gs, blockIdx.x);
@@ -197,6 +198,7 @@ tile_kernel(const int32_t* __restrict__ in, Geoms gs, int* __restrict__ P,
                            (MAXC ? tw - 1 : 0);
       __stcg(P + gr, (int)gr);
       tword[blockIdx.x] = (int)gr + 1;
+      tval[blockIdx.x] = v0;
       if (sizes) sizes[gr] = tw * th;
     }
     return;
@@ -351,13 +353,20 @@ tile_kernel(const int32_t* __restrict__ in, Geoms gs, int* __restrict__ P,
   }
 }
 
-// Border pass, one 128-thread block per tile: warps 0-1 join the top row
-// with the row above (N, NW, NE links into the tiles above), warp 2 joins
-// the left column with the column to its left (W, NW), warp 3 the right
-// column with the tile to its right (NE, 8-connectivity only).  Unions start
-// at the local roots the tile pass stored and skip links implied by others
-// (the same rules as inside a tile, with neighbours read across the edge).
+// Border pass, one warp per tile: the edges to the tile above (N, NW, NE
+// links of the top row), to the tile on the left (W, NW links of the left
+// column) and, for 8-connectivity, the NE links of the right column into the
+// tile on the right.  Unions start at the local roots the tile pass stored
+// and skip links implied by others (the same rules as inside a tile, with
+// neighbours read across the edge).
+//
+// An edge between two one-value tiles is decided from their tile words
+// alone: their components join if the values are equal, and no other link
+// crosses the edge except at the top row's two corners (8-connectivity),
+// whose diagonal links are checked pixel by pixel.  The right column of a
+// one-value tile needs no NE link (its N neighbour carries the label).
 constexpr int kBorderThreads = 128;
+constexpr int kBorderTiles = kBorderThreads / 32;
 
 // The local root named by a tile-pass entry (a non-root pixel stores its local
 // root's complement; a local root, hooked or not, stores a root index).
@@ -373,61 +382,105 @@ __device__ __forceinline__ int lroot(const int* P, const int* tword, long long g
 template <bool MAXC, int CONN>
 __global__ void __launch_bounds__(kBorderThreads)
 border_kernel(const int32_t* __restrict__ in, Geoms gs, int* P, const int* __restrict__ tword,
-              int* status) {
-  const TileRef t = tile_ref(gs, blockIdx.x);
-  const int me = blockIdx.x, up = me - t.tiles_x;
+              const int* __restrict__ tval, int* status) {
+  const int me = blockIdx.x * kBorderTiles + (threadIdx.x >> 5);
+  if (me >= gs.total_tiles) return;
+  const int lane = threadIdx.x & 31;
+  const TileRef t = tile_ref(gs, me);
+  const int up = me - t.tiles_x;
   const int W = t.W, tx0 = t.tx0, ty0 = t.ty0;
   const long long off = t.off;
   const int tw = min(TW, W - tx0), th = min(TH, t.H - ty0);
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  if (warp < 2) {
-    if (ty0 == 0) return;
-    const int c = warp * 32 + lane;
-    if (c >= tw) return;
-    const int x = tx0 + c;
-    const long long g = off + (long long)ty0 * W + x;
-    const int v = __ldg(in + g);
-    const bool hasW = x > 0, hasE = x + 1 < W;
-    const bool N = __ldg(in + g - W) == v;
-    const bool Wq = hasW && __ldg(in + g - 1) == v;
-    const bool NW = hasW && __ldg(in + g - W - 1) == v;
-    const bool NE = hasE && __ldg(in + g - W + 1) == v;
-    const bool E = hasE && __ldg(in + g + 1) == v;
-    // at the tile's first column the W link crosses into the left tile and
-    // is made by that edge's warp; the rule still holds across tiles
-    const Links l = needed<CONN>(N, Wq, NW, NE, E);
-    if (l.n || l.nw || l.ne) {
-      const int a = lroot(P, tword, g, me);
-      if (l.n) gunite<MAXC>(P, a, lroot(P, tword, g - W, up), status);
-      if (l.nw) gunite<MAXC>(P, a, lroot(P, tword, g - W - 1, c == 0 ? up - 1 : up), status);
-      if (l.ne) gunite<MAXC>(P, a, lroot(P, tword, g - W + 1, c == tw - 1 ? up + 1 : up), status);
+  bool top_px = ty0 > 0, left_px = tx0 > 0;
+  bool right_px = CONN == 8 && tx0 + tw < W;
+  const int wme = __ldcg(tword + me);
+  if (wme) {
+    right_px = false;
+    int flags = 0;   // bit 0: the top edge, bit 1: the left edge go pixel by pixel
+    if (lane == 0) {
+      const int root = wme - 1, v = __ldcg(tval + me);
+      const long long g = off + (long long)ty0 * W + tx0;   // the top-left pixel
+      if (left_px) {
+        const int wl = __ldcg(tword + me - 1);
+        if (wl) {
+          if (__ldcg(tval + me - 1) == v) gunite<MAXC>(P, root, wl - 1, status);
+        } else {
+          flags |= 2;
+        }
+      }
+      if (top_px) {
+        const int wu = __ldcg(tword + up);
+        if (wu) {
+          const bool N = __ldcg(tval + up) == v;
+          if (N) gunite<MAXC>(P, root, wu - 1, status);
+          if (CONN == 8 && !N) {
+            // the corners: NW of the first column, NE of the last
+            if (tx0 > 0 && __ldg(in + g - 1) != v && __ldg(in + g - W - 1) == v)
+              gunite<MAXC>(P, root, lroot(P, tword, g - W - 1, up - 1), status);
+            const long long gr = g + tw - 1;
+            if (tx0 + tw < W && __ldg(in + gr + 1) != v && __ldg(in + gr - W + 1) == v)
+              gunite<MAXC>(P, root, lroot(P, tword, gr - W + 1, up + 1), status);
+          }
+        } else {
+          flags |= 1;
+        }
+      }
     }
-  } else if (warp == 2) {
-    if (tx0 == 0 || lane >= th) return;
+    flags = __shfl_sync(0xffffffffu, flags, 0);
+    top_px = flags & 1;
+    left_px = flags & 2;
+  }
+  if (top_px) {
+    // the top row with the row above, columns lane and lane + 32
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int c = h * 32 + lane;
+      if (c >= tw) break;
+      const int x = tx0 + c;
+      const long long g = off + (long long)ty0 * W + x;
+      const int v = __ldg(in + g);
+      const bool hasW = x > 0, hasE = x + 1 < W;
+      const bool N = __ldg(in + g - W) == v;
+      const bool Wq = hasW && __ldg(in + g - 1) == v;
+      const bool NW = hasW && __ldg(in + g - W - 1) == v;
+      const bool NE = hasE && __ldg(in + g - W + 1) == v;
+      const bool E = hasE && __ldg(in + g + 1) == v;
+      // at the tile's first column the W link crosses into the left tile and
+      // is made by that edge's lanes; the rule still holds across tiles
+      const Links l = needed<CONN>(N, Wq, NW, NE, E);
+      if (l.n || l.nw || l.ne) {
+        const int a = lroot(P, tword, g, me);
+        if (l.n) gunite<MAXC>(P, a, lroot(P, tword, g - W, up), status);
+        if (l.nw) gunite<MAXC>(P, a, lroot(P, tword, g - W - 1, c == 0 ? up - 1 : up), status);
+        if (l.ne) gunite<MAXC>(P, a, lroot(P, tword, g - W + 1, c == tw - 1 ? up + 1 : up), status);
+      }
+    }
+  }
+  if (left_px && lane < th) {
     const int y = ty0 + lane;
     const long long g = off + (long long)y * W + tx0;
     const int v = __ldg(in + g);
     const bool Wq = __ldg(in + g - 1) == v;
     if (lane == 0) {
-      // the corner pixel: its N / NW links belong to the top-edge warps
+      // the corner pixel: its N / NW links belong to the top edge
       if (Wq) gunite<MAXC>(P, lroot(P, tword, g, me), lroot(P, tword, g - 1, me - 1), status);
-      return;
+    } else {
+      const bool N = __ldg(in + g - W) == v;
+      const bool NW = __ldg(in + g - W - 1) == v;
+      // W is implied when N and NW carry the label (both columns are joined
+      // one row up, and N joins inside this tile)
+      const bool lw = Wq && !(N && NW);
+      const bool lnw = CONN == 8 && NW && !Wq && !N;
+      if (lw || lnw) {
+        const int a = lroot(P, tword, g, me);
+        if (lw) gunite<MAXC>(P, a, lroot(P, tword, g - 1, me - 1), status);
+        if (lnw) gunite<MAXC>(P, a, lroot(P, tword, g - W - 1, me - 1), status);
+      }
     }
-    const bool N = __ldg(in + g - W) == v;
-    const bool NW = __ldg(in + g - W - 1) == v;
-    // W is implied when N and NW carry the label (both columns are joined
-    // one row up, and N joins inside this tile)
-    const bool lw = Wq && !(N && NW);
-    const bool lnw = CONN == 8 && NW && !Wq && !N;
-    if (lw || lnw) {
-      const int a = lroot(P, tword, g, me);
-      if (lw) gunite<MAXC>(P, a, lroot(P, tword, g - 1, me - 1), status);
-      if (lnw) gunite<MAXC>(P, a, lroot(P, tword, g - W - 1, me - 1), status);
-    }
-  } else if (CONN == 8) {
+  }
+  if (right_px && lane > 0 && lane < th) {
     // right column, rows 1 .. th - 1: the NE link into the tile to the right
     const int x = tx0 + tw - 1;
-    if (x + 1 >= W || lane == 0 || lane >= th) return;
     const long long g = off + (long long)(ty0 + lane) * W + x;
     const int v = __ldg(in + g);
     const bool NE = __ldg(in + g - W + 1) == v;
@@ -541,6 +594,7 @@ flatten_kernel(int* P, Geoms gs, int32_t* __restrict__ sizes, const int* __restr
 struct Layout {
   WsHeader* hdr;
   int* tword;   // [tiles]: root + 1 of a one-value tile, else 0 (written every run)
+  int* tval;    // [tiles]: the value of a one-value tile (written with its word)
   size_t bytes;
 };
 
@@ -549,6 +603,7 @@ static Layout carve(void* ws, int tiles) {
   Layout l;
   l.hdr = c.take<WsHeader>(1);
   l.tword = c.take<int>((size_t)tiles);
+  l.tval = c.take<int>((size_t)tiles);
   l.bytes = c.size();
   return l;
 }
@@ -556,12 +611,13 @@ static Layout carve(void* ws, int tiles) {
 template <bool MAXC, int CONN>
 static int run(const int32_t* in, const Geoms& gs, int32_t* out, int32_t* sizes, WsHeader* hdr,
                cudaStream_t st) {
-  int* tword = carve(hdr, gs.total_tiles).tword;
-  tile_kernel<MAXC, CONN><<<gs.total_tiles, kThreads, 0, st>>>(in, gs, out, sizes, tword,
+  const Layout l = carve(hdr, gs.total_tiles);
+  int* tword = l.tword;
+  tile_kernel<MAXC, CONN><<<gs.total_tiles, kThreads, 0, st>>>(in, gs, out, sizes, tword, l.tval,
                                                                &hdr->status);
   SG_TRY(launch_status());
-  border_kernel<MAXC, CONN><<<gs.total_tiles, kBorderThreads, 0, st>>>(in, gs, out, tword,
-                                                                      &hdr->status);
+  border_kernel<MAXC, CONN><<<(gs.total_tiles + kBorderTiles - 1) / kBorderTiles, kBorderThreads,
+                              0, st>>>(in, gs, out, tword, l.tval, &hdr->status);
   SG_TRY(launch_status());
   flatten_kernel<<<gs.total_tiles, kThreads, 0, st>>>(out, gs, sizes, tword, &hdr->status);
   return launch_status();
