@@ -383,6 +383,7 @@ template <bool MAXC, int CONN>
 __global__ void __launch_bounds__(kBorderThreads)
 border_kernel(const int32_t* __restrict__ in, Geoms gs, int* P, const int* __restrict__ tword,
               const int* __restrict__ tval, int* status) {
+  pdl_wait();
   const int me = blockIdx.x * kBorderTiles + (threadIdx.x >> 5);
   if (me >= gs.total_tiles) return;
   const int lane = threadIdx.x & 31;
@@ -502,6 +503,7 @@ border_kernel(const int32_t* __restrict__ in, Geoms gs, int* P, const int* __res
 __global__ void __launch_bounds__(kThreads)
 flatten_kernel(int* P, Geoms gs, int32_t* __restrict__ sizes, const int* __restrict__ tword,
                int* status) {
+  pdl_wait();
   const TileRef t = tile_ref(gs, blockIdx.x);
   const int W = t.W, tx0 = t.tx0, ty0 = t.ty0;
   const int tw = min(TW, W - tx0), th = min(TH, t.H - ty0);
@@ -616,10 +618,12 @@ static int run(const int32_t* in, const Geoms& gs, int32_t* out, int32_t* sizes,
   tile_kernel<MAXC, CONN><<<gs.total_tiles, kThreads, 0, st>>>(in, gs, out, sizes, tword, l.tval,
                                                                &hdr->status);
   SG_TRY(launch_status());
-  border_kernel<MAXC, CONN><<<(gs.total_tiles + kBorderTiles - 1) / kBorderTiles, kBorderThreads,
-                              0, st>>>(in, gs, out, tword, l.tval, &hdr->status);
+  launch_pdl(border_kernel<MAXC, CONN>, dim3((gs.total_tiles + kBorderTiles - 1) / kBorderTiles),
+             dim3(kBorderThreads), 0, st, in, gs, out, (const int*)tword, (const int*)l.tval,
+             &hdr->status);
   SG_TRY(launch_status());
-  flatten_kernel<<<gs.total_tiles, kThreads, 0, st>>>(out, gs, sizes, tword, &hdr->status);
+  launch_pdl(flatten_kernel, dim3(gs.total_tiles), dim3(kThreads), 0, st, out, gs, sizes,
+             (const int*)tword, &hdr->status);
   return launch_status();
 }
 

@@ -6,6 +6,8 @@
 #include <stdint.h>
 #include <stddef.h>
 
+#include <utility>
+
 #include <cuda/atomic>
 
 #include "../../include/split_gb300.h"
@@ -30,6 +32,28 @@ namespace sg {
 // Kernels launched by the library since load (every launch site reports
 // through launch_status()).
 void count_launch();
+
+// Programmatic dependent launch: the kernel may be scheduled while the
+// previous kernel on the stream finishes; it must execute pdl_wait() before
+// touching anything that kernel writes (and before any write of its own that
+// the previous kernel reads).
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem,
+                              cudaStream_t st, Args&&... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
+}
 
 inline int launch_status() {
   count_launch();
