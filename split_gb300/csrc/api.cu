@@ -61,6 +61,7 @@ extern "C" const char* split_status_string(int status) {
 namespace sg {
 // first error in source order wins, as with set_status
 __global__ void fold_status_kernel(int* dst, StatusSources s) {
+  pdl_wait();
   if (threadIdx.x != 0) return;
   for (int i = 0; i < s.n; ++i) {
     volatile int* q = s.p[i];
@@ -73,7 +74,7 @@ __global__ void fold_status_kernel(int* dst, StatusSources s) {
 }
 
 int fold_status(int* dst, const StatusSources& s, cudaStream_t st) {
-  fold_status_kernel<<<1, 32, 0, st>>>(dst, s);
+  launch_pdl(fold_status_kernel, dim3(1), dim3(32), 0, st, dst, s);
   return launch_status();
 }
 
@@ -92,11 +93,12 @@ bool layout_unchanged(const void* workspace, unsigned long long key) {
 }
 
 __global__ void clear_status_kernel(StatusSources s) {
+  pdl_wait();
   if ((int)threadIdx.x < s.n) *s.p[threadIdx.x] = 0;
 }
 
 int clear_status(const StatusSources& s, cudaStream_t st) {
-  clear_status_kernel<<<1, 32, 0, st>>>(s);
+  launch_pdl(clear_status_kernel, dim3(1), dim3(32), 0, st, s);
   return launch_status();
 }
 }  // namespace sg

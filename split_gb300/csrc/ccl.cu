@@ -168,6 +168,7 @@ __global__ void __launch_bounds__(kThreads, 5)
 tile_kernel(const int32_t* __restrict__ in, Geoms gs, int* __restrict__ P,
             int32_t* __restrict__ sizes, int* __restrict__ tword, int* __restrict__ tval,
             int* status) {
+  pdl_wait();
   __shared__ int lab[TH * TW];
   __shared__ int par[TH * TW];
   const TileRef t = tile_ref(gs, blockIdx.x);
@@ -615,8 +616,8 @@ static int run(const int32_t* in, const Geoms& gs, int32_t* out, int32_t* sizes,
                cudaStream_t st) {
   const Layout l = carve(hdr, gs.total_tiles);
   int* tword = l.tword;
-  tile_kernel<MAXC, CONN><<<gs.total_tiles, kThreads, 0, st>>>(in, gs, out, sizes, tword, l.tval,
-                                                               &hdr->status);
+  launch_pdl(tile_kernel<MAXC, CONN>, dim3(gs.total_tiles), dim3(kThreads), 0, st, in, gs, out,
+             sizes, tword, l.tval, &hdr->status);
   SG_TRY(launch_status());
   launch_pdl(border_kernel<MAXC, CONN>, dim3((gs.total_tiles + kBorderTiles - 1) / kBorderTiles),
              dim3(kBorderThreads), 0, st, in, gs, out, (const int*)tword, (const int*)l.tval,

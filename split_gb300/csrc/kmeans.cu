@@ -1243,6 +1243,7 @@ static int reset_counters(const Layout& l, int nimages, cudaStream_t st) {
 // Per-image iteration state (cluster.cu:65-68: delta = 0, old_delta =
 // delta + threshold + 1, so the first convergence test always passes).
 __global__ void init_kernel(Params p) {
+  pdl_wait();
   for (int img = blockIdx.x * blockDim.x + threadIdx.x; img < p.nimages;
        img += gridDim.x * blockDim.x) {
     const Image& im = image_of(p, img);
@@ -1258,6 +1259,7 @@ __global__ void init_kernel(Params p) {
 
 template <int DIM>
 __global__ void load_user_centroids(Params p) {
+  pdl_wait();
   for (int img = blockIdx.x; img < p.nimages; img += gridDim.x) {
     const Image& im = image_of(p, img);
     float* c0 = p.cur + (size_t)img * (kMaxK * 8);
@@ -1425,10 +1427,10 @@ static int run(int mode, const void* points, int layout, int dim, int64_t n,
   p.hdr = l.hdr;
   SG_TRY(reset_counters(l, 1, st));
   (void)centroids_in;
-  init_kernel<<<1, 256, 0, st>>>(p);
+  launch_pdl(init_kernel, dim3(1), dim3(256), 0, st, p);
   SG_TRY(launch_status());
-  if (dim == 3) load_user_centroids<3><<<1, 256, 0, st>>>(p);
-  else load_user_centroids<5><<<1, 256, 0, st>>>(p);
+  if (dim == 3) launch_pdl(load_user_centroids<3>, dim3(1), dim3(256), 0, st, p);
+  else launch_pdl(load_user_centroids<5>, dim3(1), dim3(256), 0, st, p);
   SG_TRY(launch_status());
   if (max_iter <= 0) return SPLIT_OK;
   if (mode == kCluster) return dispatch<kCluster>(layout, dim, p, st);
@@ -1744,12 +1746,12 @@ int kmeans_batch_run(const KmBatchPlan& plan, void* ws, cudaStream_t st) {
   p.wait_limit = kSpinLimit;   // the wait test applies to single images only
   p.wait_skip = -1;
   SG_TRY(reset_counters(l, plan.nimages, st));
-  init_kernel<<<(plan.nimages + 255) / 256, 256, 0, st>>>(p);
+  launch_pdl(init_kernel, dim3((plan.nimages + 255) / 256), dim3(256), 0, st, p);
   SG_TRY(launch_status());
   // one block per image (the kernel strides over images past 1024)
   const int cb = plan.nimages < 1024 ? plan.nimages : 1024;
-  if (plan.dim == 3) load_user_centroids<3><<<cb, 64, 0, st>>>(p);
-  else load_user_centroids<5><<<cb, 64, 0, st>>>(p);
+  if (plan.dim == 3) launch_pdl(load_user_centroids<3>, dim3(cb), dim3(64), 0, st, p);
+  else launch_pdl(load_user_centroids<5>, dim3(cb), dim3(64), 0, st, p);
   SG_TRY(launch_status());
   if (plan.max_iter <= 0) return SPLIT_OK;
   return dispatch<kCluster>(plan.layout, plan.dim, p, st);

@@ -130,6 +130,7 @@ __device__ __forceinline__ unsigned seg_class(int s, int lev) {
 __global__ void __launch_bounds__(kThreads)
 size_kernel(const int32_t* __restrict__ lab, int64_t n, Layout L, bool count_sizes,
             const float* __restrict__ chroma, int* status) {
+  pdl_wait();
   const unsigned full = 0xffffffffu;
   for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < n;
        base += (int64_t)gridDim.x * blockDim.x) {
@@ -208,6 +209,7 @@ __device__ __forceinline__ void pair_tile(const int32_t* __restrict__ lab, const
 __global__ void __launch_bounds__(kThreads, 4)
 pair_kernel(const int32_t* __restrict__ lab, Geoms gs, Layout L, const int32_t* sizes, int P,
             int* status) {
+  pdl_wait();
   pair_tile<false>(lab, gs, L, sizes, P, blockIdx.x, 0, 0u, status);
 }
 
@@ -453,6 +455,7 @@ list_kernel(Layout L, const int32_t* lab, Geoms gs, const int32_t* sizes, int P,
 }
 
 __global__ void relabel_kernel(int32_t* lab, int64_t n, const State* stp, const int32_t* fin) {
+  pdl_wait();
   const State st = *stp;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x)
@@ -465,6 +468,7 @@ __global__ void relabel_kernel(int32_t* lab, int64_t n, const State* stp, const 
 // sizes moves these regions.  list_kernel records the new layout at its end.
 __global__ void guard_kernel(WsHeader* h, unsigned long long stamp, Layout L, long long n,
                              const int32_t* sizes, int P, int policy) {
+  pdl_wait();
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     State* st = L.state;
     st->n = (int)n;
@@ -541,17 +545,18 @@ static int merge_run(int32_t* labels, const Geoms& gs, int P, int policy, const 
   const unsigned long long stamp = ((unsigned long long)l.cap_log2 << 40) | (unsigned long long)n;
   // the guard usually finds the stamp unchanged and exits: one block per SM
   // is enough for the rare full clear
-  mrg::guard_kernel<<<di.sm_count, mrg::kThreads, 0, st>>>(l.hdr, stamp, l, n, sizes, P, policy);
+  launch_pdl(mrg::guard_kernel, dim3(di.sm_count), dim3(mrg::kThreads), 0, st, l.hdr, stamp, l,
+             (long long)n, sizes, P, policy);
   SG_TRY(launch_status());
   if (!d_sizes) SG_CUDA_TRY(cudaMemsetAsync(l.size, 0, sizeof(int32_t) * (size_t)n, st));
   if (ref) SG_CUDA_TRY(cudaMemsetAsync(l.sum, 0, sizeof(double) * (size_t)n, st));
   if (!d_sizes || ref) {
-    mrg::size_kernel<<<grid, mrg::kThreads, 0, st>>>(labels, n, l, !d_sizes,
-                                                      ref ? chroma : nullptr, &l.hdr->status);
+    launch_pdl(mrg::size_kernel, dim3(grid), dim3(mrg::kThreads), 0, st, labels, n, l, !d_sizes,
+               ref ? chroma : nullptr, &l.hdr->status);
     SG_TRY(launch_status());
   }
-  mrg::pair_kernel<<<gs.total_tiles, mrg::kThreads, 0, st>>>(labels, gs, l, sizes, P,
-                                                              &l.hdr->status);
+  launch_pdl(mrg::pair_kernel, dim3(gs.total_tiles), dim3(mrg::kThreads), 0, st, labels, gs, l,
+             sizes, P, &l.hdr->status);
   SG_TRY(launch_status());
   {
     // one co-resident block per SM
@@ -570,7 +575,8 @@ static int merge_run(int32_t* labels, const Geoms& gs, int P, int policy, const 
   }
   SG_TRY(launch_status());
   if (relabel_labels) {
-    mrg::relabel_kernel<<<grid, mrg::kThreads, 0, st>>>(labels, n, l.state, l.fin);
+    launch_pdl(mrg::relabel_kernel, dim3(grid), dim3(mrg::kThreads), 0, st, labels, n,
+               (const mrg::State*)l.state, (const int32_t*)l.fin);
     SG_TRY(launch_status());
   }
   return SPLIT_OK;

@@ -135,6 +135,7 @@ __device__ __forceinline__ const CUtensorMap* pick_map(const Geoms& gs, const Ti
 template <bool R1>
 __global__ void __launch_bounds__(kThreads)
 erode_kernel(const __grid_constant__ CUtensorMap tmap, bool use_tma, ErodeArgs a, Geoms gs) {
+  pdl_wait();
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ __align__(8) uint64_t bar;
   const int R = R1 ? 1 : a.R, XP = R1 ? 4 : a.XP;
@@ -242,13 +243,15 @@ static int erode_geoms_launch(const int32_t* in, int32_t* out, const Geoms& gs, 
   ErodeArgs a{in, out, R, XP, ms, mfin, local_labels, status};
   size_t smem = (size_t)SW * SH * sizeof(int32_t);
   if (R == 1) {
-    erode_kernel<true><<<gs.total_tiles, kThreads, smem, st>>>(map, use_tma, a, gs);
+    launch_pdl(erode_kernel<true>, dim3(gs.total_tiles), dim3(kThreads), smem, st, map, use_tma, a,
+               gs);
   } else {
     smem += (size_t)TH * SW;
     if (smem > 48 * 1024)
       SG_CUDA_TRY(cudaFuncSetAttribute(erode_kernel<false>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    erode_kernel<false><<<gs.total_tiles, kThreads, smem, st>>>(map, use_tma, a, gs);
+    launch_pdl(erode_kernel<false>, dim3(gs.total_tiles), dim3(kThreads), smem, st, map, use_tma,
+               a, gs);
   }
   return launch_status();
 }
@@ -379,6 +382,7 @@ normals_kernel(const __grid_constant__ CUtensorMap tmap, bool use_tma, NormArgs 
 __global__ void __launch_bounds__(kThreads)
 normals_rgb8_kernel(const __grid_constant__ CUtensorMap tmap, bool use_tma, NormArgs a,
                     Geoms gs) {
+  pdl_wait();
   constexpr int SWB = 3 * TW + 32, SH = TH + 2, HP = TW + 2;
   __shared__ __align__(128) unsigned char bytes[SWB * SH];
   __shared__ float lum[SH * HP];
@@ -665,7 +669,8 @@ int normals_rgb8_geoms(const uint8_t* rgb, const Geoms& gs, float depth, float* 
                            stn::TH + 2) == SPLIT_OK;
   stn::NormArgs a{nullptr, rgb, normals, 1.0f / fmaxf(0.001f, depth),
                   nullptr, reinterpret_cast<float4*>(features4)};
-  stn::normals_rgb8_kernel<<<gs.total_tiles, stn::kThreads, 0, st>>>(map, use_tma, a, gs);
+  launch_pdl(stn::normals_rgb8_kernel, dim3(gs.total_tiles), dim3(stn::kThreads), 0, st, map,
+             use_tma, a, gs);
   return launch_status();
 }
 
