@@ -226,6 +226,30 @@ int split_compress_labels(int32_t* labels, int64_t n, int32_t* d_count,
                           void* workspace, size_t workspace_bytes,
                           void* stream);
 
+/* Replaces split::device::ccl::segment_adjacency_edges
+ * (segment_adjacency.cuh:14-16, segment_adjacency.cu:170-254): for every
+ * pixel i in index order and every in-image neighbour j in the order NW, N,
+ * NE, W, E, SW, S, SE whose label differs, one edge (i, j).  The m sources
+ * are written to edges[0, m) and the targets to edges[m, 2m); `edges` must
+ * hold 16 * width * height ints (as the reference's).  m is written to
+ * *d_count (device int).  width * height must be below 2^27. */
+size_t split_segment_adjacency_edges_workspace_size(int width, int height);
+int split_segment_adjacency_edges(const int32_t* labels, int width, int height,
+                                  int32_t* edges, int32_t* d_count, void* workspace,
+                                  size_t workspace_bytes, void* stream);
+
+/* Replaces split::device::ccl::segment_adjacency (segment_adjacency.cuh:
+ * 21-24, segment_adjacency.cu:256-289): the distinct (label, neighbouring
+ * label) pairs of those edges, sorted by key then by value, into keys[k] /
+ * adjacency[k] (each must hold 8 * width * height ints, as the reference's
+ * edge-count bound); their number is written to *d_count (device int).  Any
+ * int labels.  The workspace holds two sort buffers of 8 * width * height
+ * 64-bit keys. */
+size_t split_segment_adjacency_workspace_size(int width, int height);
+int split_segment_adjacency(const int32_t* labels, int width, int height, int32_t* keys,
+                            int32_t* adjacency, int32_t* d_count, void* workspace,
+                            size_t workspace_bytes, void* stream);
+
 /* ======================================================================== */
 /* small-segment merge                                                      */
 /* ======================================================================== */

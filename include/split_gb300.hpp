@@ -254,6 +254,41 @@ inline int compress_labels(view1d<int> labels, Temp& temp, cudaStream_t stream =
   return count;
 }
 
+/* ccl/segment_adjacency.cuh:14-16.  `edges` holds 16 entries per pixel;
+ * returns the edge count m (sources in edges[0, m), targets in edges[m, 2m);
+ * synchronises `stream`, as the reference's host-side return does). */
+inline int segment_adjacency_edges(const_view2d<int> labels, view1d<int> edges, Temp& temp,
+                                   cudaStream_t stream = nullptr) {
+  const int w = (int)labels.num_cols(), h = (int)labels.num_rows();
+  temp.reserve(split_segment_adjacency_edges_workspace_size(w, h));
+  check(split_segment_adjacency_edges(labels.data(), w, h, edges.data(), temp.scalar(1),
+                                      temp.get(), temp.size(), stream),
+        "ccl::segment_adjacency_edges");
+  int count = 0;
+  check_cuda(cudaMemcpyAsync(&count, temp.scalar(1), sizeof(int), cudaMemcpyDeviceToHost, stream),
+             "ccl::segment_adjacency_edges: count");
+  check_cuda(cudaStreamSynchronize(stream), "ccl::segment_adjacency_edges: sync");
+  temp.check(stream);
+  return count;
+}
+
+/* ccl/segment_adjacency.cuh:21-24.  `keys` and `adjacency` hold 8 entries
+ * per pixel; returns the number of distinct sorted pairs (synchronises). */
+inline int segment_adjacency(const_view2d<int> labels, view1d<int> keys, view1d<int> adjacency,
+                             Temp& temp, cudaStream_t stream = nullptr) {
+  const int w = (int)labels.num_cols(), h = (int)labels.num_rows();
+  temp.reserve(split_segment_adjacency_workspace_size(w, h));
+  check(split_segment_adjacency(labels.data(), w, h, keys.data(), adjacency.data(),
+                                temp.scalar(1), temp.get(), temp.size(), stream),
+        "ccl::segment_adjacency");
+  int count = 0;
+  check_cuda(cudaMemcpyAsync(&count, temp.scalar(1), sizeof(int), cudaMemcpyDeviceToHost, stream),
+             "ccl::segment_adjacency: count");
+  check_cuda(cudaStreamSynchronize(stream), "ccl::segment_adjacency: sync");
+  temp.check(stream);
+  return count;
+}
+
 /* ccl/merge_small_segments.cuh:21-22 (the segment count is not needed). */
 inline std::size_t merge_small_segments_workspace(int npoints, int nsegments, int width) {
   (void)nsegments;

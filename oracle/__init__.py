@@ -319,3 +319,41 @@ def propagate_centroids(labels: np.ndarray, centroids: np.ndarray) -> np.ndarray
     the centroid columns by label).  Returns (D, N) float32."""
     c = np.asarray(centroids, np.float32)
     return np.ascontiguousarray(c[:, np.asarray(labels).reshape(-1)])
+
+
+# 8-neighbourhood in the order of NeighbourKeys (segment_adjacency.cu:112-142)
+_NEIGHBOURS = ((-1, -1), (0, -1), (1, -1), (-1, 0), (1, 0), (-1, 1), (0, 1), (1, 1))
+
+
+def segment_adjacency_edges(labels: np.ndarray):
+    """segment_adjacency_edges (segment_adjacency.cu:170-254): for every pixel
+    i in index order and every in-image neighbour j in the order NW, N, NE,
+    W, E, SW, S, SE with a different label, the edge (i, j).  Returns the
+    (sources, targets) arrays."""
+    lab = np.ascontiguousarray(labels, np.int32)
+    h, w = lab.shape
+    flat = lab.ravel()
+    idx = np.arange(h * w, dtype=np.int64)
+    x, y = idx % w, idx // w
+    tgt = np.full((h * w, 8), -1, np.int64)
+    for d, (dx, dy) in enumerate(_NEIGHBOURS):
+        nx, ny = x + dx, y + dy
+        ok = (nx >= 0) & (nx < w) & (ny >= 0) & (ny < h)
+        tgt[ok, d] = (ny * w + nx)[ok]
+    src = np.repeat(idx, 8)
+    tgt = tgt.ravel()
+    keep = tgt >= 0
+    keep[keep] = flat[src[keep]] != flat[tgt[keep]]
+    return src[keep].astype(np.int32), tgt[keep].astype(np.int32)
+
+
+def segment_adjacency(labels: np.ndarray):
+    """segment_adjacency (segment_adjacency.cu:256-289): the distinct
+    (labels[i], labels[j]) pairs of the edges, sorted by key then value.
+    Returns the (keys, adjacency) arrays."""
+    flat = np.ascontiguousarray(labels, np.int32).ravel()
+    s, t = segment_adjacency_edges(labels)
+    if s.size == 0:
+        return np.zeros(0, np.int32), np.zeros(0, np.int32)
+    pairs = np.unique(np.stack([flat[s], flat[t]], axis=1), axis=0)
+    return pairs[:, 0].astype(np.int32), pairs[:, 1].astype(np.int32)

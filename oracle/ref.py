@@ -33,6 +33,8 @@ def load():
             "ref_compress_labels": [vp, i32],
             "ref_merge_small_segments": [vp, vp, i32, i32, i32],
             "ref_erode": [vp, i32, i32, i32],
+            "ref_segment_adjacency_edges": [vp, i32, i32, vp],
+            "ref_segment_adjacency": [vp, i32, i32, vp, vp],
             "ref_sobel_normals": [vp, i32, i32, f32, vp],
             "ref_propagate_centroids": [vp, i32, vp, i32, i32, vp],
             "ref_rgb_to_lab": [vp, i32, vp],
@@ -135,6 +137,27 @@ def merge_smooth_boundaries(points, labels, nsegments, threshold=0.01):
     with quiet():
         lib.ref_merge_smooth_boundaries(_p(p), _p(a), w, h, int(nsegments), float(threshold))
     return a
+
+
+def segment_adjacency_edges(labels):
+    """segment_adjacency_edges (segment_adjacency.cu:170-254): (sources,
+    targets) of the reference's own edge list."""
+    a = np.ascontiguousarray(labels, np.int32)
+    h, w = a.shape
+    out = np.zeros(16 * a.size, np.int32)
+    m = load().ref_segment_adjacency_edges(_p(a), w, h, _p(out))
+    return out[:m].copy(), out[m:2 * m].copy()
+
+
+def segment_adjacency(labels):
+    """segment_adjacency (segment_adjacency.cu:256-289): (keys, adjacency) of
+    the reference's distinct sorted label pairs."""
+    a = np.ascontiguousarray(labels, np.int32)
+    h, w = a.shape
+    k = np.zeros(8 * a.size, np.int32)
+    v = np.zeros(8 * a.size, np.int32)
+    m = load().ref_segment_adjacency(_p(a), w, h, _p(k), _p(v))
+    return k[:m].copy(), v[:m].copy()
 
 
 def erode(labels, niter=1):

@@ -19,6 +19,7 @@
 #include "split/device/ccl/connected_components.cuh"
 #include "split/device/ccl/merge_small_segments.cuh"
 #include "split/device/ccl/merge_smooth_boundaries.cuh"
+#include "split/device/ccl/segment_adjacency.cuh"
 #include "split/device/kmeans/centroids.cuh"
 #include "split/device/kmeans/cluster.cuh"
 #include "split/device/kmeans/label.cuh"
@@ -162,6 +163,31 @@ int ref_merge_smooth_boundaries(const float* pts, int32_t* labels, int w, int h,
   split::device::ccl::merge_smooth_boundaries(P, nsegments, L, t.p, threshold);
   to_host(L, labels, n);
   return 0;
+}
+
+// segment_adjacency_edges (segment_adjacency.cu:170-254): the m sources then
+// the m targets into `edges` (room for 2 m); returns m.
+int ref_segment_adjacency_edges(const int32_t* labels, int w, int h, int32_t* edges) {
+  const std::size_t n = (std::size_t)w * h;
+  IMat L(h, w);
+  to_dev(L, labels, n);
+  IVec E(16 * n);
+  const int m = split::device::ccl::segment_adjacency_edges(L, E);
+  thrust::copy(E.begin(), E.begin() + 2 * (std::size_t)m, edges);
+  return m;
+}
+
+// segment_adjacency (segment_adjacency.cu:256-289): the distinct sorted label
+// pairs into keys / adj (room for their number); returns it.
+int ref_segment_adjacency(const int32_t* labels, int w, int h, int32_t* keys, int32_t* adj) {
+  const std::size_t n = (std::size_t)w * h;
+  IMat L(h, w);
+  to_dev(L, labels, n);
+  IVec K(8 * n), A(8 * n);
+  const int m = split::device::ccl::segment_adjacency(L, K, A);
+  thrust::copy(K.begin(), K.begin() + m, keys);
+  thrust::copy(A.begin(), A.begin() + m, adj);
+  return m;
 }
 
 int ref_erode(int32_t* labels, int w, int h, int niter) {

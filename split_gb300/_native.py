@@ -44,6 +44,10 @@ _SIGS = {
     "split_ccl": (_i32, [_vp, _i32, _i32, _i32, _i32, _vp, _vp, _vp, _sz, _vp]),
     "split_compress_labels_workspace_size": (_sz, [_i64]),
     "split_compress_labels": (_i32, [_vp, _i64, _vp, _vp, _sz, _vp]),
+    "split_segment_adjacency_edges_workspace_size": (_sz, [_i32, _i32]),
+    "split_segment_adjacency_edges": (_i32, [_vp, _i32, _i32, _vp, _vp, _vp, _sz, _vp]),
+    "split_segment_adjacency_workspace_size": (_sz, [_i32, _i32]),
+    "split_segment_adjacency": (_i32, [_vp, _i32, _i32, _vp, _vp, _vp, _vp, _sz, _vp]),
     "split_merge_small_workspace_size": (_sz, [_i32, _i32]),
     "split_merge_small": (_i32, [_vp, _i32, _i32, _i32, _i32, _vp, _vp, _vp, _sz, _vp]),
     "split_erode": (_i32, [_vp, _vp, _i32, _i32, _i32, _vp]),

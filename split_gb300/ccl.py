@@ -62,6 +62,62 @@ def compress_labels(labels: torch.Tensor, temp: Workspace | None = None, *,
     return int(count.item())
 
 
+def segment_adjacency_edges_workspace(width: int, height: int) -> int:
+    return N.load().split_segment_adjacency_edges_workspace_size(width, height)
+
+
+def segment_adjacency_edges(labels: torch.Tensor, edges: torch.Tensor,
+                            temp: Workspace | None = None, *, stream=None) -> int:
+    """split::device::ccl::segment_adjacency_edges (segment_adjacency.cuh:14-16).
+
+    labels: (H, W) int32; edges: int32 with room for 16 * H * W entries.
+    Writes the m edge sources to edges[:m] and their targets to
+    edges[m:2m] and returns m (synchronises, as the reference's return value
+    does)."""
+    require_cuda(labels, "labels", torch.int32)
+    require_cuda(edges, "edges", torch.int32)
+    if labels.dim() != 2:
+        raise ValueError("labels must be (height, width)")
+    h, w = labels.shape
+    if edges.numel() < 16 * h * w:
+        raise ValueError("edges must hold 16 entries per pixel")
+    ws = ensure_workspace(temp, segment_adjacency_edges_workspace(w, h), labels.device)
+    count = torch.zeros(1, dtype=torch.int32, device=labels.device)
+    st = N.load().split_segment_adjacency_edges(ptr(labels), w, h, ptr(edges), ptr(count),
+                                                ws.ptr, ws.nbytes, stream_handle(stream))
+    N.check(st, "ccl.segment_adjacency_edges")
+    ws.check("ccl.segment_adjacency_edges", stream)
+    return int(count.item())
+
+
+def segment_adjacency_workspace(width: int, height: int) -> int:
+    return N.load().split_segment_adjacency_workspace_size(width, height)
+
+
+def segment_adjacency(labels: torch.Tensor, keys: torch.Tensor, adjacency: torch.Tensor,
+                      temp: Workspace | None = None, *, stream=None) -> int:
+    """split::device::ccl::segment_adjacency (segment_adjacency.cuh:21-24).
+
+    labels: (H, W) int32; keys, adjacency: int32 with room for 8 * H * W
+    entries each.  Writes the distinct (label, neighbouring label) pairs,
+    sorted by key then value, and returns their number (synchronises)."""
+    require_cuda(labels, "labels", torch.int32)
+    require_cuda(keys, "keys", torch.int32)
+    require_cuda(adjacency, "adjacency", torch.int32)
+    if labels.dim() != 2:
+        raise ValueError("labels must be (height, width)")
+    h, w = labels.shape
+    if keys.numel() < 8 * h * w or adjacency.numel() < 8 * h * w:
+        raise ValueError("keys and adjacency must hold 8 entries per pixel")
+    ws = ensure_workspace(temp, segment_adjacency_workspace(w, h), labels.device)
+    count = torch.zeros(1, dtype=torch.int32, device=labels.device)
+    st = N.load().split_segment_adjacency(ptr(labels), w, h, ptr(keys), ptr(adjacency),
+                                          ptr(count), ws.ptr, ws.nbytes, stream_handle(stream))
+    N.check(st, "ccl.segment_adjacency")
+    ws.check("ccl.segment_adjacency", stream)
+    return int(count.item())
+
+
 def merge_small_segments_workspace(width: int, height: int) -> int:
     return N.load().split_merge_small_workspace_size(width, height)
 

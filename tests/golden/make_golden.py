@@ -11,10 +11,14 @@ so a generator change is caught.
     python tests/golden/make_golden.py ic         # ic_golden.npz
     python tests/golden/make_golden.py threshold  # kmeans_threshold_golden.npz
     python tests/golden/make_golden.py smooth     # smooth_golden.npz
+    python tests/golden/make_golden.py adjacency  # adjacency_golden.npz
 
 Known limit of the CPU build: CCCL 3.0.1's host sort orders negative int keys
 after non-negative ones, so compress_labels is only recorded on non-negative
-labels (the reference's GPU build sorts with CUB and is not affected).
+labels (the reference's GPU build sorts with CUB and is not affected); the
+same holds for segment_adjacency.  The CPU build's segment_adjacency_edges
+runs Thrust's in-place remove_if, which races with more than one OpenMP
+thread: the adjacency fixtures are made with one thread.
 """
 from __future__ import annotations
 
@@ -33,6 +37,7 @@ OUT_LAB = os.path.join(HERE, "lab_beta_golden.npz")
 OUT_IC = os.path.join(HERE, "ic_golden.npz")
 OUT_THR = os.path.join(HERE, "kmeans_threshold_golden.npz")
 OUT_SMOOTH = os.path.join(HERE, "smooth_golden.npz")
+OUT_ADJ = os.path.join(HERE, "adjacency_golden.npz")
 SMOOTH_THRESHOLDS = (0.01, 0.03, 0.1)
 THRESHOLDS = (1e-3, 1e-2, 0.0145)
 
@@ -127,6 +132,35 @@ def main_smooth():
     print(f"wrote {OUT_SMOOTH} ({os.path.getsize(OUT_SMOOTH) / 1024:.0f} KiB)")
 
 
+def adjacency_inputs():
+    """Label images for segment adjacency: the smooth-merge segments (160 x
+    120, compressed), seeded random labels in [0, 10) (37 x 53, most pixels
+    on a boundary), a single row and a single column, and one value only."""
+    _, seg, _, _ = smooth_inputs()
+    rng = np.random.default_rng(0xAD)
+    return {"segments": seg.astype(np.int32),
+            "random": rng.integers(0, 10, size=(37, 53)).astype(np.int32),
+            "row": rng.integers(0, 3, size=(1, 41)).astype(np.int32),
+            "column": rng.integers(0, 3, size=(29, 1)).astype(np.int32),
+            "flat": np.full((9, 14), 7, np.int32)}
+
+
+def main_adjacency():
+    """segment_adjacency_edges and segment_adjacency of the reference
+    (segment_adjacency.cu:170-289) on adjacency_inputs()."""
+    os.environ["OMP_NUM_THREADS"] = "1"
+    from oracle import ref
+    g = {}
+    for name, lab in adjacency_inputs().items():
+        g[f"sha_{name}"] = np.array(sha(lab))
+        src, tgt = ref.segment_adjacency_edges(lab)
+        keys, adj = ref.segment_adjacency(lab)
+        g[f"{name}_src"], g[f"{name}_tgt"] = src, tgt
+        g[f"{name}_keys"], g[f"{name}_adj"] = keys, adj
+    np.savez_compressed(OUT_ADJ, **g)
+    print(f"wrote {OUT_ADJ} ({os.path.getsize(OUT_ADJ) / 1024:.0f} KiB)")
+
+
 def main_threshold():
     """cluster(points, c0, 100, threshold) on the 512 x 512 k-means input, for
     a few thresholds: the reference's iteration count (cluster.cu:71), the
@@ -191,5 +225,7 @@ elif __name__ == "__main__" and sys.argv[1:] == ["threshold"]:
     main_threshold()
 elif __name__ == "__main__" and sys.argv[1:] == ["smooth"]:
     main_smooth()
+elif __name__ == "__main__" and sys.argv[1:] == ["adjacency"]:
+    main_adjacency()
 elif __name__ == "__main__":
     main()

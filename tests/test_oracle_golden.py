@@ -188,3 +188,24 @@ def test_merge_smooth_boundaries(i):
     assert make_golden.sha(lab) == str(SMOOTH["labels_sha"]) and s == int(SMOOTH["nsegments"])
     got = oracle.merge_smooth(lab, pts, float(SMOOTH["thresholds"][i]))
     assert np.array_equal(got, SMOOTH[f"merged_{i}"])
+
+
+ADJ = np.load(os.path.join(HERE, "golden", "adjacency_golden.npz"))
+ADJ_CASES = ("segments", "random", "row", "column", "flat")
+
+
+@pytest.fixture(scope="module")
+def adj_inputs():
+    return make_golden.adjacency_inputs()
+
+
+@pytest.mark.parametrize("name", ADJ_CASES)
+def test_segment_adjacency_restatement(adj_inputs, name):
+    """The oracle's edge list and sorted distinct pairs equal the reference's
+    (segment_adjacency.cu:170-289), element by element."""
+    lab = adj_inputs[name]
+    assert make_golden.sha(lab) == str(ADJ[f"sha_{name}"])
+    src, tgt = oracle.segment_adjacency_edges(lab)
+    assert np.array_equal(src, ADJ[f"{name}_src"]) and np.array_equal(tgt, ADJ[f"{name}_tgt"])
+    keys, adj = oracle.segment_adjacency(lab)
+    assert np.array_equal(keys, ADJ[f"{name}_keys"]) and np.array_equal(adj, ADJ[f"{name}_adj"])
