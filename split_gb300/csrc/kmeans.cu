@@ -558,8 +558,8 @@ enum SpanKind { kSpanSingle = 0, kSpanPair = 1, kSpanAny = 2 };
 template <int LAYOUT, int DIM, int MODE, int KIND>
 __device__ __forceinline__ void span_batches(const Image& im, Smem& sm, int warp, int row_first,
                                              int col, int nbatches, unsigned long long mask,
-                                             int ka, int kb, bool write_labels, int& acc_l,
-                                             int& acc_n, float (&acc)[DIM]) {
+                                             int ka, int kb, bool write_labels, bool vec_labels,
+                                             int& acc_l, int& acc_n, float (&acc)[DIM]) {
   constexpr int CS = cstride(DIM);
   const int64_t step = (int64_t)kBatchRows * im.width;
   int64_t px0 = (int64_t)row_first * im.width + col;
@@ -652,8 +652,14 @@ __device__ __forceinline__ void span_batches(const Image& im, Smem& sm, int warp
     } else {
       nearest_px<DIM>(f, sm.cent, mask, lab);
     }
-    if (write_labels)
-      *reinterpret_cast<int4*>(im.labels + px0) = make_int4(lab[0], lab[1], lab[2], lab[3]);
+    if (write_labels) {
+      if (vec_labels) {
+        *reinterpret_cast<int4*>(im.labels + px0) = make_int4(lab[0], lab[1], lab[2], lab[3]);
+      } else {
+#pragma unroll
+        for (int j = 0; j < kPx; ++j) im.labels[px0 + j] = lab[j];
+      }
+    }
     if (MODE != kAssignOnly) {
       if (KIND == kSpanSingle) {
         // the same sums, in the same order, as accumulate_valid's uniform case
@@ -691,8 +697,8 @@ __device__ __forceinline__ void span_batches(const Image& im, Smem& sm, int warp
 template <int LAYOUT, int DIM, int MODE>
 __device__ __forceinline__ void fast_span(const Image& im, Smem& sm, int warp, int row_first,
                                           int col, int nbatches, unsigned long long mask,
-                                          bool write_labels, int& acc_l, int& acc_n,
-                                          float (&acc)[DIM]) {
+                                          bool write_labels, bool vec_labels, int& acc_l,
+                                          int& acc_n, float (&acc)[DIM]) {
   constexpr int CS = cstride(DIM);
   // A mask with one cluster names every pixel's nearest centroid outright:
   // the span's box excludes all others for every pixel it holds (and the
@@ -723,13 +729,13 @@ __device__ __forceinline__ void fast_span(const Image& im, Smem& sm, int warp, i
   }
   if (kind == kSpanSingle)
     span_batches<LAYOUT, DIM, MODE, kSpanSingle>(im, sm, warp, row_first, col, nbatches, mask, ka,
-                                                 kb, write_labels, acc_l, acc_n, acc);
+                                                 kb, write_labels, vec_labels, acc_l, acc_n, acc);
   else if (kind == kSpanPair)
     span_batches<LAYOUT, DIM, MODE, kSpanPair>(im, sm, warp, row_first, col, nbatches, mask, ka,
-                                               kb, write_labels, acc_l, acc_n, acc);
+                                               kb, write_labels, vec_labels, acc_l, acc_n, acc);
   else
     span_batches<LAYOUT, DIM, MODE, kSpanAny>(im, sm, warp, row_first, col, nbatches, mask, ka,
-                                              kb, write_labels, acc_l, acc_n, acc);
+                                              kb, write_labels, vec_labels, acc_l, acc_n, acc);
 }
 
 // Process one unit (a 64 x 64 tile): assign (unless update-only) and
@@ -784,14 +790,16 @@ __device__ void process_unit(const Image& im, int unit, Smem& sm, bool write_lab
 #pragma unroll
   for (int d = 0; d < DIM; ++d) acc[d] = 0.0f;
 
-  const bool fast = MODE != kUpdateOnly && unit_box && vec_labels && rows_in == wrows &&
-                    cols_in == kTile &&
+  // float4 features: any width (labels stored one by one where a row's
+  // start is not 16-byte aligned); RGB8 read as 32-bit words needs
+  // 4-pixel-aligned rows
+  const bool fast = MODE != kUpdateOnly && unit_box && rows_in == wrows && cols_in == kTile &&
                     (LAYOUT == SPLIT_LAYOUT_FLOAT4 ||
-                     (LAYOUT == SPLIT_LAYOUT_RGB8 &&
+                     (LAYOUT == SPLIT_LAYOUT_RGB8 && vec_labels &&
                       (reinterpret_cast<uintptr_t>(im.points) & 3) == 0));
   if (fast)
     fast_span<LAYOUT, DIM, MODE>(im, sm, warp, row0 + lrow, col0 + lcol, wrows / kBatchRows,
-                                 span_mask, write_labels, acc_l, acc_n, acc);
+                                 span_mask, write_labels, vec_labels, acc_l, acc_n, acc);
   for (int b = 0; !fast && b < wrows / kBatchRows; ++b) {
     if (b * kBatchRows >= rows_in) break;
     const int row = row0 + b * kBatchRows + lrow;

@@ -205,7 +205,10 @@ def test_kmeans_assign_pruning_exact(cuda, k):
 
 
 def test_kmeans_unit_range_flag(cuda):
-    """The unit-range promise on packed features changes no label."""
+    """The unit-range promise on packed features changes no label.  It moves
+    whole spans onto the fast path, whose spans with two candidate clusters
+    sum in another fixed order than the per-batch path: the centroids agree
+    to a few ulp (and each run is deterministic)."""
     import torch
     from split_gb300 import color, kmeans
     w, h = 333, 211
@@ -223,7 +226,12 @@ def test_kmeans_unit_range_flag(cuda):
                        width=w)
         out.append((lab.cpu().numpy(), cent.cpu().numpy()))
     for lab, cent in out[1:]:
-        assert np.array_equal(lab, out[0][0]) and np.array_equal(cent, out[0][1])
+        assert np.array_equal(lab, out[0][0])
+        rel = np.abs(cent - out[0][1]) / np.maximum(np.abs(out[0][1]), 1e-30)
+        assert rel.max() <= 1e-6, rel.max()
+    # the per-batch paths (float4 without the promise, and RGB8 at a width
+    # that is not a multiple of 4) are the same computation
+    assert np.array_equal(out[2][1], out[0][1])
 
 
 def test_workspace_reuse_across_sizes(cuda):
