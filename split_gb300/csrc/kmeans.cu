@@ -851,7 +851,15 @@ __device__ void process_unit(const Image& im, int unit, Smem& sm, bool write_lab
         }
         mask = candidates<DIM>(lo, hi, sm.cent, im.K);
       }
-      nearest_px<DIM>(f, sm.cent, mask, lab);
+      if (unit_box && mask != 0ull && (mask & (mask - 1ull)) == 0ull) {
+        // one candidate for the span names every pixel's label (features in
+        // the unit cube: none is NaN), as on the fast path
+        const int k1 = __ffsll((long long)mask) - 1;
+#pragma unroll
+        for (int j = 0; j < kPx; ++j) lab[j] = k1;
+      } else {
+        nearest_px<DIM>(f, sm.cent, mask, lab);
+      }
       if (write_labels) {
         if (all_ok && vec_labels) {
           *reinterpret_cast<int4*>(im.labels + px0) = make_int4(lab[0], lab[1], lab[2], lab[3]);
