@@ -385,6 +385,26 @@ def test_ccl_stress_8192_maze(cuda):
     ws.check("ccl")
 
 
+def test_merge_stress_8192_maze(cuda):
+    """Merge stress case: the 8192 x 8192 maze's 8-connected components (the
+    corridor and 1.39 M pieces of its random blobs, 108,519 of them at least
+    64 px) merged below 64 px into the neighbour sharing most boundary,
+    bit-exact against the oracle."""
+    import torch
+    from split_gb300 import ccl
+    n = 8192
+    lab = synth.maze_labels(2024, n, n)
+    seg = oracle.ccl(lab, 8, 0)
+    g = _t(seg, cuda)
+    ws = ccl.merge_small_segments(None, g, None, 64, policy=ccl.MOST_BOUNDARY)
+    torch.cuda.synchronize()
+    ws.check("merge")
+    want = oracle.merge_small(seg, 64, 0)
+    got = g.cpu().numpy()
+    assert np.array_equal(got, want), f"{int((got != want).sum())} labels differ"
+    assert len(np.unique(want)) < len(np.unique(seg))
+
+
 @pytest.mark.parametrize("layout,dim", [(0, 3), (1, 3), (2, 3), (2, 5), (0, 5)])
 def test_segment_means_many_clusters(cuda, layout, dim):
     """calculate_centroids with K = number of segments (thousands): per-segment
