@@ -533,10 +533,12 @@ def run_next_rows(dev, pipe, rgb, reps=7):
 
 
 def run_stress(dev, side=8192, steps=10, seed=2024):
-    """Labelling stress case: side x side maze + blob labels (one serpentine
-    corridor over half the pixels), 4- and 8-connected min-index CCL with
-    component sizes, device-resident (268 MB in, 268 MB out: larger than L2).
-    The oracle's union-find on one host thread is timed once beside it."""
+    """Labelling and merge stress case: side x side maze + blob labels (one
+    serpentine corridor over half the pixels), 4- and 8-connected min-index
+    CCL with component sizes, device-resident (268 MB in, 268 MB out: larger
+    than L2), then the merge of the 8-connected components below 64 px (gb_s
+    counts the 4 B/px label read of its pair pass).  The oracle's union-find
+    on one host thread is timed once beside it."""
     import numpy as np
     import torch
     import split_synth as synth
@@ -568,13 +570,35 @@ def run_stress(dev, side=8192, steps=10, seed=2024):
         res[f"ccl{conn}"] = {"ms": round(ms, 4), "mpix_s": round(npx / (ms * 1e-3) / 1e6, 1),
                              "gb_s": round(gbs, 1), "frac": round(gbs / peak, 4)}
     ws.check("stress ccl")
+    # merge of the 8-connected components below 64 px into the neighbour
+    # sharing most boundary (the components are the labelling's output, so
+    # each step starts from a copy of them; the copy is outside the events)
+    seg = out.clone()
+    work = torch.empty_like(seg)
+    mws = None
+    times = []
+    for s in range(3 + steps):
+        work.copy_(seg)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        mws = ccl.merge_small_segments(None, work, mws, 64, policy=ccl.MOST_BOUNDARY)
+        e1.record()
+        torch.cuda.synchronize()
+        if s >= 3:
+            times.append(e0.elapsed_time(e1))
+    mws.check("stress merge")
+    ms = statistics.median(times)
+    gbs = npx * 4 / (ms * 1e-3) / 1e9
+    res["merge64"] = {"ms": round(ms, 4), "mpix_s": round(npx / (ms * 1e-3) / 1e6, 1),
+                      "segments_after": int(torch.unique(work).numel()),
+                      "gb_s": round(gbs, 1), "frac": round(gbs / peak, 4)}
     try:
         import oracle
         t = time.perf_counter()
         ref = oracle.ccl(lab, 8, 0)
         dt = time.perf_counter() - t
         res["oracle_ccl8_s"] = round(dt, 3)
-        res["identical"] = bool(np.array_equal(out.cpu().numpy(), ref))
+        res["identical"] = bool(np.array_equal(seg.cpu().numpy(), ref))
     except Exception as exc:  # the oracle is a checker here; report why it is absent
         res["oracle"] = f"unavailable: {exc}"
     return res
