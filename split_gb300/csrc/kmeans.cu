@@ -1191,8 +1191,17 @@ __global__ void __launch_bounds__(kThreads, SG_KM_MINBLOCKS) kmeans_kernel(Param
       }
       // the last warp fetches the next unit (slot k & 1 was last read before
       // the barrier that ended unit k - 1)
-      if (threadIdx.x == kThreads - 32)
+      if (threadIdx.x == kThreads - 32) {
+        if (MODE != kAssignOnly && !more && p.nimages > 1) {
+          // a batch image that has stopped: later fetches skip the rest of its
+          // units (which only changes who does which unit, not any result)
+          const int ub = im.unit_begin, ue = ub + im.nunits;
+          const int raw_end = (it & 1) ? p.total_units - ub : ue;
+          if (raw_end > (int)gridDim.x)
+            atomicMax(&p.hdr->work_counter[it & 1], (unsigned)(raw_end - (int)gridDim.x));
+        }
         sm.next[k & 1] = (int)gridDim.x + (int)atomicAdd(&p.hdr->work_counter[it & 1], 1u);
+      }
       __syncthreads();
       raw = sm.next[k & 1];
     }
