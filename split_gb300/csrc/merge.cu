@@ -93,30 +93,45 @@ __device__ __forceinline__ unsigned long long pair_key(int s, int t) {
 __device__ __forceinline__ int key_s(unsigned long long k) { return (int)((k - 1ull) >> 32); }
 __device__ __forceinline__ int key_t(unsigned long long k) { return (int)(unsigned)((k - 1ull) & 0xffffffffull); }
 
-// Inserts (s, t) with multiplicity m.  A new pair beyond half the capacity
-// (or a probe sequence that runs out) flags the overflow instead.
-__device__ void insert(const Layout& L, int s, int t, unsigned m) {
+// Inserts (s, t) with multiplicity m.  A new pair that takes the table past
+// half its capacity (or a probe sequence that runs out) flags the overflow
+// and returns true: the caller then stops inserting (the pass decides class
+// by class instead), and so does every tile that starts after the flag is
+// set, so the table never grows past half by more than the lanes running at
+// once.  Every claimed slot is listed (the list holds as many entries as the
+// table), so the table can always be cleared through the list.  The list
+// counter is one word that every new pair increments: the lanes of a warp
+// that claim slots in the same step take their list places with one atomic,
+// and nothing else reads that word during the pass.
+__device__ bool insert(const Layout& L, int s, int t, unsigned m) {
   const unsigned long long key = pair_key(s, t);
   const unsigned mask = (1u << L.cap_log2) - 1u;
   unsigned h = (unsigned)((key * 0x9E3779B97F4A7C15ull) >> (64 - L.cap_log2));
   for (int probe = 0; probe < kProbeCap; ++probe, h = (h + 1) & mask) {
     unsigned long long k = *(volatile unsigned long long*)(L.keys + h);
     if (k == 0ull) {
-      if (*(volatile unsigned*)&L.state->list_count >= (mask >> 1)) break;
       k = atomicCAS(L.keys + h, 0ull, key);
       if (k == 0ull) {
         atomicAdd(L.counts + h, m);
-        const unsigned idx = atomicAdd(&L.state->list_count, 1u);
+        const unsigned am = __activemask();
+        const int lane = threadIdx.x & 31, leader = __ffs(am) - 1;
+        unsigned base = 0;
+        if (lane == leader) base = atomicAdd(&L.state->list_count, (unsigned)__popc(am));
+        base = __shfl_sync(am, base, leader);
+        const unsigned idx = base + __popc(am & ((1u << lane) - 1u));
         L.list[idx] = (int)h;
-        return;
+        if (idx < (mask >> 1)) return false;
+        *(volatile int*)&L.state->overflow = 1;
+        return true;
       }
     }
     if (k == key) {
       atomicAdd(L.counts + h, m);
-      return;
+      return false;
     }
   }
   *(volatile int*)&L.state->overflow = 1;
+  return true;
 }
 
 // Class of segment s at split level `lev`: the top lev bits of a hash of s
@@ -161,6 +176,11 @@ __device__ __forceinline__ void pair_tile(const int32_t* __restrict__ lab, const
   const long long n = gs.total_px;
   const TileRef tr = tile_ref(gs, tile);
   const int W = tr.W, H = tr.H;
+  // an overflow flagged before the tile starts: nothing more to insert
+  __shared__ int stopped;
+  if (threadIdx.x == 0) stopped = *(volatile int*)&L.state->overflow;
+  __syncthreads();
+  bool go = stopped == 0;
   // all label loads, then all size gathers, before any pixel is examined:
   // the eight pixels' dependent load pairs overlap instead of serialising
   constexpr int kPer = kTileH * kTileW / kThreads;
@@ -200,7 +220,7 @@ __device__ __forceinline__ void pair_tile(const int32_t* __restrict__ lab, const
       for (int b = 0; b < a; ++b) first &= (t[b] != t[a]);
       if (!first) continue;
       for (int b = a + 1; b < nt; ++b) m += (t[b] == t[a]);
-      insert(L, s, t[a], m);
+      if (go && insert(L, s, t[a], m)) go = false;
     }
   }
 }
