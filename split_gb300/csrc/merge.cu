@@ -29,6 +29,8 @@
 // split in two again.  Bids only compare pairs of one segment, so rounds over
 // disjoint classes decide exactly what one pass over a large enough table
 // would.  The chains then resolve over the decided segments.
+#include <algorithm>
+
 #include "geom.cuh"
 #include "merge_state.cuh"
 
@@ -579,18 +581,23 @@ static int merge_run(int32_t* labels, const Geoms& gs, int P, int policy, const 
              sizes, P, &l.hdr->status);
   SG_TRY(launch_status());
   {
-    // one co-resident block per SM
+    // One co-resident block per SM: the lists of most images are short and
+    // the decision is bound by its grid barriers, which slow with the block
+    // count.  Images and arenas of 2^24 pixels and more can hold lists of
+    // millions of pairs, walked with a dependent load or two per entry:
+    // there as many blocks as fit, up to 4 per SM.
     int per_sm = 0;
     SG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mrg::list_kernel,
                                                               mrg::kThreads, 0));
     if (per_sm < 1) return SPLIT_ERR_UNSUPPORTED;
+    const int list_blocks = di.sm_count * (n >= ((int64_t)1 << 24) ? std::min(per_sm, 4) : 1);
     unsigned long long stamp_arg = stamp;
     int P_arg = P, policy_arg = policy;
     const int32_t* sizes_arg = sizes;
     const int32_t* lab_arg = labels;
     Geoms gs_arg = gs;
     void* args[] = {&l, &lab_arg, &gs_arg, &sizes_arg, &P_arg, &policy_arg, &stamp_arg};
-    SG_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)mrg::list_kernel, dim3(di.sm_count),
+    SG_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)mrg::list_kernel, dim3(list_blocks),
                                             dim3(mrg::kThreads), args, 0, st));
   }
   SG_TRY(launch_status());
