@@ -1282,6 +1282,34 @@ __global__ void init_kernel(Params p) {
   }
 }
 
+// Per-call setup of a single-image clustering in one launch: the header's
+// barrier and work counters and all three accumulator slots to zero
+// (`zero` .. `zero` + zero_words: the slots and the counts), the iteration
+// state (cluster.cu:65-68), and the caller's planar centroids into slot 0.
+template <int DIM>
+__global__ void setup_kernel(Params p, unsigned* zero, int zero_words) {
+  pdl_wait();
+  const Image& im = p.img0;
+  if (threadIdx.x == 0) {
+    p.hdr->barrier_count = 0u;
+    p.hdr->barrier_gen = 0u;
+    p.hdr->work_counter[0] = 0u;
+    p.hdr->work_counter[1] = 0u;
+    ImageState st;
+    st.delta = 0.0f;
+    st.old_delta = st.delta + im.threshold + 1.0f;
+    st.iters = 0;
+    st.done = im.max_iter <= 0;
+    p.state[0] = st;
+    if (im.d_iterations && st.done) *im.d_iterations = 0;
+  }
+  for (int i = threadIdx.x; i < zero_words; i += blockDim.x) zero[i] = 0u;
+  for (int idx = threadIdx.x; idx < im.K * DIM; idx += blockDim.x) {
+    const int k = idx / DIM, d = idx % DIM;
+    p.cur[k * 8 + d] = im.centroids[d * im.K + k];
+  }
+}
+
 template <int DIM>
 __global__ void load_user_centroids(Params p) {
   pdl_wait();
@@ -1450,12 +1478,14 @@ static int run(int mode, const void* points, int layout, int dim, int64_t n,
   p.cur = l.cur;
   p.state = l.state;
   p.hdr = l.hdr;
-  SG_TRY(reset_counters(l, 1, st));
   (void)centroids_in;
-  launch_pdl(init_kernel, dim3(1), dim3(256), 0, st, p);
-  SG_TRY(launch_status());
-  if (dim == 3) launch_pdl(load_user_centroids<3>, dim3(1), dim3(256), 0, st, p);
-  else launch_pdl(load_user_centroids<5>, dim3(1), dim3(256), 0, st, p);
+  // counters, accumulator slots, state and centroids in one launch (the
+  // slots and counts lie between acc_lo and cur, 256-byte aligned pieces)
+  unsigned* zero = reinterpret_cast<unsigned*>(l.acc_lo);
+  const int zero_words = (int)((reinterpret_cast<char*>(l.cur) -
+                                reinterpret_cast<char*>(l.acc_lo)) / sizeof(unsigned));
+  if (dim == 3) launch_pdl(setup_kernel<3>, dim3(1), dim3(256), 0, st, p, zero, zero_words);
+  else launch_pdl(setup_kernel<5>, dim3(1), dim3(256), 0, st, p, zero, zero_words);
   SG_TRY(launch_status());
   if (max_iter <= 0) return SPLIT_OK;
   if (mode == kCluster) return dispatch<kCluster>(layout, dim, p, st);
