@@ -117,7 +117,11 @@ size_t split_kmeans_cluster_workspace_size_2d(int64_t npoints, int width,
  * of iterations performed is written to *d_iterations (device int) if not
  * null.  The returned labels are the assignment computed from the centroids
  * of the final iteration's input, the returned centroids the update computed
- * from those labels, as in the reference. */
+ * from those labels, as in the reference.  nclusters: 1 to 64 in one
+ * persistent launch; 65 to 2^20 (the reference sets no limit) in the
+ * many-cluster path, which queues one assignment and one forming launch per
+ * iteration (max_iter pairs; those after the device-side stop return at
+ * once) and needs the workspace size for that K. */
 int split_kmeans_cluster(const void* points, int layout, int dim,
                          int64_t npoints, int width, float xy_scale,
                          float* centroids, int nclusters, int32_t* labels,
@@ -166,7 +170,8 @@ size_t split_kmeans_assign_workspace_size(int64_t npoints, int nclusters);
 
 /* Replaces split::device::kmeans::label_points (label.cuh:27-31,
  * label.cu:74-106): nearest centroid, squared distance accumulated in
- * dimension order, ties to the lowest cluster index. */
+ * dimension order, ties to the lowest cluster index.  nclusters 1 to 2^20
+ * (above 64 through the many-cluster path). */
 int split_kmeans_assign(const void* points, int layout, int dim,
                         int64_t npoints, int width, float xy_scale,
                         const float* centroids, int nclusters, int32_t* labels,

@@ -143,9 +143,10 @@ inline std::size_t cluster_workspace(int npoints, int nclusters, int dim, int wi
 enum class Convergence { reference, l2_change };
 
 /* kmeans/cluster.cuh:31-37.  Planar D x N points (D = 3 or 5, all rows read
- * from memory), D x K centroids in/out, K <= 64 (the centroids live in shared
- * memory; a larger K throws split::device::error with SPLIT_ERR_INVALID).  Returns the iterations performed
- * (the reference returns nothing; reading the count synchronises `stream`). */
+ * from memory), D x K centroids in/out, any K up to 2^20 (K <= 64 in the
+ * persistent kernel, larger K in the many-cluster path).  Returns the
+ * iterations performed (the reference returns nothing; reading the count
+ * synchronises `stream`). */
 inline int cluster(const_view2d<float> points, view2d<float> centroids, view1d<int> labels,
                    Temp& temp, int max_iter, float threshold = 1.f, int width = 0,
                    cudaStream_t stream = nullptr,

@@ -34,6 +34,8 @@
 #include <vector>
 
 #include "common.cuh"
+#include "f32x2.cuh"
+#include "fixsum.cuh"
 
 namespace sg {
 namespace km {
@@ -185,7 +187,9 @@ __device__ __forceinline__ unsigned long long candidates(const float (&lo)[DIM],
 #pragma unroll
   for (int h = 0; h < 2; ++h) {
     const int k = lane + 32 * h;
-    lb[h] = INFINITY;
+    // a slot past K compares false even against an infinite thr (a box
+    // with an infinite feature)
+    lb[h] = __int_as_float(0x7fffffff);
     if (k < K) {
       float l = 0.0f, u = 0.0f;
 #pragma unroll
@@ -265,45 +269,6 @@ __device__ __forceinline__ void advance(int& row, int& col, int s, int w) {
     row += q;
     col -= q * w;
   }
-}
-
-// ---- packed FP32x2 helpers (per-lane IEEE round-to-nearest, so results are
-// bit-identical to the scalar __fsub_rn / __fmul_rn / __fmaf_rn forms)
-__device__ __forceinline__ float2 fsub2(float2 a, float2 b) {
-  float2 r;
-  asm("{.reg .b64 a_, b_, r_;\n\t"
-      "mov.b64 a_, {%2, %3};\n\tmov.b64 b_, {%4, %5};\n\t"
-      "sub.rn.f32x2 r_, a_, b_;\n\tmov.b64 {%0, %1}, r_;}"
-      : "=f"(r.x), "=f"(r.y)
-      : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
-  return r;
-}
-__device__ __forceinline__ float2 fadd2(float2 a, float2 b) {
-  float2 r;
-  asm("{.reg .b64 a_, b_, r_;\n\t"
-      "mov.b64 a_, {%2, %3};\n\tmov.b64 b_, {%4, %5};\n\t"
-      "add.rn.f32x2 r_, a_, b_;\n\tmov.b64 {%0, %1}, r_;}"
-      : "=f"(r.x), "=f"(r.y)
-      : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
-  return r;
-}
-__device__ __forceinline__ float2 fmul2(float2 a, float2 b) {
-  float2 r;
-  asm("{.reg .b64 a_, b_, r_;\n\t"
-      "mov.b64 a_, {%2, %3};\n\tmov.b64 b_, {%4, %5};\n\t"
-      "mul.rn.f32x2 r_, a_, b_;\n\tmov.b64 {%0, %1}, r_;}"
-      : "=f"(r.x), "=f"(r.y)
-      : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
-  return r;
-}
-__device__ __forceinline__ float2 ffma2(float2 a, float2 b, float2 c) {
-  float2 r;
-  asm("{.reg .b64 a_, b_, c_, r_;\n\t"
-      "mov.b64 a_, {%2, %3};\n\tmov.b64 b_, {%4, %5};\n\tmov.b64 c_, {%6, %7};\n\t"
-      "fma.rn.f32x2 r_, a_, b_, c_;\n\tmov.b64 {%0, %1}, r_;}"
-      : "=f"(r.x), "=f"(r.y)
-      : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y), "f"(c.x), "f"(c.y));
-  return r;
 }
 
 // acc[d] += x[d] - c[d] for every dimension, in IEEE single precision: the
@@ -1498,6 +1463,17 @@ static int run(int mode, const void* points, int layout, int dim, int64_t n,
 
 using namespace sg;
 
+namespace sg {
+namespace kmw {
+// more clusters than the persistent kernel holds (kmeans_wide.cu)
+int run(bool cluster, const void* points, int layout, int dim, int64_t n, int width,
+        float xy_scale, float* centroids, const float* cent_in, int K, int32_t* labels,
+        void* ws, size_t ws_bytes, int max_iter, float threshold, int32_t* d_iter,
+        cudaStream_t st);
+size_t workspace_bytes(int K, int dim);
+}  // namespace kmw
+}  // namespace sg
+
 extern "C" void split_kmeans_set_wait_test(unsigned spin_limit, int skip_block) {
   km::g_wait_limit.store(spin_limit, std::memory_order_relaxed);
   km::g_wait_skip.store(skip_block < 0 ? -1 : skip_block, std::memory_order_relaxed);
@@ -1505,9 +1481,11 @@ extern "C" void split_kmeans_set_wait_test(unsigned spin_limit, int skip_block) 
 
 extern "C" size_t split_kmeans_cluster_workspace_size_2d(int64_t npoints, int width,
                                                          int nclusters, int dim) {
-  (void)nclusters;
-  (void)dim;
   if (npoints <= 0 || width < 1) return 0;
+  if (nclusters > km::kMaxK) {
+    if (dim != 3 && dim != 5) dim = 5;
+    return kmw::workspace_bytes(nclusters, dim);
+  }
   return km::carve(nullptr, 1).bytes;
 }
 
@@ -1522,6 +1500,10 @@ extern "C" int split_kmeans_cluster(const void* points, int layout, int dim, int
                                     int max_iter, float threshold, int32_t* d_iterations,
                                     void* stream) {
   if (!centroids || !labels) return SPLIT_ERR_INVALID;
+  if (nclusters > km::kMaxK)
+    return kmw::run(true, points, layout, dim, npoints, width, xy_scale, centroids, centroids,
+                    nclusters, labels, workspace, workspace_bytes, max_iter, threshold,
+                    d_iterations, as_stream(stream));
   return km::run(km::kCluster, points, layout, dim, npoints, width, xy_scale, centroids,
                  centroids, nclusters, labels, nullptr, workspace, workspace_bytes, max_iter,
                  threshold, d_iterations, as_stream(stream));
@@ -1536,6 +1518,10 @@ extern "C" int split_kmeans_assign(const void* points, int layout, int dim, int6
                                    int nclusters, int32_t* labels, void* workspace,
                                    size_t workspace_bytes, void* stream) {
   if (!centroids || !labels) return SPLIT_ERR_INVALID;
+  if (nclusters > km::kMaxK)
+    return kmw::run(false, points, layout, dim, npoints, width, xy_scale, nullptr, centroids,
+                    nclusters, labels, workspace, workspace_bytes, 1, -1.0f, nullptr,
+                    as_stream(stream));
   return km::run(km::kAssignOnly, points, layout, dim, npoints, width, xy_scale,
                  const_cast<float*>(centroids), centroids, nclusters, labels, nullptr,
                  workspace, workspace_bytes, 1, -1.0f, nullptr, as_stream(stream));
@@ -1876,22 +1862,10 @@ inline Layout carve(void* ws, int K, int dim) {
   return l;
 }
 
-__device__ __forceinline__ unsigned long long shfl_xor_u64(unsigned long long v, int o) {
-  const unsigned a = __shfl_xor_sync(0xffffffffu, (unsigned)v, o);
-  const unsigned b = __shfl_xor_sync(0xffffffffu, (unsigned)(v >> 32), o);
-  return ((unsigned long long)b << 32) | a;
-}
-__device__ __forceinline__ unsigned long long shfl_down_u64(unsigned long long v, int o) {
-  const unsigned a = __shfl_down_sync(0xffffffffu, (unsigned)v, o);
-  const unsigned b = __shfl_down_sync(0xffffffffu, (unsigned)(v >> 32), o);
-  return ((unsigned long long)b << 32) | a;
-}
-
 template <int LAYOUT, int DIM>
 __global__ void __launch_bounds__(kThreads)
 accumulate_kernel(const int32_t* __restrict__ labels, const void* __restrict__ points,
                   int64_t n, int width, float xy_scale, int K, Layout L) {
-  const int lane = threadIdx.x & 31;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   // every lane runs the same number of rounds (warp-wide shuffles below)
   const int64_t rounds = (n + stride - 1) / stride;
@@ -1927,67 +1901,8 @@ accumulate_kernel(const int32_t* __restrict__ labels, const void* __restrict__ p
       }
     }
     unsigned long long qlo[DIM], qhi[DIM];
-#pragma unroll
-    for (int d = 0; d < DIM; ++d) {
-      if (!(fabsf(f[d]) < 274877906944.0f)) set_status(&L.hdr->status, SPLIT_ERR_OVERFLOW);
-      const long long q = l >= 0 ? __float2ll_rn(__fmul_rn(f[d], 16777216.0f)) : 0ll;
-      qlo[d] = (unsigned long long)q & 0xffffffffull;
-      qhi[d] = (unsigned long long)(q >> 32);
-    }
-    const int l0 = __shfl_sync(0xffffffffu, l, 0);
-    if (__all_sync(0xffffffffu, l == l0) && l0 >= 0) {
-      // one label across the warp: butterfly sums, one set of atomics
-#pragma unroll
-      for (int d = 0; d < DIM; ++d) {
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-          qlo[d] += shfl_xor_u64(qlo[d], o);
-          qhi[d] += shfl_xor_u64(qhi[d], o);
-        }
-      }
-      if (lane == 0) {
-#pragma unroll
-        for (int d = 0; d < DIM; ++d) {
-          atomicAdd(L.lo + (size_t)l0 * DIM + d, qlo[d]);
-          atomicAdd(L.hi + (size_t)l0 * DIM + d, qhi[d]);
-        }
-        atomicAdd(L.cnt + l0, 32u);
-      }
-    } else {
-      // Several labels: lanes hold consecutive pixels, so labels come in runs.
-      // A segmented reduction leaves each run's sums in its first lane (each
-      // lane adds from lane + o while that lane is still in its run), and only
-      // run heads issue atomics.  Integer sums: the same totals as per-pixel
-      // adds.
-      const int lprev = __shfl_up_sync(0xffffffffu, l, 1);
-      const unsigned heads = __ballot_sync(0xffffffffu, lane == 0 || l != lprev);
-      const unsigned after = heads & ~(0xffffffffu >> (31 - lane));   // heads right of this lane
-      const int run_end = after ? __ffs(after) - 1 : 32;
-      unsigned cnt = l >= 0 ? 1u : 0u;
-#pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        const bool in_run = lane + o < run_end;
-#pragma unroll
-        for (int d = 0; d < DIM; ++d) {
-          const unsigned long long a = shfl_down_u64(qlo[d], o);
-          const unsigned long long b = shfl_down_u64(qhi[d], o);
-          if (in_run) {
-            qlo[d] += a;
-            qhi[d] += b;
-          }
-        }
-        const unsigned c = __shfl_down_sync(0xffffffffu, cnt, o);
-        if (in_run) cnt += c;
-      }
-      if (l >= 0 && ((heads >> lane) & 1u)) {
-#pragma unroll
-        for (int d = 0; d < DIM; ++d) {
-          atomicAdd(L.lo + (size_t)l * DIM + d, qlo[d]);
-          atomicAdd(L.hi + (size_t)l * DIM + d, qhi[d]);
-        }
-        atomicAdd(L.cnt + l, cnt);
-      }
-    }
+    fix::quantize<DIM>(f, l, &L.hdr->status, qlo, qhi);
+    fix::warp_add<DIM>(l, qlo, qhi, L.lo, L.hi, L.cnt);
   }
 }
 
@@ -1998,10 +1913,7 @@ finish_kernel(Layout L, int K, int dim, float* __restrict__ centroids) {
     const int k = (int)(idx / dim), d = (int)(idx - (int64_t)k * dim);
     const unsigned nk = L.cnt[k];
     if (nk == 0) continue;
-    const double h = (double)(long long)L.hi[idx];
-    const double l = (double)L.lo[idx];
-    const double S = __dmul_rn(__dadd_rn(__dmul_rn(h, 4294967296.0), l), 1.0 / 16777216.0);
-    centroids[(int64_t)d * K + k] = __double2float_rn(__ddiv_rn(S, (double)nk));
+    centroids[(int64_t)d * K + k] = fix::mean(L.lo[idx], L.hi[idx], nk);
   }
 }
 
