@@ -527,6 +527,34 @@ def run_next_rows(dev, pipe, rgb, reps=7):
                                    "mpix_sweeps_s": round(hh * ww * sweeps / (t_e * 1e-3) / 1e6, 1),
                                    "gb_s": round(hh * ww * sweeps * (3 * 16 + 12) / (t_e * 1e-3) / 1e9, 1)}
     out["estimate_normals_1080p"] = sor
+    # 5: label_points and cluster with more clusters than the persistent
+    # kernel holds (K = 256, 5-D features of the RGB8 frame, centroids picked
+    # from the frame); a clustering iteration reads the RGB8 pixel and writes
+    # its label, as the assignment does
+    from split_gb300 import synth
+    rgb_h = rgb.cpu().numpy()
+    many = {}
+    for k in (256, 1024):
+        ck0 = torch.from_numpy(synth.pick_centroids(5, rgb_h, k, 5)).to(dev)
+        ck = ck0.clone()
+        labk = torch.empty(n, dtype=torch.int32, device=dev)
+        kws = kmeans.label_points(ck, rgb, labk, layout=N.LAYOUT_RGB8, dim=5, width=W)
+        t_a = timed(lambda: kmeans.label_points(ck, rgb, labk, kws, layout=N.LAYOUT_RGB8,
+                                                dim=5, width=W))
+        e = entry(t_a, 7)
+        e["distance_pairs_g_s"] = round(n * k / (t_a * 1e-3) / 1e9, 1)   # brute-force equivalent
+        many[f"label_points_k{k}"] = e
+        if k == 256:
+            kmeans.cluster(rgb, ck, labk, kws, max_iter=20, threshold=-1.0,
+                           layout=N.LAYOUT_RGB8, dim=5, width=W)
+            t_k = timed(lambda: kmeans.cluster(rgb, ck, labk, kws, max_iter=20, threshold=-1.0,
+                                               layout=N.LAYOUT_RGB8, dim=5, width=W),
+                        prep=lambda: ck.copy_(ck0))
+            e = entry(t_k / 20, 7)
+            e["ms_20_iterations"] = round(t_k, 3)
+            many[f"cluster_k{k}_per_iteration"] = e
+        kws.check("many clusters")
+    out["kmeans_many_clusters"] = many
     for ws in (cws, sws, lws, ews):
         ws.check("next rows")
     return out

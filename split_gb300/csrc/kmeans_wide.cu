@@ -11,7 +11,9 @@
 // operation, and ties go to the lowest cluster index (strict < in ascending
 // k, as the reference's argmin over the distance row, label.cu:98-105).  In
 // a clustering the same pass adds every pixel's features to its cluster's
-// fixed-point sums (fixsum.cuh), so the update reads no pixel again.
+// fixed-point sums (fixsum.cuh), so the update reads no pixel again: for
+// features below 2^32 as one 64-bit word per dimension, summed first over a
+// lane's four pixels where the warp's 128 pixels share one label.
 //
 // Clustering: per iteration one assignment launch and one forming launch
 // (form_kernel, one block), all max_iter pairs queued at once, each launch a
@@ -173,7 +175,7 @@ __device__ __forceinline__ void closer(const float (&fp)[DIM], const float (&fq)
 // centroids at a time; the survivors of a ballot are then measured against
 // the warp's pixels in ascending k, as pairs on the packed FP32x2 pipe.
 template <int LAYOUT, int DIM, bool ACC>
-__global__ void __launch_bounds__(kThreads) assign_kernel(AssignArgs a) {
+__global__ void __launch_bounds__(kThreads, 3) assign_kernel(AssignArgs a) {
   constexpr int CS = DIM == 5 ? 2 : 1;          // float4 slots per centroid
   constexpr int kChunk = kChunkF4 / CS;         // centroids per chunk
   constexpr unsigned full = 0xffffffffu;
@@ -284,13 +286,50 @@ __global__ void __launch_bounds__(kThreads) assign_kernel(AssignArgs a) {
       }
     }
 #pragma unroll
-    for (int j = 0; j < kPix; ++j) {
+    for (int j = 0; j < kPix; ++j)
       if (ok[j]) a.labels[base + 32 * j] = bk[j];
-      if (ACC) {
-        unsigned long long qlo[DIM], qhi[DIM];
-        const int l = ok[j] ? bk[j] : -1;
-        fix::quantize<DIM>(f[j], l, a.status, qlo, qhi);
-        fix::warp_add<DIM>(l, qlo, qhi, a.lo, a.hi, a.cnt);
+    if (ACC) {
+      // Features below 2^32 (the common case by far): the narrow fixed-point
+      // form, and where all 128 pixels share one label each lane first adds
+      // its four pixels' words.  Otherwise the general form, pixel by pixel.
+      bool small = true;
+#pragma unroll
+      for (int j = 0; j < kPix; ++j)
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) small = small && (!ok[j] || fabsf(f[j][d]) < 4294967296.0f);
+      const int b0 = __shfl_sync(full, bk[0], 0);   // every lane, before any branch
+      bool one = ok[kPix - 1];                        // (ok[3] implies ok[0..2])
+#pragma unroll
+      for (int j = 1; j < kPix; ++j) one = one && bk[j] == bk[0];
+      if (__all_sync(full, small)) {
+        if (__all_sync(full, one && bk[0] == b0)) {
+          long long q[DIM];
+#pragma unroll
+          for (int d = 0; d < DIM; ++d) {
+            q[d] = 0;
+#pragma unroll
+            for (int j = 0; j < kPix; ++j) q[d] += __float2ll_rn(__fmul_rn(f[j][d], fix::kScale));
+          }
+          fix::warp_add_narrow<DIM>(b0, q, kPix, a.lo, a.hi, a.cnt);
+        } else {
+#pragma unroll
+          for (int j = 0; j < kPix; ++j) {
+            const int l = ok[j] ? bk[j] : -1;
+            long long q[DIM];
+#pragma unroll
+            for (int d = 0; d < DIM; ++d)
+              q[d] = l >= 0 ? __float2ll_rn(__fmul_rn(f[j][d], fix::kScale)) : 0ll;
+            fix::warp_add_narrow<DIM>(l, q, 1u, a.lo, a.hi, a.cnt);
+          }
+        }
+      } else {
+#pragma unroll
+        for (int j = 0; j < kPix; ++j) {
+          unsigned long long qlo[DIM], qhi[DIM];
+          const int l = ok[j] ? bk[j] : -1;
+          fix::quantize<DIM>(f[j], l, a.status, qlo, qhi);
+          fix::warp_add<DIM>(l, qlo, qhi, a.lo, a.hi, a.cnt);
+        }
       }
     }
   }

@@ -172,3 +172,27 @@ def test_label_points_infinite_features(cuda, k, layout):
     got = labels.cpu().numpy()
     assert np.array_equal(got, exact)
     assert (got[bad] == 0).all() and got.max() < k
+
+
+def test_cluster_many_clusters_large_features(cuda):
+    """Features from 2^32 up (below the fixed-point format's 2^38) take the
+    general 96-bit sums instead of the one-word form: one iteration still
+    equals the FP32-exact assignment and the FP64 mean."""
+    import torch
+    from split_gb300 import kmeans
+    w, h, k = 90, 70, 72
+    rgb = synth.voronoi_rgb8(17, w, h, 40, sigma=5.0)
+    feats = synth.features(rgb, 3) * np.float32(2.0 ** 34)
+    feats[:, ::7] *= np.float32(1.0 / 1024.0)       # some warps mix small and large values
+    c0 = np.ascontiguousarray(feats[:, np.random.default_rng(17).choice(w * h, k, replace=False)])
+    cent = _t(c0, cuda)
+    labels = torch.empty(w * h, dtype=torch.int32, device=cuda)
+    ws = kmeans.cluster(_t(feats, cuda), cent, labels, None, max_iter=1, threshold=-1.0,
+                        layout=kmeans.PLANAR, dim=3, width=w)
+    torch.cuda.synchronize()
+    ws.check("kmeans")
+    gl = labels.cpu().numpy()
+    assert np.array_equal(gl, oracle.kmeans_assign_f32(feats, c0))
+    ref, _ = oracle.kmeans_update_f64(gl, feats, c0)
+    rel = np.abs(cent.cpu().numpy() - ref) / np.maximum(np.abs(ref), 1e-30)
+    assert rel.max() <= 1e-6
