@@ -378,7 +378,7 @@ int split_pack_lab_beta(const uint8_t* rgb, int64_t npixels, float mu, int layou
  * features -> kmeans::cluster -> ccl::connected_components -> small-segment
  * merge -> morph::erode) plus Sobel normals of the luminance plane. */
 typedef struct split_pipeline_params {
-  int nclusters;          /* K <= 64                                         */
+  int nclusters;          /* 1 to 2^20 (above 64: the many-cluster k-means) */
   int dim;                /* 3 (RGB) or 5 (RGB + xy_scale * (column, row))   */
   float xy_scale;
   int kmeans_iters;

@@ -54,7 +54,8 @@ static Layout carve(void* ws, int W, int H, const split_pipeline_params& p) {
 }
 
 static bool valid(const split_pipeline_params* p) {
-  return p && p->nclusters >= 1 && p->nclusters <= 64 && (p->dim == 3 || p->dim == 5) &&
+  // K above 64 runs the many-cluster k-means (split_kmeans_cluster picks it)
+  return p && p->nclusters >= 1 && p->nclusters <= (1 << 20) && (p->dim == 3 || p->dim == 5) &&
          p->kmeans_iters >= 0 &&
          (p->features == SPLIT_LAYOUT_FLOAT4 || p->features == SPLIT_LAYOUT_RGB8 ||
           p->features == kFeaturesLabBeta) &&

@@ -196,3 +196,30 @@ def test_cluster_many_clusters_large_features(cuda):
     ref, _ = oracle.kmeans_update_f64(gl, feats, c0)
     rel = np.abs(cent.cpu().numpy() - ref) / np.maximum(np.abs(ref), 1e-30)
     assert rel.max() <= 1e-6
+
+
+def test_pipeline_many_clusters(cuda):
+    """The single-image pipeline with K = 100: its clustering equals a
+    standalone cluster() call bit for bit, and labelling, merge and erosion
+    equal the oracle's on its cluster labels."""
+    import torch
+    from split_gb300 import color, kmeans, pipeline
+    w, h, k = 320, 200, 100
+    rgb = synth.voronoi_rgb8(31, w, h, 120, npalette=24, sigma=3.0)
+    c0 = synth.pick_centroids(31, rgb, k, 5)
+    params = pipeline.Params(nclusters=k, kmeans_iters=6, merge_P=32)
+    pipe = pipeline.Pipeline(w, h, params, cuda)
+    d_rgb = _t(rgb, cuda)
+    pipe.run(d_rgb, _t(c0, cuda))
+    torch.cuda.synchronize()
+    pipe.ws.check("pipeline")
+    f4 = torch.empty((w * h, 4), dtype=torch.float32, device=cuda)
+    color.pack_rgb8(d_rgb, f4)
+    cent = _t(c0, cuda)
+    lab = torch.empty(w * h, dtype=torch.int32, device=cuda)
+    kmeans.cluster(f4, cent, lab, None, max_iter=6, threshold=-1.0,
+                   layout=kmeans.FLOAT4 | kmeans.UNIT_RANGE, dim=5, width=w)
+    assert torch.equal(lab, pipe.cluster_labels) and torch.equal(cent, pipe.centroids)
+    seg = oracle.ccl(lab.cpu().numpy().reshape(h, w), 8, 0)
+    want = oracle.erode(oracle.merge_small(seg, 32, 0), 1)
+    assert np.array_equal(pipe.segment_labels.cpu().numpy(), want)
