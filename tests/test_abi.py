@@ -55,8 +55,14 @@ def test_workspace_queries():
     assert lib.split_compress_labels_workspace_size(3840 * 2160) < 4 * 3840 * 2160 // 8
     p = _native.PipelineParams(16, 5, 0.1, 20, -1.0, 1, 8, 0, 256, 0, 1, 1, 1.0)
     assert lib.split_pipeline_workspace_size(3840, 2160, C.byref(p)) > 0
-    bad = _native.PipelineParams(65, 5, 0.1, 20, -1.0, 1, 8, 0, 256, 0, 1, 1, 1.0)
-    assert lib.split_pipeline_workspace_size(3840, 2160, C.byref(bad)) == 0
+    # more than 64 clusters: the many-cluster k-means, with its own workspace
+    many = _native.PipelineParams(1000, 5, 0.1, 20, -1.0, 1, 8, 0, 256, 0, 1, 1, 1.0)
+    assert lib.split_pipeline_workspace_size(3840, 2160, C.byref(many)) > 0
+    assert lib.split_kmeans_cluster_workspace_size_2d(3840 * 2160, 3840, 1000, 5) >= \
+        2 * 5 * 1000 * 4 + 2 * 5 * 1000 * 8
+    for k, d in ((0, 5), ((1 << 20) + 1, 5), (16, 4)):
+        bad = _native.PipelineParams(k, d, 0.1, 20, -1.0, 1, 8, 0, 256, 0, 1, 1, 1.0)
+        assert lib.split_pipeline_workspace_size(3840, 2160, C.byref(bad)) == 0
 
 
 def test_invalid_arguments_rejected_on_host():
