@@ -51,6 +51,7 @@ constexpr int kWarps = kThreads / 32;
 constexpr int kTile = 64;
 constexpr int kMaxK = 64;
 constexpr int kMaxDim = 5;
+constexpr int kSpanSums = 8;   // words of a span's entry in Image::span_sum (kMaxDim used)
 // Unit partials are added into the image accumulators as multiples of
 // 2^-24; a partial must stay below 2^38 in magnitude (a unit holds at most
 // 8192 pixels, so |x - c| below 3e7 everywhere).  Beyond it the call reports
@@ -79,6 +80,11 @@ struct Image {
   int ntx;                  // tiles per row of tiles
   int unit_rows;            // rows of a unit (kTile or 2 * kTile, from the tuning table)
   int ref_shift;            // SPLIT_KMEANS_REFERENCE_SHIFT (D = 3, K >= 3)
+  // Exact feature sums of the fast spans (kSpanSums words each), written in
+  // the first iteration of a call (null: none kept).  A fast span's slot is
+  // (first row / span rows) * span_cols + tile column.
+  long long* span_sum;
+  int span_cols;            // width / kTile: tile columns of full width
 };
 
 struct ImageState {
@@ -256,6 +262,9 @@ struct Smem {
   alignas(16) float cent[kMaxK * 8];
   float acc[kWarps][kMaxK * kMaxDim];
   int cnt[kWarps][kMaxK];
+  // the unit's single-candidate spans, in fixed point (added as integers)
+  long long fix[kMaxK * kMaxDim];
+  int fixn[kMaxK];
   float lut[256];
   int next[2];
   int more;
@@ -511,6 +520,58 @@ __device__ __forceinline__ void nearest_pair(const float (&f)[kPx][DIM],
   }
 }
 
+// Adds a single-candidate span's pixels to cluster k's sums of the unit, as
+// the exact fixed-point sum of (x - c_k): S (the span's exact feature words,
+// lane d holding dimension d) minus n * c_k * 2^24 (exact in FP64, rounded
+// once).  The same integers whether S was just summed from the pixels or
+// kept from the first iteration, so a call's result does not depend on
+// which; integer adds, so not on their order either.
+template <int DIM>
+__device__ __forceinline__ void add_span_sums(Smem& sm, int k, long long s_lane, int n) {
+  constexpr int CS = cstride(DIM);
+  const int lane = threadIdx.x & 31;
+  if (lane < DIM) {
+    const double nc = __dmul_rn((double)n, __dmul_rn((double)sm.cent[k * CS + lane], 16777216.0));
+    atomicAdd(reinterpret_cast<unsigned long long*>(&sm.fix[k * kMaxDim + lane]),
+              (unsigned long long)(s_lane - __double2ll_rn(nc)));
+  } else if (lane == DIM) {
+    atomicAdd(&sm.fixn[k], n);
+  }
+}
+
+// Exact feature words of a span (2^-24 units): colour from the lanes' pixel
+// sums `qc`, the xy features from the geometry (each lane's kPx columns in
+// every batch row it covers); summed over the warp, lane d returns
+// dimension d.
+template <int DIM>
+__device__ __forceinline__ long long span_words(const long long (&qc)[3], const float (&fx)[kPx],
+                                                float xy_scale, int row_first, int nbatches) {
+  const int lane = threadIdx.x & 31;
+  long long w[DIM];
+  w[0] = qc[0];
+  w[1] = qc[1];
+  w[2] = qc[2];
+  if (DIM == 5) {
+    long long qx = 0, qy = 0;
+#pragma unroll
+    for (int j = 0; j < kPx; ++j) qx += __float2ll_rn(__fmul_rn(fx[j], kFixScale));
+    for (int b = 0; b < nbatches; ++b)
+      qy += __float2ll_rn(
+          __fmul_rn(__fmul_rn(xy_scale, (float)(row_first + b * kBatchRows)), kFixScale));
+    w[DIM == 5 ? 3 : 0] = qx * nbatches;
+    w[DIM == 5 ? 4 : 0] = qy * kPx;
+  }
+  long long mine = 0;
+#pragma unroll
+  for (int d = 0; d < DIM; ++d) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+      w[d] += (long long)__shfl_xor_sync(0xffffffffu, (unsigned long long)w[d], o);
+    if (lane == d) mine = w[d];
+  }
+  return mine;
+}
+
 // How a span's candidate mask is used: one cluster (every pixel's label
 // outright), two clusters with finite centroids (two running sums per lane),
 // or any other mask (per-batch reduction by label).
@@ -520,12 +581,18 @@ enum SpanKind { kSpanSingle = 0, kSpanPair = 1, kSpanAny = 2 };
 // label is ka or kb (finite features and centroids), so `acc` runs for ka
 // and a second per-lane sum for kb, reduced once at the end of the span
 // however often the two labels mix within its batches.
+//
+// A single-candidate span of a clustering adds its pixels' exact feature
+// words instead of running FP32 sums, and keeps them in `entry` (if any).
 template <int LAYOUT, int DIM, int MODE, int KIND>
 __device__ __forceinline__ void span_batches(const Image& im, Smem& sm, int warp, int row_first,
                                              int col, int nbatches, unsigned long long mask,
                                              int ka, int kb, bool write_labels, bool vec_labels,
-                                             int& acc_l, int& acc_n, float (&acc)[DIM]) {
+                                             int& acc_l, int& acc_n, float (&acc)[DIM],
+                                             long long* entry) {
   constexpr int CS = cstride(DIM);
+  constexpr bool kFixSingle = KIND == kSpanSingle && MODE == kCluster;
+  long long qc[3] = {0, 0, 0};
   const int64_t step = (int64_t)kBatchRows * im.width;
   int64_t px0 = (int64_t)row_first * im.width + col;
   float acc2[DIM];
@@ -607,6 +674,12 @@ __device__ __forceinline__ void span_batches(const Image& im, Smem& sm, int warp
         f[j][4] = fy;
       }
     }
+    if (kFixSingle) {
+#pragma unroll
+      for (int j = 0; j < kPx; ++j)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) qc[c] += __float2int_rn(__fmul_rn(f[j][c], kFixScale));
+    }
     int lab[kPx];
     if (KIND == kSpanSingle) {
       // one candidate for the whole span: every pixel's argmin, no distances
@@ -627,11 +700,13 @@ __device__ __forceinline__ void span_batches(const Image& im, Smem& sm, int warp
     }
     if (MODE != kAssignOnly) {
       if (KIND == kSpanSingle) {
-        // the same sums, in the same order, as accumulate_valid's uniform case
-        const float* c = sm.cent + ka * CS;
+        // a clustering's single spans are summed exactly (after the loop)
+        if (!kFixSingle) {
+          const float* c = sm.cent + ka * CS;
 #pragma unroll
-        for (int j = 0; j < kPx; ++j) add_centered<DIM>(f[j], c, acc);
-        acc_n += kPx;
+          for (int j = 0; j < kPx; ++j) add_centered<DIM>(f[j], c, acc);
+          acc_n += kPx;
+        }
       } else if (KIND == kSpanPair) {
         const float* ca = sm.cent + ka * CS;
         const float* cb = sm.cent + kb * CS;
@@ -652,6 +727,49 @@ __device__ __forceinline__ void span_batches(const Image& im, Smem& sm, int warp
   }
   // the second candidate's sums (the first's stay running)
   if (MODE != kAssignOnly && KIND == kSpanPair) flush_acc<DIM>(sm, warp, kb, acc2, acc2_n);
+  if (kFixSingle) {
+    const long long w = span_words<DIM>(qc, fx, im.xy_scale, row_first, nbatches);
+    if (entry && (threadIdx.x & 31) < DIM) __stcg(entry + (threadIdx.x & 31), w);
+    add_span_sums<DIM>(sm, ka, w, 32 * kPx * nbatches);
+  }
+}
+
+// The exact feature words of a fast span into `entry`, read from the pixels
+// (in the first iteration, for spans with more than one candidate: they may
+// have a single one later).
+template <int LAYOUT, int DIM>
+__device__ __forceinline__ void keep_span_words(const Image& im, const float* lut, int row_first,
+                                             int col, int nbatches, long long* entry) {
+  long long qc[3] = {0, 0, 0};
+  float fx[kPx];
+#pragma unroll
+  for (int j = 0; j < kPx; ++j) fx[j] = __fmul_rn(im.xy_scale, (float)(col + j));
+  const int64_t step = (int64_t)kBatchRows * im.width;
+  int64_t px0 = (int64_t)row_first * im.width + col;
+  for (int b = 0; b < nbatches; ++b, px0 += step) {
+    float f[kPx][3];
+    if (LAYOUT == SPLIT_LAYOUT_FLOAT4) {
+#pragma unroll
+      for (int j = 0; j < kPx; ++j) {
+        const float4 v = __ldg(static_cast<const float4*>(im.points) + px0 + j);
+        f[j][0] = v.x;
+        f[j][1] = v.y;
+        f[j][2] = v.z;
+      }
+    } else {
+      const uint8_t* p = static_cast<const uint8_t*>(im.points) + 3 * px0;
+#pragma unroll
+      for (int j = 0; j < kPx; ++j)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) f[j][c] = lut[__ldg(p + 3 * j + c)];
+    }
+#pragma unroll
+    for (int j = 0; j < kPx; ++j)
+#pragma unroll
+      for (int c = 0; c < 3; ++c) qc[c] += __float2int_rn(__fmul_rn(f[j][c], kFixScale));
+  }
+  const long long w = span_words<DIM>(qc, fx, im.xy_scale, row_first, nbatches);
+  if ((threadIdx.x & 31) < DIM) __stcg(entry + (threadIdx.x & 31), w);
 }
 
 // A warp span that lies wholly inside the image, with packed features (float4,
@@ -659,11 +777,18 @@ __device__ __forceinline__ void span_batches(const Image& im, Smem& sm, int warp
 // for the whole span: no per-pixel bounds checks, one pointer step per batch,
 // the column feature hoisted.  Results equal the general path's labels; the
 // sums are the same pixels' in a fixed, data-dependent order.
+//
+// In a clustering, `entry` is the span's slot of kept feature words (or
+// null).  Iteration 0 writes it for every span; in later iterations a span
+// with one candidate reads it back instead of its pixels: its labels are
+// that candidate's (written when asked) and its sums are exact integers, so
+// nothing else needs the pixels.
 template <int LAYOUT, int DIM, int MODE>
 __device__ __forceinline__ void fast_span(const Image& im, Smem& sm, int warp, int row_first,
                                           int col, int nbatches, unsigned long long mask,
                                           bool write_labels, bool vec_labels, int& acc_l,
-                                          int& acc_n, float (&acc)[DIM]) {
+                                          int& acc_n, float (&acc)[DIM], long long* entry,
+                                          int it) {
   constexpr int CS = cstride(DIM);
   // A mask with one cluster names every pixel's nearest centroid outright:
   // the span's box excludes all others for every pixel it holds (and the
@@ -684,8 +809,26 @@ __device__ __forceinline__ void fast_span(const Image& im, Smem& sm, int warp, i
       kb = b;
     }
   }
+  if (MODE == kCluster && kind == kSpanSingle && entry && it > 0) {
+    const int lane = threadIdx.x & 31;
+    add_span_sums<DIM>(sm, ka, lane < DIM ? __ldcg(entry + lane) : 0ll, 32 * kPx * nbatches);
+    if (write_labels) {
+      const int64_t step = (int64_t)kBatchRows * im.width;
+      int64_t px0 = (int64_t)row_first * im.width + col;
+      for (int b = 0; b < nbatches; ++b, px0 += step) {
+        if (vec_labels) {
+          *reinterpret_cast<int4*>(im.labels + px0) = make_int4(ka, ka, ka, ka);
+        } else {
+#pragma unroll
+          for (int j = 0; j < kPx; ++j) im.labels[px0 + j] = ka;
+        }
+      }
+    }
+    return;
+  }
   // with one running label for the whole span the sums switch to it once
-  if (MODE != kAssignOnly && ka >= 0 && ka != acc_l) {
+  // (a clustering sums its single spans exactly instead)
+  if (MODE != kAssignOnly && ka >= 0 && ka != acc_l && !(MODE == kCluster && kind == kSpanSingle)) {
     if (acc_l >= 0) flush_acc<DIM>(sm, warp, acc_l, acc, acc_n);
     acc_l = ka;
     acc_n = 0;
@@ -694,13 +837,18 @@ __device__ __forceinline__ void fast_span(const Image& im, Smem& sm, int warp, i
   }
   if (kind == kSpanSingle)
     span_batches<LAYOUT, DIM, MODE, kSpanSingle>(im, sm, warp, row_first, col, nbatches, mask, ka,
-                                                 kb, write_labels, vec_labels, acc_l, acc_n, acc);
+                                                 kb, write_labels, vec_labels, acc_l, acc_n, acc,
+                                                 entry);
   else if (kind == kSpanPair)
     span_batches<LAYOUT, DIM, MODE, kSpanPair>(im, sm, warp, row_first, col, nbatches, mask, ka,
-                                               kb, write_labels, vec_labels, acc_l, acc_n, acc);
+                                               kb, write_labels, vec_labels, acc_l, acc_n, acc,
+                                               entry);
   else
     span_batches<LAYOUT, DIM, MODE, kSpanAny>(im, sm, warp, row_first, col, nbatches, mask, ka,
-                                              kb, write_labels, vec_labels, acc_l, acc_n, acc);
+                                              kb, write_labels, vec_labels, acc_l, acc_n, acc,
+                                              entry);
+  if (MODE == kCluster && kind != kSpanSingle && entry && it == 0)
+    keep_span_words<LAYOUT, DIM>(im, sm.lut, row_first, col, nbatches, entry);
 }
 
 // Process one unit (a 64 x 64 tile): assign (unless update-only) and
@@ -717,7 +865,7 @@ __device__ __forceinline__ void fast_span(const Image& im, Smem& sm, int warp, i
 // running sum; a batch with several labels is reduced label by label in
 // ascending order.  All orders depend only on the data.
 template <int LAYOUT, int DIM, int MODE>
-__device__ void process_unit(const Image& im, int unit, Smem& sm, bool write_labels) {
+__device__ void process_unit(const Image& im, int unit, Smem& sm, bool write_labels, int it) {
   const unsigned full = 0xffffffffu;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   constexpr int CS = cstride(DIM);
@@ -762,9 +910,15 @@ __device__ void process_unit(const Image& im, int unit, Smem& sm, bool write_lab
                     (LAYOUT == SPLIT_LAYOUT_FLOAT4 ||
                      (LAYOUT == SPLIT_LAYOUT_RGB8 && vec_labels &&
                       (reinterpret_cast<uintptr_t>(im.points) & 3) == 0));
-  if (fast)
+  if (fast) {
+    // a fast span lies wholly inside the image: slot (row0 / wrows, tx)
+    long long* entry = (MODE == kCluster && im.span_sum)
+                           ? im.span_sum + ((size_t)(row0 / wrows) * im.span_cols + tx) * kSpanSums
+                           : nullptr;
     fast_span<LAYOUT, DIM, MODE>(im, sm, warp, row0 + lrow, col0 + lcol, wrows / kBatchRows,
-                                 span_mask, write_labels, vec_labels, acc_l, acc_n, acc);
+                                 span_mask, write_labels, vec_labels, acc_l, acc_n, acc, entry,
+                                 it);
+  }
   for (int b = 0; !fast && b < wrows / kBatchRows; ++b) {
     if (b * kBatchRows >= rows_in) break;
     const int row = row0 + b * kBatchRows + lrow;
@@ -910,15 +1064,21 @@ __device__ void block_to_accum(Smem& sm, const Params& p, int img, int K, int di
       s = __fadd_rn(s, sm.acc[w][idx]);
       sm.acc[w][idx] = 0.0f;
     }
+    // plus the single spans' exact words
+    long long q = sm.fix[idx];
+    sm.fix[idx] = 0;
     if ((idx % kMaxDim) < dim && s != 0.0f) {
       if (!(fabsf(s) < kFixLimit)) set_status(&p.hdr->status, SPLIT_ERR_OVERFLOW);
-      const long long q = __float2ll_rn(__fmul_rn(s, kFixScale));
+      q += __float2ll_rn(__fmul_rn(s, kFixScale));
+    }
+    if ((idx % kMaxDim) < dim && q != 0) {
       atomicAdd(lo + idx, (unsigned long long)q & 0xffffffffull);
       atomicAdd(hi + idx, (unsigned long long)(q >> 32));
     }
   }
   for (int k = threadIdx.x; k < K; k += blockDim.x) {
-    int c = 0;
+    int c = sm.fixn[k];
+    sm.fixn[k] = 0;
 #pragma unroll
     for (int w = 0; w < kWarps; ++w) {
       c += sm.cnt[w][k];
@@ -1094,6 +1254,8 @@ __global__ void __launch_bounds__(kThreads, SG_KM_MINBLOCKS) kmeans_kernel(Param
   for (int i = threadIdx.x; i < kWarps * kMaxK * kMaxDim; i += blockDim.x)
     (&sm.acc[0][0])[i] = 0.0f;
   for (int i = threadIdx.x; i < kWarps * kMaxK; i += blockDim.x) (&sm.cnt[0][0])[i] = 0;
+  for (int i = threadIdx.x; i < kMaxK * kMaxDim; i += blockDim.x) sm.fix[i] = 0;
+  for (int i = threadIdx.x; i < kMaxK; i += blockDim.x) sm.fixn[i] = 0;
   if (LAYOUT == SPLIT_LAYOUT_RGB8)
     for (int i = threadIdx.x; i < 256; i += blockDim.x) sm.lut[i] = (float)i / 255.0f;
   __syncthreads();
@@ -1151,7 +1313,7 @@ __global__ void __launch_bounds__(kThreads, SG_KM_MINBLOCKS) kmeans_kernel(Param
         const int lu = u - im.unit_begin;
         const bool wl = (MODE == kAssignOnly) ||
                         (MODE == kCluster && (im.threshold >= 0.0f || it == im.max_iter - 1));
-        process_unit<LAYOUT, DIM, MODE>(im, lu, sm, wl);
+        process_unit<LAYOUT, DIM, MODE>(im, lu, sm, wl, it);
         if (MODE != kAssignOnly) block_to_accum(sm, p, img, im.K, DIM, it % 3);
       }
       // the last warp fetches the next unit (slot k & 1 was last read before
@@ -1193,6 +1355,7 @@ struct Layout {
   float* cur;
   ImageState* state;
   Image* images;
+  long long* span_sum;   // single image: kept span feature words (after the rest)
   WsHeader* hdr;
   size_t bytes;
 };
@@ -1202,9 +1365,19 @@ inline int tiles_x(int width) { return (width + kTile - 1) / kTile; }
 inline int units_of(int64_t n, int width, int rows = kTile) {
   return tiles_x(width) * ((height_of(n, width) + rows - 1) / rows);
 }
-// The workspace holds per-image state only (accumulators, centroids, counters):
-// its size does not depend on the image sizes.
-static Layout carve(void* ws, int nimages) {
+// Fast spans of an image: full kTile-wide tile columns times full span-row
+// slices at the smallest span height (2 rows, 16-row units), which bounds
+// every unit height the tuning table may choose.
+inline int64_t span_slots(int64_t n, int width) {
+  return (int64_t)(width / kTile) * (height_of(n, width) / 2);
+}
+
+// The workspace holds per-image state (accumulators, centroids, counters),
+// whose size does not depend on the image sizes, and optionally a single
+// image's kept span sums (kSpanSums words per fast span, after the rest: a
+// workspace without them runs the same clustering, reading every pixel in
+// every iteration).
+static Layout carve(void* ws, int nimages, int64_t span_entries = 0) {
   Carver c(ws);
   Layout l;
   l.hdr = c.take<WsHeader>(1);
@@ -1214,6 +1387,7 @@ static Layout carve(void* ws, int nimages) {
   l.cur = c.take<float>((size_t)2 * nimages * kMaxK * 8);
   l.state = c.take<ImageState>((size_t)2 * nimages);
   l.images = nimages > 1 ? c.take<Image>((size_t)nimages) : nullptr;
+  l.span_sum = span_entries > 0 ? c.take<long long>((size_t)span_entries * kSpanSums) : nullptr;
   l.bytes = c.size();
   return l;
 }
@@ -1410,7 +1584,12 @@ static int run(int mode, const void* points, int layout, int dim, int64_t n,
   Layout l = carve(nullptr, 1);
   if (!ws || ws_bytes < l.bytes || (reinterpret_cast<uintptr_t>(ws) & 255))
     return SPLIT_ERR_WORKSPACE;
-  l = carve(ws, 1);
+  // span sums for a clustering of more than one iteration, where the
+  // workspace holds them
+  const int64_t slots = span_slots(n, width);
+  const bool keep = mode == kCluster && max_iter > 1 && slots > 0 &&
+                    ws_bytes >= carve(nullptr, 1, slots).bytes;
+  l = carve(ws, 1, keep ? slots : 0);
   Params p{};
   Image& im = p.img0;
   im.points = points;
@@ -1431,6 +1610,8 @@ static int run(int mode, const void* points, int layout, int dim, int64_t n,
   im.ntx = tiles_x(width);
   im.unit_rows = te.kmeans_unit_rows;
   im.ref_shift = ref_shift;
+  im.span_sum = l.span_sum;
+  im.span_cols = width / kTile;
   p.blocks_per_sm = te.kmeans_blocks_per_sm;
   wait_test(&p.wait_limit, &p.wait_skip);
   p.nimages = 1;
@@ -1486,12 +1667,16 @@ extern "C" size_t split_kmeans_cluster_workspace_size_2d(int64_t npoints, int wi
     if (dim != 3 && dim != 5) dim = 5;
     return kmw::workspace_bytes(nclusters, dim);
   }
-  return km::carve(nullptr, 1).bytes;
+  // with the kept span sums of a clustering
+  return km::carve(nullptr, 1, km::span_slots(npoints, width)).bytes;
 }
 
 extern "C" size_t split_kmeans_cluster_workspace_size(int64_t npoints, int nclusters, int dim) {
-  // without the image width: the largest tile count, reached at width 1
-  return split_kmeans_cluster_workspace_size_2d(npoints, 1, nclusters, dim);
+  // without the image width: room for the span sums at any width
+  // ((width / 64) * (height / 2) <= npoints / 64 + 1)
+  if (npoints <= 0) return 0;
+  if (nclusters > km::kMaxK) return split_kmeans_cluster_workspace_size_2d(npoints, 1, nclusters, dim);
+  return km::carve(nullptr, 1, npoints / 64 + 1).bytes;
 }
 
 extern "C" int split_kmeans_cluster(const void* points, int layout, int dim, int64_t npoints,
@@ -1510,7 +1695,10 @@ extern "C" int split_kmeans_cluster(const void* points, int layout, int dim, int
 }
 
 extern "C" size_t split_kmeans_assign_workspace_size(int64_t npoints, int nclusters) {
-  return split_kmeans_cluster_workspace_size(npoints, nclusters, 5);
+  // one assignment keeps no span sums
+  if (npoints <= 0) return 0;
+  if (nclusters > km::kMaxK) return split_kmeans_cluster_workspace_size(npoints, nclusters, 5);
+  return km::carve(nullptr, 1).bytes;
 }
 
 extern "C" int split_kmeans_assign(const void* points, int layout, int dim, int64_t npoints,
@@ -1542,7 +1730,8 @@ extern "C" size_t split_kmeans_update_workspace_size(int64_t npoints, int nclust
     if (npoints <= 0 || dim < 1) return 0;
     return segm::workspace_bytes(nclusters, dim);
   }
-  return split_kmeans_cluster_workspace_size(npoints, nclusters, dim);
+  if (npoints <= 0) return 0;
+  return km::carve(nullptr, 1).bytes;
 }
 
 extern "C" int split_kmeans_update(const int32_t* labels, const void* points, int layout,
