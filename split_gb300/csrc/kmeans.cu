@@ -52,6 +52,7 @@ constexpr int kTile = 64;
 constexpr int kMaxK = 64;
 constexpr int kMaxDim = 5;
 constexpr int kSpanSums = 8;   // words of a span's entry in Image::span_sum (kMaxDim used)
+constexpr int kHeavyCap = 256; // deferred spans a block lists per iteration
 // Unit partials are added into the image accumulators as multiples of
 // 2^-24; a partial must stay below 2^38 in magnitude (a unit holds at most
 // 8192 pixels, so |x - c| below 3e7 everywhere).  Beyond it the call reports
@@ -262,9 +263,14 @@ struct Smem {
   alignas(16) float cent[kMaxK * 8];
   float acc[kWarps][kMaxK * kMaxDim];
   int cnt[kWarps][kMaxK];
-  // the unit's single-candidate spans, in fixed point (added as integers)
+  // the sums of the spans processed since the last flush, in fixed point
+  // (each span's converted on its own, then added as integers)
   long long fix[kMaxK * kMaxDim];
   int fixn[kMaxK];
+  // spans deferred to the second pass of an iteration (see kmeans_kernel)
+  int heavy[kHeavyCap];
+  int nheavy;
+  int next_heavy;
   float lut[256];
   int next[2];
   int more;
@@ -412,6 +418,31 @@ __device__ __forceinline__ void flush_acc(Smem& sm, int warp, int l, const float
   if (lane == 0) sm.cnt[warp][l] += c;
 }
 
+// The end of a span: the warp's FP32 sums (its slots, one per label it met)
+// rounded to fixed point and added into the block's integer sums, the slots
+// cleared.  Each span's sums are converted on their own, so the totals do not
+// depend on which block or pass took the span, nor in what order.
+template <int DIM>
+__device__ __forceinline__ void warp_to_fix(Smem& sm, int warp, int K, int* status) {
+  __syncwarp();   // lane 0's slot updates are visible to the warp
+  for (int k = threadIdx.x & 31; k < K; k += 32) {
+    const int c = sm.cnt[warp][k];
+    if (c == 0) continue;
+    sm.cnt[warp][k] = 0;
+    atomicAdd(&sm.fixn[k], c);
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) {
+      const float v = sm.acc[warp][k * kMaxDim + d];
+      if (v == 0.0f) continue;
+      sm.acc[warp][k * kMaxDim + d] = 0.0f;
+      if (!(fabsf(v) < kFixLimit)) set_status(status, SPLIT_ERR_OVERFLOW);
+      atomicAdd(reinterpret_cast<unsigned long long*>(&sm.fix[k * kMaxDim + d]),
+                (unsigned long long)__float2ll_rn(__fmul_rn(v, kFixScale)));
+    }
+  }
+  __syncwarp();
+}
+
 // Accumulate one batch whose kPx labels are all valid: the same sums, in the
 // same order, as the general path below.
 template <int DIM>
@@ -516,6 +547,21 @@ __device__ __forceinline__ void nearest_pair(const float (&f)[kPx][DIM],
         best[b] = d.y;
         lab[b] = k;
       }
+    }
+  }
+}
+
+// Labels of a whole fast span set to k (lane rows and columns as in a batch).
+__device__ __forceinline__ void write_span_labels(const Image& im, int row_first, int col,
+                                                  int nbatches, int k, bool vec_labels) {
+  const int64_t step = (int64_t)kBatchRows * im.width;
+  int64_t px0 = (int64_t)row_first * im.width + col;
+  for (int b = 0; b < nbatches; ++b, px0 += step) {
+    if (vec_labels) {
+      *reinterpret_cast<int4*>(im.labels + px0) = make_int4(k, k, k, k);
+    } else {
+#pragma unroll
+      for (int j = 0; j < kPx; ++j) im.labels[px0 + j] = k;
     }
   }
 }
@@ -812,18 +858,7 @@ __device__ __forceinline__ void fast_span(const Image& im, Smem& sm, int warp, i
   if (MODE == kCluster && kind == kSpanSingle && entry && it > 0) {
     const int lane = threadIdx.x & 31;
     add_span_sums<DIM>(sm, ka, lane < DIM ? __ldcg(entry + lane) : 0ll, 32 * kPx * nbatches);
-    if (write_labels) {
-      const int64_t step = (int64_t)kBatchRows * im.width;
-      int64_t px0 = (int64_t)row_first * im.width + col;
-      for (int b = 0; b < nbatches; ++b, px0 += step) {
-        if (vec_labels) {
-          *reinterpret_cast<int4*>(im.labels + px0) = make_int4(ka, ka, ka, ka);
-        } else {
-#pragma unroll
-          for (int j = 0; j < kPx; ++j) im.labels[px0 + j] = ka;
-        }
-      }
-    }
+    if (write_labels) write_span_labels(im, row_first, col, nbatches, ka, vec_labels);
     return;
   }
   // with one running label for the whole span the sums switch to it once
@@ -851,28 +886,66 @@ __device__ __forceinline__ void fast_span(const Image& im, Smem& sm, int warp, i
     keep_span_words<LAYOUT, DIM>(im, sm.lut, row_first, col, nbatches, entry);
 }
 
-// Process one unit (a 64 x 64 tile): assign (unless update-only) and
-// accumulate per-warp sums of (x - c_label).  Warp w owns 8 tile rows; a batch
-// is 2 rows x 64 columns, each lane holding kPx consecutive pixels of a row.
+// Whether a warp span takes the fast path: xy features with colour known to
+// lie in [0, 1], the whole span inside the image, and (RGB8) 4-pixel-aligned
+// rows.  It depends only on the geometry and the layout, so a span is fast in
+// every iteration or in none.
+template <int LAYOUT, int DIM, int MODE>
+__device__ __forceinline__ bool fast_geometry(const Image& im, int row0, int col0, int wrows,
+                                              bool vec_labels) {
+  constexpr bool kXY = DIM == 5 && LAYOUT != SPLIT_LAYOUT_PLANAR;
+  const bool unit_box = kXY && (LAYOUT == SPLIT_LAYOUT_RGB8 || im.unit_range);
+  return MODE != kUpdateOnly && unit_box && row0 + wrows <= im.height &&
+         col0 + kTile <= im.width &&
+         (LAYOUT == SPLIT_LAYOUT_FLOAT4 ||
+          (LAYOUT == SPLIT_LAYOUT_RGB8 && vec_labels &&
+           (reinterpret_cast<uintptr_t>(im.points) & 3) == 0));
+}
+
+// The candidate mask of a span with xy features and colour in [0, 1]: the
+// box is exact without the pixels.
+template <int DIM>
+__device__ __forceinline__ unsigned long long unit_box_mask(const Image& im, const Smem& sm,
+                                                            int row0, int col0, int rows_in,
+                                                            int cols_in) {
+  float lo[DIM], hi[DIM];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    lo[d] = 0.0f;
+    hi[d] = 1.0f;
+  }
+  lo[DIM == 5 ? 3 : 0] = __fmul_rn(im.xy_scale, (float)col0);
+  hi[DIM == 5 ? 3 : 0] = __fmul_rn(im.xy_scale, (float)(col0 + cols_in - 1));
+  lo[DIM == 5 ? 4 : 0] = __fmul_rn(im.xy_scale, (float)row0);
+  hi[DIM == 5 ? 4 : 0] = __fmul_rn(im.xy_scale, (float)(row0 + rows_in - 1));
+  return candidates<DIM>(lo, hi, sm.cent, im.K);
+}
+
+// One warp span: rows srow * wrows .. + wrows of tile column tx (wrows =
+// unit_rows / kWarps; a unit, a 64-column tile of unit_rows rows, is the
+// spans of its kWarps warps): assign (unless update-only) and accumulate the
+// calling warp's sums of (x - c_label).  A batch is 2 rows x 64 columns, each
+// lane holding kPx consecutive pixels of a row.
 //
 // Candidate clusters: with xy features and colour features known to lie in
-// [0, 1] the box of the warp's 8 x 64 span is exact without touching the
-// pixels, so one candidate mask serves all its batches.  Otherwise the colour
-// box of every batch is measured (warp min / max) and joined with the batch's
-// xy extent.
+// [0, 1] the box of the warp's span is exact without touching the pixels, so
+// one candidate mask serves all its batches.  Otherwise the colour box of
+// every batch is measured (warp min / max) and joined with the batch's xy
+// extent.
 //
 // While consecutive batches carry one label, every lane keeps a register
 // running sum; a batch with several labels is reduced label by label in
-// ascending order.  All orders depend only on the data.
+// ascending order.  All orders depend only on the data.  The span's sums end
+// in the block's integer sums (warp_to_fix).
 template <int LAYOUT, int DIM, int MODE>
-__device__ void process_unit(const Image& im, int unit, Smem& sm, bool write_labels, int it) {
+__device__ void process_span(const Image& im, int srow, int tx, Smem& sm, bool write_labels,
+                             int it, int* status) {
   const unsigned full = 0xffffffffu;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   constexpr int CS = cstride(DIM);
   constexpr bool kXY = DIM == 5 && LAYOUT != SPLIT_LAYOUT_PLANAR;
   const int wrows = im.unit_rows / kWarps;
-  const int ty = unit / im.ntx, tx = unit - ty * im.ntx;
-  const int row0 = ty * im.unit_rows + warp * wrows;
+  const int row0 = srow * wrows;
   const int col0 = tx * kTile;
   if (row0 >= im.height) return;
   const int lrow = lane / kLanesPerRow, lcol = (lane % kLanesPerRow) * kPx;
@@ -882,43 +955,28 @@ __device__ void process_unit(const Image& im, int unit, Smem& sm, bool write_lab
   const bool vec_labels =
       (reinterpret_cast<uintptr_t>(MODE == kUpdateOnly ? im.labels_in : im.labels) & 15) == 0 &&
       (im.width % kPx) == 0;
+  // float4 features: any width (labels stored one by one where a row's
+  // start is not 16-byte aligned); RGB8 read as 32-bit words needs
+  // 4-pixel-aligned rows
+  const bool fast = fast_geometry<LAYOUT, DIM, MODE>(im, row0, col0, wrows, vec_labels);
+  // slot (srow, tx) of a fast span's kept sums
+  long long* entry = (fast && MODE == kCluster && im.span_sum)
+                         ? im.span_sum + ((size_t)srow * im.span_cols + tx) * kSpanSums
+                         : nullptr;
 
   unsigned long long span_mask = 0;
-  if (MODE != kUpdateOnly && unit_box) {
-    float lo[DIM], hi[DIM];
-#pragma unroll
-    for (int d = 0; d < 3; ++d) {
-      lo[d] = 0.0f;
-      hi[d] = 1.0f;
-    }
-    lo[3] = __fmul_rn(im.xy_scale, (float)col0);
-    hi[3] = __fmul_rn(im.xy_scale, (float)(col0 + cols_in - 1));
-    lo[4] = __fmul_rn(im.xy_scale, (float)row0);
-    hi[4] = __fmul_rn(im.xy_scale, (float)(row0 + rows_in - 1));
-    span_mask = candidates<DIM>(lo, hi, sm.cent, im.K);
-  }
+  if (MODE != kUpdateOnly && unit_box)
+    span_mask = unit_box_mask<DIM>(im, sm, row0, col0, rows_in, cols_in);
 
   int acc_l = -1, acc_n = 0;
   float acc[DIM];
 #pragma unroll
   for (int d = 0; d < DIM; ++d) acc[d] = 0.0f;
 
-  // float4 features: any width (labels stored one by one where a row's
-  // start is not 16-byte aligned); RGB8 read as 32-bit words needs
-  // 4-pixel-aligned rows
-  const bool fast = MODE != kUpdateOnly && unit_box && rows_in == wrows && cols_in == kTile &&
-                    (LAYOUT == SPLIT_LAYOUT_FLOAT4 ||
-                     (LAYOUT == SPLIT_LAYOUT_RGB8 && vec_labels &&
-                      (reinterpret_cast<uintptr_t>(im.points) & 3) == 0));
-  if (fast) {
-    // a fast span lies wholly inside the image: slot (row0 / wrows, tx)
-    long long* entry = (MODE == kCluster && im.span_sum)
-                           ? im.span_sum + ((size_t)(row0 / wrows) * im.span_cols + tx) * kSpanSums
-                           : nullptr;
+  if (fast)
     fast_span<LAYOUT, DIM, MODE>(im, sm, warp, row0 + lrow, col0 + lcol, wrows / kBatchRows,
                                  span_mask, write_labels, vec_labels, acc_l, acc_n, acc, entry,
                                  it);
-  }
   for (int b = 0; !fast && b < wrows / kBatchRows; ++b) {
     if (b * kBatchRows >= rows_in) break;
     const int row = row0 + b * kBatchRows + lrow;
@@ -1047,43 +1105,31 @@ __device__ void process_unit(const Image& im, int unit, Smem& sm, bool write_lab
       }
     }
   }
-  if (MODE != kAssignOnly && acc_l >= 0) flush_acc<DIM>(sm, warp, acc_l, acc, acc_n);
+  if (MODE != kAssignOnly) {
+    if (acc_l >= 0) flush_acc<DIM>(sm, warp, acc_l, acc, acc_n);
+    warp_to_fix<DIM>(sm, warp, im.K, status);
+  }
 }
 
-// Sums the block's 8 warp slots in warp order (the unit partial), clears
-// them, and adds the partial into the image accumulators (96-bit fixed point:
-// low 32 bits and the signed rest in two 64-bit words).
+// Adds the block's integer sums into the image accumulators (96-bit fixed
+// point: low 32 bits and the signed rest in two 64-bit words) and clears
+// them.
 __device__ void block_to_accum(Smem& sm, const Params& p, int img, int K, int dim, int slot) {
   __syncthreads();
   unsigned long long* lo = p.acc_lo + acc_slot(p, slot, img) * (kMaxK * kMaxDim);
   unsigned long long* hi = p.acc_hi + acc_slot(p, slot, img) * (kMaxK * kMaxDim);
   for (int idx = threadIdx.x; idx < K * kMaxDim; idx += blockDim.x) {
-    float s = 0.0f;
-#pragma unroll
-    for (int w = 0; w < kWarps; ++w) {
-      s = __fadd_rn(s, sm.acc[w][idx]);
-      sm.acc[w][idx] = 0.0f;
-    }
-    // plus the single spans' exact words
-    long long q = sm.fix[idx];
+    const long long q = sm.fix[idx];
+    if (q == 0) continue;
     sm.fix[idx] = 0;
-    if ((idx % kMaxDim) < dim && s != 0.0f) {
-      if (!(fabsf(s) < kFixLimit)) set_status(&p.hdr->status, SPLIT_ERR_OVERFLOW);
-      q += __float2ll_rn(__fmul_rn(s, kFixScale));
-    }
-    if ((idx % kMaxDim) < dim && q != 0) {
+    if ((idx % kMaxDim) < dim) {
       atomicAdd(lo + idx, (unsigned long long)q & 0xffffffffull);
       atomicAdd(hi + idx, (unsigned long long)(q >> 32));
     }
   }
   for (int k = threadIdx.x; k < K; k += blockDim.x) {
-    int c = sm.fixn[k];
+    const int c = sm.fixn[k];
     sm.fixn[k] = 0;
-#pragma unroll
-    for (int w = 0; w < kWarps; ++w) {
-      c += sm.cnt[w][k];
-      sm.cnt[w][k] = 0;
-    }
     if (c) atomicAdd(p.acc_cnt + acc_slot(p, slot, img) * kMaxK + k, (unsigned)c);
   }
 }
@@ -1248,6 +1294,97 @@ __device__ bool form_centroids(const Params& p, int img, const Image& im, int i,
   return more;
 }
 
+// An iteration after the first of a single image whose fast spans' sums are
+// kept, by spans instead of units.  Most spans then need none of their pixels
+// (one candidate: labels and sums known), so the block takes its share of
+// spans, s = blockIdx.x + j * gridDim.x with warp w taking j = w, w + kWarps,
+// ... (odd iterations in reverse order, starting on what the last one left
+// in L2), finishes those at once and lists the others; its warps then take
+// the listed spans one at a time.  No block barrier per span, and the block's
+// integer sums go to the image accumulators once.  Each span's contribution
+// is the same as in the unit loop, so the result is too.
+template <int LAYOUT, int DIM, int MODE>
+__device__ void span_iteration(const Params& p, Smem& sm, int it) {
+  constexpr unsigned full = 0xffffffffu;
+  const Image& im = p.img0;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int wrows = im.unit_rows / kWarps;
+  const int nspans = ((im.height + wrows - 1) / wrows) * im.ntx;
+  const bool wl = im.threshold >= 0.0f || it == im.max_iter - 1;
+  int* status = &p.hdr->status;
+  if (threadIdx.x == 0) {
+    sm.nheavy = 0;
+    sm.next_heavy = 0;
+  }
+  __syncthreads();
+  const int rows = wrows / kBatchRows;
+  const int lrow = lane / kLanesPerRow, lcol = (lane % kLanesPerRow) * kPx;
+  const bool vec_labels = (reinterpret_cast<uintptr_t>(im.labels) & 15) == 0 && (im.width % kPx) == 0;
+  // Groups of up to kGroup of the warp's spans: classify each (candidates
+  // from the geometry alone), then one round of loads brings every light
+  // span's kept words (lane g * DIM + d: span g, dimension d).
+  constexpr int kGroup = 32 / DIM < 6 ? 32 / DIM : 6;
+  for (int j0 = warp;; j0 += kGroup * kWarps) {
+    int s_lane = -1, k_lane = -1;   // lane g: light span g and its cluster
+    int g = 0;
+    for (; g < kGroup; ++g) {
+      const int64_t s64 = (int64_t)blockIdx.x + (int64_t)(j0 + g * kWarps) * gridDim.x;
+      if (s64 >= nspans) break;
+      const int s = (it & 1) ? nspans - 1 - (int)s64 : (int)s64;
+      const int sr = s / im.ntx, tx = s - sr * im.ntx;
+      int k = -1;
+      if (fast_geometry<LAYOUT, DIM, MODE>(im, sr * wrows, tx * kTile, wrows, vec_labels)) {
+        const unsigned long long m =
+            unit_box_mask<DIM>(im, sm, sr * wrows, tx * kTile, wrows, kTile);
+        if (m != 0ull && (m & (m - 1ull)) == 0ull) k = __ffsll((long long)m) - 1;
+      }
+      if (k >= 0) {
+        if (lane == g) {
+          s_lane = s;
+          k_lane = k;
+        }
+        if (wl) write_span_labels(im, sr * wrows + lrow, tx * kTile + lcol, rows, k, vec_labels);
+        continue;
+      }
+      int slot = 0;
+      if (lane == 0) slot = atomicAdd(&sm.nheavy, 1);
+      slot = __shfl_sync(full, slot, 0);
+      if (slot < kHeavyCap) {
+        if (lane == 0) sm.heavy[slot] = s;
+      } else {
+        // the list is full: this one now
+        process_span<LAYOUT, DIM, MODE>(im, sr, tx, sm, wl, it, status);
+      }
+    }
+    const int gs = lane / DIM, d = lane - gs * DIM;
+    const int s = __shfl_sync(full, s_lane, gs < kGroup ? gs : 0);
+    const int k = __shfl_sync(full, k_lane, gs < kGroup ? gs : 0);
+    if (gs < kGroup && s >= 0) {
+      const int sr = s / im.ntx;
+      const long long w =
+          __ldcg(im.span_sum + ((size_t)sr * im.span_cols + (s - sr * im.ntx)) * kSpanSums + d);
+      const double nc = __dmul_rn((double)(wrows * kTile),
+                                  __dmul_rn((double)sm.cent[k * cstride(DIM) + d], 16777216.0));
+      atomicAdd(reinterpret_cast<unsigned long long*>(&sm.fix[k * kMaxDim + d]),
+                (unsigned long long)(w - __double2ll_rn(nc)));
+    }
+    if (lane < kGroup && s_lane >= 0) atomicAdd(&sm.fixn[k_lane], wrows * kTile);
+    if (g < kGroup) break;
+  }
+  __syncthreads();
+  const int nh = min(sm.nheavy, kHeavyCap);
+  for (;;) {
+    int idx = 0;
+    if (lane == 0) idx = atomicAdd(&sm.next_heavy, 1);
+    idx = __shfl_sync(full, idx, 0);
+    if (idx >= nh) break;
+    const int s = sm.heavy[idx];
+    const int sr = s / im.ntx;
+    process_span<LAYOUT, DIM, MODE>(im, sr, s - sr * im.ntx, sm, wl, it, status);
+  }
+  block_to_accum(sm, p, 0, im.K, DIM, it % 3);
+}
+
 template <int LAYOUT, int DIM, int MODE>
 __global__ void __launch_bounds__(kThreads, SG_KM_MINBLOCKS) kmeans_kernel(Params p) {
   __shared__ Smem sm;
@@ -1286,6 +1423,11 @@ __global__ void __launch_bounds__(kThreads, SG_KM_MINBLOCKS) kmeans_kernel(Param
         if (!grid_barrier(p.hdr, p.wait_limit, p.wait_skip)) return;
       }
     }
+    if (MODE == kCluster && p.nimages == 1 && it > 0 && p.img0.span_sum) {
+      span_iteration<LAYOUT, DIM, MODE>(p, sm, it);
+      if (!grid_barrier(p.hdr, p.wait_limit, p.wait_skip)) return;
+      continue;
+    }
     // The first wave is static (block b takes unit b): only later fetches go
     // through the work counter, so blocks do not queue on it as they start.
     int raw = (int)blockIdx.x;
@@ -1313,7 +1455,9 @@ __global__ void __launch_bounds__(kThreads, SG_KM_MINBLOCKS) kmeans_kernel(Param
         const int lu = u - im.unit_begin;
         const bool wl = (MODE == kAssignOnly) ||
                         (MODE == kCluster && (im.threshold >= 0.0f || it == im.max_iter - 1));
-        process_unit<LAYOUT, DIM, MODE>(im, lu, sm, wl, it);
+        const int ty = lu / im.ntx;
+        process_span<LAYOUT, DIM, MODE>(im, ty * kWarps + (int)(threadIdx.x >> 5),
+                                        lu - ty * im.ntx, sm, wl, it, &p.hdr->status);
         if (MODE != kAssignOnly) block_to_accum(sm, p, img, im.K, DIM, it % 3);
       }
       // the last warp fetches the next unit (slot k & 1 was last read before
