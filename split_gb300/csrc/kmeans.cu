@@ -2038,9 +2038,17 @@ BatchCounts batch_counts(const KmBatchImage* imgs, int n, bool tuned_rows) {
 using kmb::BatchCounts;
 using kmb::batch_counts;
 
+// Kept span sums of a batch's images (those clustered more than once).
+static int64_t batch_span_slots(const KmBatchImage* imgs, int nimages) {
+  int64_t t = 0;
+  for (int i = 0; i < nimages; ++i)
+    if (imgs[i].iters > 1) t += km::span_slots(imgs[i].npoints, imgs[i].width);
+  return t;
+}
+
 size_t kmeans_batch_workspace(const KmBatchImage* imgs, int nimages) {
   (void)batch_counts;
-  return km::carve(nullptr, nimages > 1 ? nimages : 2).bytes;
+  return km::carve(nullptr, nimages > 1 ? nimages : 2, batch_span_slots(imgs, nimages)).bytes;
 }
 
 int kmeans_batch_prepare(const KmBatchImage* imgs, int nimages, int layout, int dim,
@@ -2058,7 +2066,11 @@ int kmeans_batch_prepare(const KmBatchImage* imgs, int nimages, int layout, int 
   Layout l = carve(nullptr, slots);
   if (!ws || ws_bytes < l.bytes || (reinterpret_cast<uintptr_t>(ws) & 255))
     return SPLIT_ERR_WORKSPACE;
-  l = carve(ws, slots);
+  // the images' kept span sums, where the workspace holds them
+  const int64_t span_total = batch_span_slots(imgs, nimages);
+  const bool keep = span_total > 0 && ws_bytes >= carve(nullptr, slots, span_total).bytes;
+  l = carve(ws, slots, keep ? span_total : 0);
+  int64_t span_off = 0;
   std::vector<Image> host(nimages);
   int ub = 0, max_iter = 0;
   int64_t total_px = 0;
@@ -2085,6 +2097,11 @@ int kmeans_batch_prepare(const KmBatchImage* imgs, int nimages, int layout, int 
     total_px += b.npoints;
     im.height = height_of(b.npoints, b.width);
     im.ntx = tiles_x(b.width);
+    im.span_cols = b.width / kTile;
+    if (keep && b.iters > 1) {
+      im.span_sum = l.span_sum + span_off * kSpanSums;
+      span_off += span_slots(b.npoints, b.width);
+    }
     ub += im.nunits;
     max_iter = max_iter > b.iters ? max_iter : b.iters;
   }

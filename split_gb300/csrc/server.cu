@@ -171,10 +171,11 @@ struct Flight {
 };
 
 // Device bytes one pixel of a batch holds: the arenas (RGB8, two label
-// planes, normals) plus the batch workspace of a 1024 x 1024 probe image,
-// per pixel, rounded up.
+// planes, normals) plus the batch workspace of a 1024 x 1024 probe image
+// clustered more than once (so that it keeps span sums), per pixel, rounded
+// up.
 size_t bytes_per_pixel(const split_pipeline_params& p) {
-  split_batch_image im{1024, 1024, 64, 1};
+  split_batch_image im{1024, 1024, 64, 2};
   split_batch* b = nullptr;
   if (split_batch_create(&im, 1, &p, &b) != SPLIT_OK) return 0;
   const size_t ws = split_batch_workspace_size(b);
@@ -422,10 +423,12 @@ extern "C" int split_server_reserve(split_server* s, int64_t pixels, int max_req
   std::unique_lock<std::mutex> lk(s->mu);
   if (s->nflights > 0 || !s->adm.waiting.empty() || !s->adm.admitted.empty())
     return SPLIT_ERR_INVALID;   // only while the server is idle
-  // a batch of `pixels` in one image gives the workspace bound; every image
-  // of a batch may add a 64-pixel granule of arena
+  // a batch of `pixels` in one image, clustered more than once, gives the
+  // workspace bound (its kept span sums, pixels / 128 spans, bound those of
+  // any images of the same total); every image of a batch may add a
+  // 64-pixel granule of arena
   const int side = 8192;
-  split_batch_image im{side, (int)((pixels + side - 1) / side), 64, 1};
+  split_batch_image im{side, (int)((pixels + side - 1) / side) + 2, 64, 2};
   split_batch* b = nullptr;
   SG_TRY(split_batch_create(&im, 1, &s->cfg.params, &b));
   const size_t wsb = split_batch_workspace_size(b);
