@@ -585,7 +585,9 @@ int split_server_admission_test(const int64_t* footprints, const int64_t* pixels
 typedef struct {
   int64_t max_pixels;        /* upper bound of the class (entries ascending) */
   int kmeans_unit_rows;      /* 16, 32, 64 or 128: rows of a k-means unit    */
-  int kmeans_blocks_per_sm;  /* 0 = as many as fit, else 1..8 (capped)       */
+  int kmeans_blocks_per_sm;  /* 0 = as many as fit, else 1..8 (capped);
+                                single-image clustering only (batches run
+                                as many as fit)                           */
 } split_tune_entry;
 
 /* Replaces the table (n = 0 restores the defaults).  Rejects unsorted

@@ -40,9 +40,16 @@
 namespace sg {
 namespace km {
 
+// Resident blocks per SM the register budget is set for.  Single images: 2
+// (up to 128 registers a thread) keeps the span passes free of spills; at 3
+// (80 registers) they spill, and small images, whose iterations are
+// latency-bound, lose more than the extra occupancy gives.  Batches (many
+// small images through the unit loop): 3, where the extra resident blocks
+// hide more latency than the spills cost.
 #ifndef SG_KM_MINBLOCKS
-#define SG_KM_MINBLOCKS 3
+#define SG_KM_MINBLOCKS 2
 #endif
+constexpr int kBatchMinBlocks = 3;
 constexpr int kThreads = 256;
 constexpr int kWarps = kThreads / 32;
 // A unit is a tile of unit_rows x kTile pixels (unit_rows = 16 to 128, per
@@ -1300,7 +1307,8 @@ __device__ bool form_centroids(const Params& p, int img, const Image& im, int i,
 // spans, s = blockIdx.x + j * gridDim.x with warp w taking j = w, w + kWarps,
 // ... (odd iterations in reverse order, starting on what the last one left
 // in L2), finishes those at once and lists the others; its warps then take
-// the listed spans one at a time.  No block barrier per span, and the block's
+// the listed spans one at a time (with at most one span per warp, a warp
+// does its span at once).  No block barrier per span, and the block's
 // integer sums go to the image accumulators once.  Each span's contribution
 // is the same as in the unit loop, so the result is too.
 template <int LAYOUT, int DIM, int MODE>
@@ -1324,6 +1332,9 @@ __device__ void span_iteration(const Params& p, Smem& sm, int it) {
   // from the geometry alone), then one round of loads brings every light
   // span's kept words (lane g * DIM + d: span g, dimension d).
   constexpr int kGroup = 32 / DIM < 6 ? 32 / DIM : 6;
+  // with at most one span per warp (small images) nothing is gained by
+  // deferring: a warp does its span at once
+  const bool defer = nspans > (int)gridDim.x * kWarps;
   for (int j0 = warp;; j0 += kGroup * kWarps) {
     int s_lane = -1, k_lane = -1;   // lane g: light span g and its cluster
     int g = 0;
@@ -1346,15 +1357,17 @@ __device__ void span_iteration(const Params& p, Smem& sm, int it) {
         if (wl) write_span_labels(im, sr * wrows + lrow, tx * kTile + lcol, rows, k, vec_labels);
         continue;
       }
-      int slot = 0;
-      if (lane == 0) slot = atomicAdd(&sm.nheavy, 1);
-      slot = __shfl_sync(full, slot, 0);
-      if (slot < kHeavyCap) {
-        if (lane == 0) sm.heavy[slot] = s;
-      } else {
-        // the list is full: this one now
-        process_span<LAYOUT, DIM, MODE>(im, sr, tx, sm, wl, it, status);
+      if (defer) {
+        int slot = 0;
+        if (lane == 0) slot = atomicAdd(&sm.nheavy, 1);
+        slot = __shfl_sync(full, slot, 0);
+        if (slot < kHeavyCap) {
+          if (lane == 0) sm.heavy[slot] = s;
+          continue;
+        }
       }
+      // not deferred, or the list is full: this one now
+      process_span<LAYOUT, DIM, MODE>(im, sr, tx, sm, wl, it, status);
     }
     const int gs = lane / DIM, d = lane - gs * DIM;
     const int s = __shfl_sync(full, s_lane, gs < kGroup ? gs : 0);
@@ -1385,8 +1398,11 @@ __device__ void span_iteration(const Params& p, Smem& sm, int it) {
   block_to_accum(sm, p, 0, im.K, DIM, it % 3);
 }
 
-template <int LAYOUT, int DIM, int MODE>
-__global__ void __launch_bounds__(kThreads, SG_KM_MINBLOCKS) kmeans_kernel(Params p) {
+// BATCH: the instance for multi-image launches (no span iterations: a
+// batch's images go through the unit loop).
+template <int LAYOUT, int DIM, int MODE, bool BATCH = false>
+__global__ void __launch_bounds__(kThreads, BATCH ? kBatchMinBlocks : SG_KM_MINBLOCKS)
+    kmeans_kernel(Params p) {
   __shared__ Smem sm;
   for (int i = threadIdx.x; i < kWarps * kMaxK * kMaxDim; i += blockDim.x)
     (&sm.acc[0][0])[i] = 0.0f;
@@ -1423,10 +1439,12 @@ __global__ void __launch_bounds__(kThreads, SG_KM_MINBLOCKS) kmeans_kernel(Param
         if (!grid_barrier(p.hdr, p.wait_limit, p.wait_skip)) return;
       }
     }
-    if (MODE == kCluster && p.nimages == 1 && it > 0 && p.img0.span_sum) {
-      span_iteration<LAYOUT, DIM, MODE>(p, sm, it);
-      if (!grid_barrier(p.hdr, p.wait_limit, p.wait_skip)) return;
-      continue;
+    if constexpr (MODE == kCluster && !BATCH) {
+      if (p.nimages == 1 && it > 0 && p.img0.span_sum) {
+        span_iteration<LAYOUT, DIM, MODE>(p, sm, it);
+        if (!grid_barrier(p.hdr, p.wait_limit, p.wait_skip)) return;
+        continue;
+      }
     }
     // The first wave is static (block b takes unit b): only later fetches go
     // through the work counter, so blocks do not queue on it as they start.
@@ -1644,7 +1662,9 @@ static int stage_attributes() {
       (const void*)kmeans_kernel<SPLIT_LAYOUT_FLOAT4, 3, kUpdateOnly>,
       (const void*)kmeans_kernel<SPLIT_LAYOUT_FLOAT4, 5, kUpdateOnly>,
       (const void*)kmeans_kernel<SPLIT_LAYOUT_FLOAT4, 3, kAssignOnly>,
-      (const void*)kmeans_kernel<SPLIT_LAYOUT_FLOAT4, 5, kAssignOnly>};
+      (const void*)kmeans_kernel<SPLIT_LAYOUT_FLOAT4, 5, kAssignOnly>,
+      (const void*)kmeans_kernel<SPLIT_LAYOUT_FLOAT4, 3, kCluster, true>,
+      (const void*)kmeans_kernel<SPLIT_LAYOUT_FLOAT4, 5, kCluster, true>};
   for (const void* k : kerns)
     SG_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)kStageBytes));
@@ -1657,6 +1677,8 @@ static int launch(Params& p, cudaStream_t st) {
   DeviceInfo di;
   SG_TRY(device_info(&di));
   auto kern = kmeans_kernel<LAYOUT, DIM, MODE>;
+  if constexpr (MODE == kCluster)
+    if (p.images) kern = kmeans_kernel<LAYOUT, DIM, MODE, true>;   // a batch
   const size_t dyn = LAYOUT == SPLIT_LAYOUT_FLOAT4 ? kStageBytes : 0;
   if (dyn) SG_TRY(stage_attributes());
   int per_sm = 0;
@@ -2114,7 +2136,10 @@ int kmeans_batch_prepare(const KmBatchImage* imgs, int nimages, int layout, int 
   plan->max_iter = max_iter;
   plan->layout = layout;
   plan->dim = dim;
-  plan->blocks_per_sm = tuned(total_px).kmeans_blocks_per_sm;
+  // the tuning table's residency is measured on single images, whose kernel
+  // instance differs: a batch runs as many blocks as fit
+  (void)total_px;
+  plan->blocks_per_sm = 0;
   return SPLIT_OK;
 }
 
