@@ -97,9 +97,14 @@ int split_workspace_status(void* workspace, void* stream, int* out_status);
 /* ======================================================================== */
 
 /* Replaces split::device::kmeans::cluster_workspace
- * (split/include/split/device/kmeans/cluster.cuh:46-47).  Points are
- * processed in 64 x 64 pixel tiles of the image; without the width this
- * bound covers any width (the tile count peaks at width 1). */
+ * (split/include/split/device/kmeans/cluster.cuh:46-47).  The workspace holds
+ * the clustering state (about 21 KB) and, for images at least 64 pixels wide,
+ * the exact feature sums of 64-column spans kept from the first iteration
+ * (64 bytes per span, about 0.5 byte per pixel), which let later iterations
+ * skip the pixels of spans with a single candidate cluster.  Without the
+ * width the bound covers any width.  A smaller workspace (at least the state)
+ * is accepted: the call then reads every pixel in every iteration, with the
+ * same results. */
 size_t split_kmeans_cluster_workspace_size(int64_t npoints, int nclusters,
                                            int dim);
 /* The same for a known image width (what the call's `width` will be). */
