@@ -613,3 +613,49 @@ def test_merge_every_pixel_its_own_segment(cuda, shape, policy):
     ccl.merge_small_segments(None, g2, ws, 24, policy=0)
     ws.check("merge after")
     assert np.array_equal(g2.cpu().numpy(), oracle.merge_small(seg, 24, 0))
+
+
+@pytest.mark.parametrize("layout", [1, 2])
+def test_kmeans_kept_span_sums_change_nothing(cuda, layout):
+    """The span sums kept from the first iteration are the same integers as
+    freshly summed ones: a workspace with room for them, one without (the
+    clustering state only), and a reused workspace that last held another
+    image's sums all give bit-identical labels and centroids."""
+    import torch
+    from split_gb300 import _native, kmeans
+    from split_gb300._util import Workspace
+    lib = _native.load()
+    w, h, k, iters = 640, 480, 16, 8
+    rgb = synth.voronoi_rgb8(19, w, h, 96, npalette=16, sigma=3.0)
+    other = synth.voronoi_rgb8(20, w, h, 40, npalette=8, sigma=5.0)
+    c0 = synth.pick_centroids(19, rgb, k, 5)
+    n = w * h
+
+    def points(img):
+        if layout == 2:
+            return _t(img.reshape(-1, 3), cuda)
+        f4 = np.zeros((n, 4), np.float32)
+        f4[:, :3] = synth.features(img, 3).T
+        return _t(f4, cuda)
+
+    lay = layout | (kmeans.UNIT_RANGE if layout == 1 else 0)
+    full = Workspace(lib.split_kmeans_cluster_workspace_size_2d(n, w, k, 5), cuda)
+    small = Workspace(lib.split_kmeans_assign_workspace_size(n, k), cuda)
+    assert small.nbytes < full.nbytes
+    def run(ws, img):
+        # through the C ABI: the Python wrapper would replace a small workspace
+        pts = points(img)
+        cent = _t(c0, cuda)
+        lab = torch.empty(n, dtype=torch.int32, device=cuda)
+        _native.check(lib.split_kmeans_cluster(pts.data_ptr(), lay, 5, n, w, 0.1,
+                                               cent.data_ptr(), k, lab.data_ptr(), ws.ptr,
+                                               ws.nbytes, iters, -1.0, None, None), "cluster")
+        torch.cuda.synchronize()
+        ws.check("kmeans")
+        return lab.cpu().numpy(), cent.cpu().numpy()
+
+    out = [run(full, rgb), run(small, rgb)]
+    run(full, other)            # leave another image's sums in the workspace
+    out.append(run(full, rgb))
+    for lab, cent in out[1:]:
+        assert np.array_equal(lab, out[0][0]) and np.array_equal(cent, out[0][1])
