@@ -181,6 +181,44 @@ __device__ __forceinline__ bool grid_barrier(WsHeader* h, unsigned limit = kSpin
   return ok != 0;
 }
 
+// Device-wide barrier on a counter that only grows within a launch (the
+// launch's setup zeroes it): the k-th barrier (k from 1) is passed when the
+// counter reaches k * nblocks, and waiters poll the counter itself, so the
+// last arrival releases everyone without a second word to publish.  Limits,
+// the skipping block and the timeout status as in grid_barrier.
+__device__ __forceinline__ bool grid_barrier_counted(WsHeader* h, unsigned k,
+                                                     unsigned limit = kSpinLimit,
+                                                     int skip = -1) {
+  __syncthreads();
+  __shared__ int ok;
+  if (threadIdx.x == 0) {
+    cuda::atomic_ref<unsigned, cuda::thread_scope_device> cnt(h->barrier_count);
+    const unsigned target = k * (gridDim.x * gridDim.y * gridDim.z);
+    ok = 1;
+    if (skip == (int)blockIdx.x) {
+      ok = 0;
+    } else {
+      // acq_rel: publish this block's writes, observe the others' on release
+      unsigned v = cnt.fetch_add(1, cuda::memory_order_acq_rel) + 1u;
+      unsigned spins = 0;
+      while ((int)(v - target) < 0) {
+        if (++spins > limit) {
+          set_status(&h->status, SPLIT_ERR_TIMEOUT);
+          ok = 0;
+          break;
+        }
+        __nanosleep(64);
+        v = cnt.load(cuda::memory_order_acquire);
+      }
+    }
+    if (cuda::atomic_ref<int, cuda::thread_scope_device>(h->status).load(
+            cuda::memory_order_relaxed) == SPLIT_ERR_TIMEOUT)
+      ok = 0;
+  }
+  __syncthreads();
+  return ok != 0;
+}
+
 __device__ __forceinline__ int warp_lane() { return threadIdx.x & 31; }
 
 }  // namespace sg

@@ -1414,6 +1414,7 @@ __global__ void __launch_bounds__(kThreads, BATCH ? kBatchMinBlocks : SG_KM_MINB
   __syncthreads();
 
   bool stopped = false;   // a single image that converged: no iterations left
+  unsigned nbar = 0;      // grid barriers passed (every block passes the same ones)
   for (int it = 0; it < p.max_iter; ++it) {
     if (blockIdx.x == 0 && threadIdx.x == 0) p.hdr->work_counter[(it + 1) & 1] = 0;
     int cached = -1;
@@ -1436,13 +1437,13 @@ __global__ void __launch_bounds__(kThreads, BATCH ? kBatchMinBlocks : SG_KM_MINB
         for (int img = (int)blockIdx.x; img < p.nimages; img += gridDim.x)
           form_centroids<LAYOUT, DIM, MODE>(p, img, image_of(p, img), it, sm.cent, true,
                                             sm.lut);
-        if (!grid_barrier(p.hdr, p.wait_limit, p.wait_skip)) return;
+        if (!grid_barrier_counted(p.hdr, ++nbar, p.wait_limit, p.wait_skip)) return;
       }
     }
     if constexpr (MODE == kCluster && !BATCH) {
       if (p.nimages == 1 && it > 0 && p.img0.span_sum) {
         span_iteration<LAYOUT, DIM, MODE>(p, sm, it);
-        if (!grid_barrier(p.hdr, p.wait_limit, p.wait_skip)) return;
+        if (!grid_barrier_counted(p.hdr, ++nbar, p.wait_limit, p.wait_skip)) return;
         continue;
       }
     }
@@ -1497,7 +1498,7 @@ __global__ void __launch_bounds__(kThreads, BATCH ? kBatchMinBlocks : SG_KM_MINB
     if (MODE == kAssignOnly) return;
     // the barrier publishes every block's sums (fire-and-forget adds ordered
     // by the block barrier before the arrival's release)
-    if (!grid_barrier(p.hdr, p.wait_limit, p.wait_skip)) return;
+    if (!grid_barrier_counted(p.hdr, ++nbar, p.wait_limit, p.wait_skip)) return;
   }
   if (MODE == kAssignOnly || stopped) return;
   // centroids after the last iteration; every image stops here
