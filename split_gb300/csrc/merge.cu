@@ -387,12 +387,12 @@ __device__ void resolve_dec_phase(const Layout& L, const int32_t* sizes, int P, 
 // bounded grid barrier and the round count is bounded.
 __device__ void overflow_path(const Layout& L, const int32_t* lab, const Geoms& gs,
                               const int32_t* sizes, int P, int policy,
-                              unsigned long long stamp) {
+                              unsigned long long stamp, unsigned& nbar) {
   WsHeader* h = L.hdr;
   State* st = L.state;
   const bool lead = blockIdx.x == 0 && threadIdx.x == 0;
   clear_table(L);
-  if (!grid_barrier(h)) return;
+  if (!grid_barrier_counted(h, ++nbar)) return;
   if (lead) {
     st->list_count = 0;
     st->overflow = 0;
@@ -401,7 +401,7 @@ __device__ void overflow_path(const Layout& L, const int32_t* lab, const Geoms& 
     L.stack[1] = 1, L.stack[2] = 1;
     L.stack[3] = 1, L.stack[4] = 0;
   }
-  if (!grid_barrier(h)) return;
+  if (!grid_barrier_counted(h, ++nbar)) return;
   __shared__ int lev, cls;
   for (unsigned round = 0;; ++round) {
     if (threadIdx.x == 0) {
@@ -413,16 +413,16 @@ __device__ void overflow_path(const Layout& L, const int32_t* lab, const Geoms& 
     if (lev < 0) break;   // the same decision in every block
     for (int t = blockIdx.x; t < gs.total_tiles; t += gridDim.x)
       pair_tile<true>(lab, gs, L, sizes, P, t, lev, (unsigned)cls, &h->status);
-    if (!grid_barrier(h)) return;
+    if (!grid_barrier_counted(h, ++nbar)) return;
     const bool split = *(volatile int*)&st->overflow != 0;
     if (!split) {
       bid_phase(L, sizes, policy);
-      if (!grid_barrier(h)) return;
+      if (!grid_barrier_counted(h, ++nbar)) return;
       decide_list_phase(L, policy);
-      if (!grid_barrier(h)) return;
+      if (!grid_barrier_counted(h, ++nbar)) return;
     }
     clear_table(L);
-    if (!grid_barrier(h)) return;
+    if (!grid_barrier_counted(h, ++nbar)) return;
     if (lead) {
       int depth = L.stack[0] - 1;   // pop (lev, cls)
       if (split) {
@@ -440,12 +440,12 @@ __device__ void overflow_path(const Layout& L, const int32_t* lab, const Geoms& 
       st->overflow = 0;
       if (round + 1 >= kRoundCap) set_status(&h->status, SPLIT_ERR_NOT_CONVERGED);
     }
-    if (!grid_barrier(h)) return;
+    if (!grid_barrier_counted(h, ++nbar)) return;
   }
   cycle_dec_phase(L, sizes, P);
-  if (!grid_barrier(h)) return;
+  if (!grid_barrier_counted(h, ++nbar)) return;
   resolve_dec_phase(L, sizes, P, &h->status);
-  if (!grid_barrier(h)) return;
+  if (!grid_barrier_counted(h, ++nbar)) return;
   const unsigned cnt = *(volatile unsigned*)&st->dec_count;
   for (unsigned j = blockIdx.x * blockDim.x + threadIdx.x; j < cnt; j += gridDim.x * blockDim.x)
     L.best[L.dec[j]] = 0ull;
@@ -460,18 +460,20 @@ __global__ void __launch_bounds__(kThreads)
 list_kernel(Layout L, const int32_t* lab, Geoms gs, const int32_t* sizes, int P, int policy,
             unsigned long long stamp) {
   WsHeader* h = L.hdr;
+  // grid barriers passed (the guard zeroed the counter they count on)
+  unsigned nbar = 0;
   if (*(volatile int*)&L.state->overflow) {   // set before this launch: the same in every block
-    overflow_path(L, lab, gs, sizes, P, policy, stamp);
+    overflow_path(L, lab, gs, sizes, P, policy, stamp, nbar);
     return;
   }
   bid_phase(L, sizes, policy);
-  if (!grid_barrier(h)) return;
+  if (!grid_barrier_counted(h, ++nbar)) return;
   decide_phase(L, policy);
-  if (!grid_barrier(h)) return;
+  if (!grid_barrier_counted(h, ++nbar)) return;
   cycle_phase(L, sizes, P, policy);
-  if (!grid_barrier(h)) return;
+  if (!grid_barrier_counted(h, ++nbar)) return;
   resolve_phase(L, sizes, P, policy, &h->status);
-  if (!grid_barrier(h)) return;
+  if (!grid_barrier_counted(h, ++nbar)) return;
   cleanup_phase(L);
   if (blockIdx.x == 0 && threadIdx.x == 0) h->stamp = stamp;
 }
