@@ -8,23 +8,30 @@
 //
 // Work decomposition (fixed per image, so a result never depends on what else
 // shares the launch): an image is cut into units (tiles of 16, 32, 64 or 128
-// rows by 64 columns); blocks take units from a device work counter.  Per unit, every
-// warp accumulates (x - c_label) over its pixel batches in FP32 registers and
-// a warp-private shared-memory slot (warp butterfly sums per distinct label),
-// and the block sums the 8 warp slots in warp order: the unit partial, a
-// fixed-shape FP32 sum.  Unit partials are added into per-image accumulators
-// exactly: each is rounded to a multiple of 2^-24 and added as a 96-bit
-// fixed-point integer (64-bit atomics on a low and a high word).  Integer
-// addition does not depend on order, so the image total is the same whatever
-// order units finish in and whatever else shares the launch.  A unit ends with
-// fire-and-forget adds and one block barrier: no fence, no arrival counter.
-// The grid barrier that ends the iteration publishes the sums; then c_new =
-// c + S / n is formed in FP32 from the exact sum (form_centroids): for a single
-// image by every block from the same inputs (bit-identical), block 0
-// publishing it; in a batch by one owner block per image, published before a
-// second grid barrier.  The sums are
-// kept in three slots by iteration, so the owner can clear the slot of the
-// iteration after next while the current slot fills and the last one is read.
+// rows by 64 columns), a unit into warp spans (each warp's rows of it).
+// Every warp accumulates (x - c_label) over its span's pixel batches in FP32
+// registers and a warp-private shared-memory slot (warp butterfly sums per
+// distinct label); at the end of the span the slots are rounded to multiples
+// of 2^-24 and added, as integers, into the block's shared sums
+// (warp_to_fix).  A span whose candidate mask names one cluster adds the
+// exact integer sum of its pixels' features instead (add_span_sums).  The
+// block adds its integer sums into per-image accumulators as 96-bit fixed
+// point (64-bit atomics on a low and a high word).  Integer addition does not
+// depend on order, so the image total is the same whatever blocks took which
+// spans and whatever else shares the launch.
+//
+// Iterations: the first (and every iteration of a batch, of a workspace
+// without room for kept sums) goes by units taken from a device work counter.
+// The first iteration keeps every fast span's exact feature sum; later
+// iterations of a single image go by spans (span_iteration), where a span
+// with one candidate needs none of its pixels.  The grid barrier that ends
+// the iteration publishes the sums; then c_new = c + S / n is formed in FP32
+// from the exact sum (form_centroids): for a single image by every block from
+// the same inputs (bit-identical), block 0 publishing it; in a batch by one
+// owner block per image, published before a second grid barrier.  The sums
+// are kept in three slots by iteration, so the owner can clear the slot of
+// the iteration after next while the current slot fills and the last one is
+// read.
 #include <limits.h>
 #include <math.h>
 #include <string.h>
