@@ -67,10 +67,10 @@ constexpr int kMaxK = 64;
 constexpr int kMaxDim = 5;
 constexpr int kSpanSums = 8;   // words of a span's entry in Image::span_sum (kMaxDim used)
 constexpr int kHeavyCap = 256; // deferred spans a block lists per iteration
-// Unit partials are added into the image accumulators as multiples of
-// 2^-24; a partial must stay below 2^38 in magnitude (a unit holds at most
-// 8192 pixels, so |x - c| below 3e7 everywhere).  Beyond it the call reports
-// SPLIT_ERR_OVERFLOW.
+// Span sums are added into the image accumulators as multiples of 2^-24; a
+// span's FP32 sum must stay below 2^38 in magnitude (a span holds at most
+// 1024 pixels, so |x - c| below 2.6e8 everywhere).  Beyond it the call
+// reports SPLIT_ERR_OVERFLOW.
 constexpr float kFixScale = 16777216.0f;   // 2^24
 constexpr float kFixLimit = 274877906944.0f;   // 2^38
 
