@@ -643,7 +643,9 @@ enum SpanKind { kSpanSingle = 0, kSpanPair = 1, kSpanAny = 2 };
 // however often the two labels mix within its batches.
 //
 // A single-candidate span of a clustering adds its pixels' exact feature
-// words instead of running FP32 sums, and keeps them in `entry` (if any).
+// words instead of running FP32 sums, and keeps them in `entry` (if any);
+// any other span given an `entry` (the first iteration's) also sums and keeps
+// its words, besides its FP32 sums.
 template <int LAYOUT, int DIM, int MODE, int KIND>
 __device__ __forceinline__ void span_batches(const Image& im, Smem& sm, int warp, int row_first,
                                              int col, int nbatches, unsigned long long mask,
@@ -652,6 +654,8 @@ __device__ __forceinline__ void span_batches(const Image& im, Smem& sm, int warp
                                              long long* entry) {
   constexpr int CS = cstride(DIM);
   constexpr bool kFixSingle = KIND == kSpanSingle && MODE == kCluster;
+  // the first iteration also keeps the words of spans with several candidates
+  const bool keep = MODE == kCluster && KIND != kSpanSingle && entry != nullptr;
   long long qc[3] = {0, 0, 0};
   const int64_t step = (int64_t)kBatchRows * im.width;
   int64_t px0 = (int64_t)row_first * im.width + col;
@@ -734,7 +738,7 @@ __device__ __forceinline__ void span_batches(const Image& im, Smem& sm, int warp
         f[j][4] = fy;
       }
     }
-    if (kFixSingle) {
+    if (kFixSingle || keep) {
 #pragma unroll
       for (int j = 0; j < kPx; ++j)
 #pragma unroll
@@ -787,50 +791,13 @@ __device__ __forceinline__ void span_batches(const Image& im, Smem& sm, int warp
   }
   // the second candidate's sums (the first's stay running)
   if (MODE != kAssignOnly && KIND == kSpanPair) flush_acc<DIM>(sm, warp, kb, acc2, acc2_n);
-  if (kFixSingle) {
+  if (kFixSingle || keep) {
     const long long w = span_words<DIM>(qc, fx, im.xy_scale, row_first, nbatches);
     if (entry && (threadIdx.x & 31) < DIM) __stcg(entry + (threadIdx.x & 31), w);
-    add_span_sums<DIM>(sm, ka, w, 32 * kPx * nbatches);
+    if (kFixSingle) add_span_sums<DIM>(sm, ka, w, 32 * kPx * nbatches);
   }
 }
 
-// The exact feature words of a fast span into `entry`, read from the pixels
-// (in the first iteration, for spans with more than one candidate: they may
-// have a single one later).
-template <int LAYOUT, int DIM>
-__device__ __forceinline__ void keep_span_words(const Image& im, const float* lut, int row_first,
-                                             int col, int nbatches, long long* entry) {
-  long long qc[3] = {0, 0, 0};
-  float fx[kPx];
-#pragma unroll
-  for (int j = 0; j < kPx; ++j) fx[j] = __fmul_rn(im.xy_scale, (float)(col + j));
-  const int64_t step = (int64_t)kBatchRows * im.width;
-  int64_t px0 = (int64_t)row_first * im.width + col;
-  for (int b = 0; b < nbatches; ++b, px0 += step) {
-    float f[kPx][3];
-    if (LAYOUT == SPLIT_LAYOUT_FLOAT4) {
-#pragma unroll
-      for (int j = 0; j < kPx; ++j) {
-        const float4 v = __ldg(static_cast<const float4*>(im.points) + px0 + j);
-        f[j][0] = v.x;
-        f[j][1] = v.y;
-        f[j][2] = v.z;
-      }
-    } else {
-      const uint8_t* p = static_cast<const uint8_t*>(im.points) + 3 * px0;
-#pragma unroll
-      for (int j = 0; j < kPx; ++j)
-#pragma unroll
-        for (int c = 0; c < 3; ++c) f[j][c] = lut[__ldg(p + 3 * j + c)];
-    }
-#pragma unroll
-    for (int j = 0; j < kPx; ++j)
-#pragma unroll
-      for (int c = 0; c < 3; ++c) qc[c] += __float2int_rn(__fmul_rn(f[j][c], kFixScale));
-  }
-  const long long w = span_words<DIM>(qc, fx, im.xy_scale, row_first, nbatches);
-  if ((threadIdx.x & 31) < DIM) __stcg(entry + (threadIdx.x & 31), w);
-}
 
 // A warp span that lies wholly inside the image, with packed features (float4,
 // or RGB8 read as three 32-bit words per 4 pixels) and a candidate mask known
@@ -891,13 +858,11 @@ __device__ __forceinline__ void fast_span(const Image& im, Smem& sm, int warp, i
   else if (kind == kSpanPair)
     span_batches<LAYOUT, DIM, MODE, kSpanPair>(im, sm, warp, row_first, col, nbatches, mask, ka,
                                                kb, write_labels, vec_labels, acc_l, acc_n, acc,
-                                               entry);
+                                               it == 0 ? entry : nullptr);
   else
     span_batches<LAYOUT, DIM, MODE, kSpanAny>(im, sm, warp, row_first, col, nbatches, mask, ka,
                                               kb, write_labels, vec_labels, acc_l, acc_n, acc,
-                                              entry);
-  if (MODE == kCluster && kind != kSpanSingle && entry && it == 0)
-    keep_span_words<LAYOUT, DIM>(im, sm.lut, row_first, col, nbatches, entry);
+                                              it == 0 ? entry : nullptr);
 }
 
 // Whether a warp span takes the fast path: xy features with colour known to
