@@ -55,6 +55,12 @@ def test_workspace_queries():
     assert lib.split_compress_labels_workspace_size(3840 * 2160) < 4 * 3840 * 2160 // 8
     p = _native.PipelineParams(16, 5, 0.1, 20, -1.0, 1, 8, 0, 256, 0, 1, 1, 1.0)
     assert lib.split_pipeline_workspace_size(3840, 2160, C.byref(p)) > 0
+    # the kept span sums of a clustering: about 0.5 B per pixel on top of the
+    # state, which one assignment does not need
+    state = lib.split_kmeans_assign_workspace_size(3840 * 2160, 16)
+    assert 0.4 * 3840 * 2160 < ws - state < 0.6 * 3840 * 2160
+    assert lib.split_kmeans_cluster_workspace_size_2d(3840 * 2160, 3840, 16, 5) >= \
+        lib.split_kmeans_cluster_workspace_size_2d(1920 * 1080, 1920, 16, 5)
     # more than 64 clusters: the many-cluster k-means, with its own workspace
     many = _native.PipelineParams(1000, 5, 0.1, 20, -1.0, 1, 8, 0, 256, 0, 1, 1, 1.0)
     assert lib.split_pipeline_workspace_size(3840, 2160, C.byref(many)) > 0
@@ -72,6 +78,18 @@ def test_invalid_arguments_rejected_on_host():
     assert lib.split_erode(None, None, 4, 4, 1, None) == _native.ERR_INVALID
     assert lib.split_kmeans_cluster(None, 0, 3, 10, 1, 0.1, None, 4, None, None, 0, 1, -1.0,
                                     None, None) == _native.ERR_INVALID
+    # the many-cluster path checks its arguments the same way (pointers that
+    # are never dereferenced: every case fails before any device call)
+    fake = C.c_void_p(256)
+    big = (1 << 20) + 1
+    assert lib.split_kmeans_assign(fake, 0, 3, 100, 10, 0.1, fake, big, fake, fake, 1 << 30,
+                                   None) == _native.ERR_INVALID
+    assert lib.split_kmeans_cluster(fake, 0x200, 5, 100, 10, 0.1, fake, 100, fake, fake, 1 << 30,
+                                    5, 1e-3, None, None) == _native.ERR_INVALID   # shift: 3-D only
+    assert lib.split_kmeans_cluster(fake, 0, 4, 100, 10, 0.1, fake, 100, fake, fake, 1 << 30, 5,
+                                    -1.0, None, None) == _native.ERR_INVALID      # D = 3 or 5
+    assert lib.split_kmeans_cluster(fake, 0, 5, 100, 10, 0.1, fake, 100, fake, fake, 64, 5, -1.0,
+                                    None, None) == _native.ERR_WORKSPACE
 
 
 def test_synth_deterministic():
