@@ -876,7 +876,12 @@ def main():
     roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "traffic": profiled_traffic(),
                 "kernel": "kmeans_kernel (cooperative, 20 iterations)",
-                "algorithmic_bytes_per_launch": km_bytes, "peak_source": peak_kind}
+                "algorithmic_bytes_per_launch": km_bytes, "peak_source": peak_kind,
+                "bytes_note": "algorithmic bytes of the reference's algorithm (every pixel's "
+                              "16 B features in every iteration, plus the labels); after the "
+                              "first iteration the kernel reads only the pixels of spans with "
+                              "more than one candidate cluster, so its DRAM traffic (ncu) is "
+                              "far below them"}
 
     batched = None
     if not args.no_batch and args.batch_images > 0:
