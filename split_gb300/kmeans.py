@@ -72,7 +72,9 @@ def cluster(points: torch.Tensor, centroids: torch.Tensor, labels: torch.Tensor,
     with ``dim`` 3 or 5 (5 adds xy_scale * (column, row) for image ``width``).
     centroids (dim, K) float32 is updated in place; labels (N,) int32 receives
     the final assignment.  Exactly ``max_iter`` iterations when threshold < 0.
-    Returns the workspace used (pass it back in to reuse it).
+    K from 1 to 2**20: up to 64 in one persistent launch, more through the
+    many-cluster path.  Returns the workspace used (pass it back in to reuse
+    it).
     """
     n, d = _features(points, layout, dim)
     width = default_width(n) if width is None else width
@@ -94,7 +96,9 @@ def cluster(points: torch.Tensor, centroids: torch.Tensor, labels: torch.Tensor,
 def label_points(centroids: torch.Tensor, points: torch.Tensor, labels: torch.Tensor,
                  temp: Workspace | None = None, *, layout: int = PLANAR, dim: int | None = None,
                  width: int | None = None, xy_scale: float = 0.1, stream=None) -> Workspace:
-    """split::device::kmeans::label_points (label.cuh:27-31, label.cu:74-106)."""
+    """split::device::kmeans::label_points (label.cuh:27-31, label.cu:74-106):
+    nearest centroid by the reference's squared distance, ties to the lowest
+    index; K from 1 to 2**20."""
     n, d = _features(points, layout, dim)
     width = default_width(n) if width is None else width
     require_cuda(centroids, "centroids", torch.float32)
