@@ -7,8 +7,8 @@ device system, through the CUSP container subset in oracle/cusp_shim, and
 links them with oracle/ref_driver.cpp into oracle/_ref/libsplitref.so.
 
 The reference sources are read from REF_ROOT (the SPLIT_REF_ROOT environment
-variable, else the "reference_path" recorded in the repository's
-the benchmark spec) and copied into the git-ignored oracle/_ref/src, where two mechanical edits are
+variable, else /root/reference, where this recipe's build machine mounts the
+reference read-only) and copied into the git-ignored oracle/_ref/src, where two mechanical edits are
 applied to the copies (the reference itself is never modified and nothing of
 it is committed):
   1. member ``x.get<N>()`` becomes ``thrust::get<N>(x)``: CCCL 3's
@@ -35,17 +35,12 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 
 
 def _reference_root() -> str:
-    """SPLIT_REF_ROOT, else BASELINE.json's reference_path; "" when neither
-    names one (the staged copies are then compiled as they are)."""
+    """SPLIT_REF_ROOT, else the read-only mount /root/reference if present; ""
+    otherwise (the staged copies are then compiled as they are)."""
     env = os.environ.get("SPLIT_REF_ROOT")
     if env:
         return env
-    try:
-        import json
-        with open(os.path.join(os.path.dirname(HERE), "BASELINE.json")) as f:
-            return str(json.load(f).get("reference_path", ""))
-    except (OSError, ValueError):
-        return ""
+    return "/root/reference" if os.path.isdir("/root/reference") else ""
 
 
 REF_ROOT = _reference_root()
